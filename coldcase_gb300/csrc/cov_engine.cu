@@ -1,0 +1,1721 @@
+// cov_engine.cu -- GB300 (sm_103a) tabu engine for q-ary covering codes.
+//
+// The search is the reference engine's p5b trajectory
+// (cov/engine/covsearch2e.c:1304-1580, `--preset p5b`, no --wide): the same
+// RNG stream, candidate order, tie-breaking, tabu and kick rules, so every
+// committed move and every delta equals the reference's.  What differs is how
+// a move's delta is obtained:
+//
+//   * the reference walks, for every candidate codeword c, the whole
+//     distance-R sphere around c to count T = #{w : d(w,c)=R, cnt[w]=1} and
+//     H_j (covsearch2e.c:592-654), i.e. C(n,R)(q-1)^R gathers per candidate;
+//   * here those counts are kept per codeword in P[k] = (T_k, H_k[0..n-1])
+//     and updated incrementally: a word's count crosses 1 only inside a
+//     commit or a kick, and when cnt[w] == 1 the covering codeword is named
+//     by the xor of covering ids stored beside cnt.  Only the moved
+//     codeword's sphere is walked again.  pos_p = T_k - H_k[p] exactly as in
+//     covsearch2e.c:755-758.
+//   * the entering side (neg) is read off the uncovered-word list as in
+//     covsearch2e.c:720-734, or by the per-position walk of :735-753 while
+//     the list is not valid.
+//
+// Execution: one thread-block cluster per search instance ("slot").  The
+// leader CTA (rank 0) runs the serial, RNG-ordered part of each iteration;
+// every CTA of the cluster shares the commit and the sphere walks.  Plan and
+// reductions travel through distributed shared memory; the CTAs meet at
+// hardware cluster barriers, so there is no software spin-wait anywhere in
+// the engine.  Each launch is bounded by a move budget, an op-count guard and
+// a wall-clock deadline read from %globaltimer.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include <cooperative_groups.h>
+#include "cov_common.cuh"
+#include "../../include/covgpu.h"
+
+namespace cg = cooperative_groups;
+
+#define NT        512          // threads per CTA
+#define NWARP     (NT / 32)
+#define PERM_CAP  4096         // candidates kept in shared memory
+#define L_SM      256          // candidate codewords kept in shared memory
+#define RB        1024         // RNG outputs generated per batch
+#define UL_CAP_DEFAULT (1 << 20)
+
+enum { OP_STOP = 0, OP_MOVE, OP_NEGWALK, OP_BALL, OP_RECOMPUTE, OP_ZERO_TABU, OP_REBUILD_UL };
+enum {
+    PH_PLAN = 0, PH_SELECT, PH_FINISH_MOVE, PH_KICK_START, PH_KICK_PICK, PH_KICK_RECOMP,
+    PH_KICK_END, PH_KICK_DONE, PH_REBUILD_DONE, PH_GREEDY, PH_GREEDY_NEXT, PH_STOPPED
+};
+enum { MODE_SEARCH = 0, MODE_GREEDY = 1 };
+
+// Parameters of the op the leader broadcasts to the cluster.
+struct OpParams {
+    int op;
+    int mi, mp, mv;            // codeword, position, value
+    int sgn;                   // BALL: +1 / -1
+    int ul_valid;
+    uint32_t base, dv, basen;  // word index before / offset / after
+    uint64_t pc, pcn, pu;      // packed codeword before / after, target word
+    int nL, dtar;
+    int L_sm, neg_sm;          // list / neg arrays live in the leader's smem
+};
+
+struct Smem {
+    CovSlot slot;              // this CTA's copy of the slot descriptor
+    OpParams opp;              // written by the leader
+    OpParams opl;              // each CTA's local copy
+    // leader accumulators (targets of DSMEM atomics)
+    unsigned long long dunc;
+    int accT;
+    int accH[COV_MAXN];
+    // per-CTA partials
+    int partT;
+    int partH[COV_MAXN];
+    // leader state
+    CovRng rng;
+    long long it, unc, best_unc, since_improve, nkicks, moves_left, target, trace_n;
+    long long chosen_delta;
+    unsigned long long t_deadline;
+    long long guard;
+    int ul_valid, status, phase, kick_t, finished, greedy_i, mode;
+    int nL, dtar, ncand, take, improved, dokick;
+    uint64_t pu;
+    long long uw;
+    cov_move_rec rec;
+    // scratch
+    int red_i[NWARP];
+    unsigned red_u[NWARP];
+    unsigned long long red_ull[NWARP];
+    int ibc[4];
+    long long lbc[4];
+    unsigned hitmask[2];
+    // arrays
+    uint32_t perm[PERM_CAP];
+    int32_t dval[PERM_CAP];
+    uint8_t tflag[PERM_CAP];
+    uint64_t rbuf[RB];
+    uint32_t L[L_SM];
+    uint64_t Lpk[L_SM];
+    int32_t neg[L_SM * COV_MAXN];
+    uint32_t lbits[L_SM / 32];
+};
+
+// ------------------------------------------------------------ helpers -----
+__device__ __forceinline__ uint32_t widx_pk(const CovSlot &d, uint64_t pk)
+{
+    uint32_t x = 0;
+    for (int j = 0; j < d.n; j++) x += (uint32_t)cov_nib(pk, j) * d.pw[j];
+    return x;
+}
+
+__device__ __forceinline__ uint64_t pk_of_idx(const CovSlot &d, uint32_t x)
+{
+    uint64_t pk = 0;
+    for (int j = d.n - 1; j >= 0; j--) {
+        uint32_t qd = x / (uint32_t)d.q;
+        pk |= (uint64_t)(x - qd * (uint32_t)d.q) << (4 * j);
+        x = qd;
+    }
+    return pk;
+}
+
+__device__ __forceinline__ int cnt_of(const CovSlot &d, uint32_t w)
+{
+    return (int)(cov_ldcg(&d.cw[w]) & 0xffffu);
+}
+
+__device__ __forceinline__ int nth_set_pos(uint64_t spread, int r)
+{
+    for (int k = 0; k < r; k++) spread &= spread - 1;
+    return (__ffsll((long long)spread) - 1) >> 2;
+}
+
+__device__ __forceinline__ uint64_t nibmask(int n)
+{
+    return n >= 16 ? 0x1111111111111111ull : (0x1111111111111111ull & ((1ull << (4 * n)) - 1));
+}
+
+__device__ __forceinline__ void set_error(const CovSlot &d, int code)
+{
+    atomicCAS(&d.st->status, 0, code);
+}
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-wide sum of an int (all threads get the result)
+__device__ int block_sum_int(Smem &S, int v)
+{
+    v = warp_sum(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) S.red_i[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int t = 0;
+    for (int w = 0; w < NWARP; w++) t += S.red_i[w];
+    __syncthreads();
+    return t;
+}
+
+__device__ unsigned block_min_u32(Smem &S, unsigned v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) S.red_u[threadIdx.x >> 5] = v;
+    __syncthreads();
+    unsigned t = 0xffffffffu;
+    for (int w = 0; w < NWARP; w++) t = min(t, S.red_u[w]);
+    __syncthreads();
+    return t;
+}
+
+// exclusive prefix of flag over the block; returns the block total
+__device__ int block_excl_scan(Smem &S, int flag, int &pos)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned m = __ballot_sync(0xffffffffu, flag);
+    int inwarp = __popc(m & ((1u << lane) - 1));
+    __syncthreads();
+    if (lane == 0) S.red_i[wid] = __popc(m);
+    __syncthreads();
+    int before = 0, tot = 0;
+    for (int w = 0; w < NWARP; w++) {
+        if (w < wid) before += S.red_i[w];
+        tot += S.red_i[w];
+    }
+    pos = before + inwarp;
+    __syncthreads();
+    return tot;
+}
+
+// ------------------------------------------------ private-count upkeep -----
+// Word w (packed pkw) just became (s=+1) or stopped being (s=-1) privately
+// covered by codeword k.  If w sits on k's distance-R sphere, T_k and H_k[j]
+// (j in D(w,c_k)) move with it.
+__device__ __forceinline__ void private_adjust(const CovSlot &d, int k, uint64_t pkw, int s)
+{
+    if (k < 0 || k >= d.M) { set_error(d, COV_EDRIFT); return; }
+    uint64_t D = cov_spread(pkw ^ cov_ldcg(&d.code[k]));
+    if (__popcll(D) != d.R) return;
+    int32_t *Pk = d.P + (size_t)k * (d.n + 1);
+    atomicAdd(&Pk[0], s);
+    while (D) {
+        int j = (__ffsll((long long)D) - 1) >> 2;
+        atomicAdd(&Pk[1 + j], s);
+        D &= D - 1;
+    }
+}
+
+__device__ __forceinline__ void ul_insert(const CovSlot &d, int ul_valid, uint32_t x, uint64_t pk)
+{
+    if (!ul_valid) return;
+    uint32_t bit = 1u << (x & 31);
+    uint32_t old = atomicOr(&d.ul_bit[x >> 5], bit);
+    if (old & bit) return;
+    int slot = atomicAdd(&d.st->ul_n, 1);
+    if (slot < d.ul_cap) {
+        cov_stcg(&d.ul_idx[slot], x);
+        cov_stcg(&d.ul_pk[slot], pk);
+    } else {
+        atomicExch(&d.st->ul_n, d.ul_cap + 1);
+    }
+}
+
+// word w loses coverage by codeword i (leaving side of a commit / -1 ball)
+__device__ __forceinline__ long long word_dec(const CovSlot &d, int ul_valid, int i, uint32_t w, uint64_t pk)
+{
+    uint32_t o = cov_ldcg(&d.cw[w]);
+    uint32_t c = o & 0xffffu;
+    if (c == 0) { set_error(d, COV_EDRIFT); return 0; }
+    uint32_t nw = (o - 1u) ^ ((uint32_t)i << 16);
+    cov_stcg(&d.cw[w], nw);
+    if (c == 1) { ul_insert(d, ul_valid, w, pk); return 1; }
+    if (c == 2) private_adjust(d, (int)(nw >> 16), pk, +1);
+    return 0;
+}
+
+// word w gains coverage by codeword i (entering side / +1 ball)
+__device__ __forceinline__ long long word_inc(const CovSlot &d, int i, uint32_t w, uint64_t pk)
+{
+    uint32_t o = cov_ldcg(&d.cw[w]);
+    uint32_t c = o & 0xffffu;
+    if (c == 0xffffu) { set_error(d, COV_EDRIFT); return 0; }
+    uint32_t nw = (o + 1u) ^ ((uint32_t)i << 16);
+    cov_stcg(&d.cw[w], nw);
+    if (c == 0) return -1;
+    if (c == 1) private_adjust(d, (int)(o >> 16), pk, -1);
+    return 0;
+}
+
+// ------------------------------------------------------ cluster ops --------
+__device__ __forceinline__ uint32_t sphere_items(const CovSlot &d, int r, int nsubs)
+{
+    return r == 0 ? 1u : (uint32_t)nsubs * d.ppow[r - 1];
+}
+
+// Commit of move (i: p -> v): covsearch2e.c:450-493 (mode 1), 562-590.
+__device__ void op_commit(const CovSlot &d, const OpParams &P, Smem *LS, int rank, int csize)
+{
+    const int R = d.R;
+    const uint8_t *subp = d.sub + (size_t)P.mp * d.nsub * d.rs;
+    const uint32_t nit = sphere_items(d, R, d.nsub);
+    long long dunc = 0;
+    const uint32_t stride = (uint32_t)csize * NT;
+    for (uint32_t t = (uint32_t)rank * NT + threadIdx.x; t < nit; t += stride) {
+        if (R == 0) {
+            dunc += word_dec(d, P.ul_valid, P.mi, P.base, P.pc);
+            dunc += word_inc(d, P.mi, P.base + P.dv, cov_setnib(P.pc, P.mp, P.mv));
+        } else {
+            CovItem it = cov_item(d, subp, R, t, P.base, P.pc);
+            for (int kk = 0; kk < d.q - 1; kk++) {
+                uint32_t a; uint64_t pka;
+                cov_item_word(d, it, kk, a, pka);
+                dunc += word_dec(d, P.ul_valid, P.mi, a, pka);
+                dunc += word_inc(d, P.mi, a + P.dv, cov_setnib(pka, P.mp, P.mv));
+            }
+        }
+    }
+    dunc = warp_sum(dunc);
+    if ((threadIdx.x & 31) == 0 && dunc != 0) atomicAdd(&LS->dunc, (unsigned long long)dunc);
+}
+
+// T and H of the codeword with packed digits pc at word index base: one
+// walk of its distance-R sphere (covsearch2e.c:621-650, read side only).
+__device__ void op_recompute(const CovSlot &d, uint32_t base, uint64_t pc, Smem &S, Smem *LS,
+                             int rank, int csize)
+{
+    const int R = d.R;
+    if (threadIdx.x == 0) S.partT = 0;
+    if (threadIdx.x < COV_MAXN) S.partH[threadIdx.x] = 0;
+    __syncthreads();
+    const uint8_t *fs = d.ball_sub + (size_t)d.ball_off[R] * d.rs;
+    const uint32_t nit = sphere_items(d, R, d.nfsub);
+    const uint32_t stride = (uint32_t)csize * NT;
+    int T = 0;
+    for (uint32_t t = (uint32_t)rank * NT + threadIdx.x; t < nit; t += stride) {
+        if (R == 0) {
+            T += (cnt_of(d, base) == 1);
+        } else {
+            CovItem it = cov_item(d, fs, R, t, base, pc);
+            int t1 = 0;
+            for (int kk = 0; kk < d.q - 1; kk++) {
+                uint32_t w; uint64_t pk;
+                cov_item_word(d, it, kk, w, pk);
+                t1 += (cnt_of(d, w) == 1);
+            }
+            if (t1) {
+                T += t1;
+                for (int s = 0; s < R; s++) atomicAdd(&S.partH[it.ps[s]], t1);
+            }
+        }
+    }
+    T = warp_sum(T);
+    if ((threadIdx.x & 31) == 0 && T) atomicAdd(&S.partT, T);
+    __syncthreads();
+    if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
+    if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
+}
+
+// +1 / -1 over the whole radius-R ball of codeword i: covsearch2e.c:353-380
+__device__ void op_ball(const CovSlot &d, const OpParams &P, Smem *LS, int rank, int csize)
+{
+    const int R = d.R;
+    uint32_t cum[COV_MAXN + 2];
+    cum[0] = 1;   // the centre
+    for (int r = 1; r <= R; r++)
+        cum[r] = cum[r - 1] + sphere_items(d, r, d.ball_off[r + 1] - d.ball_off[r]);
+    const uint32_t nit = cum[R];
+    const uint32_t stride = (uint32_t)csize * NT;
+    long long dunc = 0;
+    for (uint32_t t = (uint32_t)rank * NT + threadIdx.x; t < nit; t += stride) {
+        if (t == 0) {
+            if (P.sgn < 0) dunc += word_dec(d, P.ul_valid, P.mi, P.base, P.pc);
+            else dunc += word_inc(d, P.mi, P.base, P.pc);
+            continue;
+        }
+        int r = 1;
+        while (t >= cum[r]) r++;
+        const uint8_t *subs = d.ball_sub + (size_t)d.ball_off[r] * d.rs;
+        CovItem it = cov_item(d, subs, r, t - cum[r - 1], P.base, P.pc);
+        for (int kk = 0; kk < d.q - 1; kk++) {
+            uint32_t w; uint64_t pk;
+            cov_item_word(d, it, kk, w, pk);
+            if (P.sgn < 0) dunc += word_dec(d, P.ul_valid, P.mi, w, pk);
+            else dunc += word_inc(d, P.mi, w, pk);
+        }
+    }
+    dunc = warp_sum(dunc);
+    if ((threadIdx.x & 31) == 0 && dunc != 0) atomicAdd(&LS->dunc, (unsigned long long)dunc);
+}
+
+// Entering-side counts by walking, used while the uncovered list is not
+// valid: covsearch2e.c:656-683, 735-753.
+__device__ void op_negwalk(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank,
+                           int csize, cg::cluster_group &cl)
+{
+    const int R = d.R;
+    const uint32_t *Lp = P.L_sm ? cl.map_shared_rank(S.L, 0) : d.g_list;
+    int32_t *negp = P.neg_sm ? cl.map_shared_rank(S.neg, 0) : d.g_neg;
+    const uint32_t nit = sphere_items(d, R, d.nsub);
+    const unsigned long long per_l = (unsigned long long)P.dtar * nit;
+    const unsigned long long total = per_l * (unsigned long long)P.nL;
+    const unsigned long long stride = (unsigned long long)csize * NT;
+    for (unsigned long long t = (unsigned long long)rank * NT + threadIdx.x; t < total; t += stride) {
+        int l = (int)(t / per_l);
+        unsigned long long rem = t - (unsigned long long)l * per_l;
+        int pi = (int)(rem / nit);
+        uint32_t tt = (uint32_t)(rem - (unsigned long long)pi * nit);
+        int k = P.L_sm ? (int)Lp[l] : (int)cov_ldcg(&Lp[l]);
+        uint64_t pck = cov_ldcg(&d.code[k]);
+        int p = nth_set_pos(cov_spread(pck ^ P.pu), pi);
+        int v = cov_nib(P.pu, p), c = cov_nib(pck, p);
+        uint32_t b0 = widx_pk(d, pck) + (uint32_t)((long long)(v - c) * (long long)d.pw[p]);
+        uint64_t pc2 = cov_setnib(pck, p, v);
+        int nz = 0;
+        if (R == 0) {
+            nz = (cnt_of(d, b0) == 0);
+        } else {
+            const uint8_t *subp = d.sub + (size_t)p * d.nsub * d.rs;
+            CovItem it = cov_item(d, subp, R, tt, b0, pc2);
+            for (int kk = 0; kk < d.q - 1; kk++) {
+                uint32_t w; uint64_t pk;
+                cov_item_word(d, it, kk, w, pk);
+                nz += (cnt_of(d, w) == 0);
+            }
+        }
+        if (nz) atomicAdd(&negp[l * d.n + p], nz);
+    }
+}
+
+__device__ void op_zero_tabu(const CovSlot &d, int rank, int csize)
+{
+    const size_t tot = (size_t)d.M * d.n * d.q;
+    for (size_t x = (size_t)rank * NT + threadIdx.x; x < tot; x += (size_t)csize * NT)
+        cov_stcg(&d.tabu[x], 0);
+}
+
+// rebuild of the uncovered list from cnt (covsearch2e.c:323-338): clear the
+// membership bits, then append every zero-count word.
+__device__ void op_rebuild_ul(const CovSlot &d, int rank, int csize, cg::cluster_group &cl)
+{
+    const uint32_t nb = (d.N + 31) / 32;
+    for (uint32_t x = (uint32_t)rank * NT + threadIdx.x; x < nb; x += (uint32_t)csize * NT)
+        cov_stcg(&d.ul_bit[x], 0u);
+    cl.sync();
+    for (uint32_t x = (uint32_t)rank * NT + threadIdx.x; x < d.N; x += (uint32_t)csize * NT) {
+        if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) ul_insert(d, 1, x, pk_of_idx(d, x));
+    }
+}
+
+// ----------------------------------------------------- leader routines -----
+// pick_uncovered (covsearch2e.c:973-1016, opt_upick = opt_ucache = 0):
+// 64 uniform probes, then the first zero cyclically after a random start.
+// The probes are drawn up front and the RNG is advanced by exactly the
+// number the reference consumes.
+__device__ long long leader_pick(const CovSlot &d, Smem &S)
+{
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        CovRng r = S.rng;
+        for (int t = 0; t < 65; t++) S.rbuf[t] = cov_rng_next(r);
+    }
+    __syncthreads();
+    if (tid < 64) {
+        uint32_t w = (uint32_t)(S.rbuf[tid] % (uint64_t)d.N);
+        unsigned m = __ballot_sync(0xffffffffu, cnt_of(d, w) == 0);
+        if ((tid & 31) == 0) S.hitmask[tid >> 5] = m;
+    }
+    __syncthreads();
+    int first = -1;
+    if (S.hitmask[0]) first = __ffs(S.hitmask[0]) - 1;
+    else if (S.hitmask[1]) first = 32 + __ffs(S.hitmask[1]) - 1;
+    const int consumed = first >= 0 ? first + 1 : 65;
+    long long result = -1;
+    uint32_t start = 0;
+    if (first >= 0) result = (long long)(S.rbuf[first] % (uint64_t)d.N);
+    else start = (uint32_t)(S.rbuf[64] % (uint64_t)d.N);
+    __syncthreads();
+    if (tid == 0) {
+        CovRng r = S.rng;
+        for (int t = 0; t < consumed; t++) cov_rng_next(r);
+        S.rng = r;
+    }
+    if (first >= 0 || S.unc <= 0) return result;     // no zero anywhere: -1
+    if (S.ul_valid) {
+        // every zero-count word is on the list: the first one after start is
+        // the entry minimising (x - start) mod N
+        const int n0 = min(cov_ldcg(&d.st->ul_n), d.ul_cap);
+        unsigned best = 0xffffffffu;
+        for (int e = tid; e < n0; e += NT) {
+            uint32_t x = cov_ldcg(&d.ul_idx[e]);
+            if ((cov_ldcg(&d.cw[x]) & 0xffffu) != 0) continue;
+            unsigned key = x >= start ? x - start : x + (d.N - start);
+            best = min(best, key);
+        }
+        best = block_min_u32(S, best);
+        if (best != 0xffffffffu) {
+            uint32_t x = start + best;
+            if (x >= d.N) x -= d.N;
+            return (long long)x;
+        }
+        if (tid == 0) set_error(d, COV_EDRIFT);
+        return -1;
+    }
+    // chunked linear scan from start
+    for (uint32_t off = 0; off < d.N; off += NT * 4) {
+        unsigned best = 0xffffffffu;
+        for (int k = 0; k < 4; k++) {
+            uint32_t o2 = off + (uint32_t)tid * 4 + k;
+            if (o2 >= d.N) break;
+            uint32_t x = start + o2;
+            if (x >= d.N) x -= d.N;
+            if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) { best = o2; break; }
+        }
+        best = block_min_u32(S, best);
+        if (best != 0xffffffffu) {
+            uint32_t x = start + best;
+            if (x >= d.N) x -= d.N;
+            return (long long)x;
+        }
+    }
+    if (tid == 0) set_error(d, COV_EDRIFT);
+    return -1;
+}
+
+// drop list entries that are covered again (covsearch2e.c:305-320)
+__device__ void leader_compact(const CovSlot &d, Smem &S)
+{
+    const int n0 = min(cov_ldcg(&d.st->ul_n), d.ul_cap);
+    int m = 0;
+    for (int c0 = 0; c0 < n0; c0 += NT) {
+        int e = c0 + threadIdx.x;
+        int keep = 0;
+        uint32_t x = 0; uint64_t pk = 0;
+        if (e < n0) {
+            x = cov_ldcg(&d.ul_idx[e]);
+            pk = cov_ldcg(&d.ul_pk[e]);
+            keep = (cov_ldcg(&d.cw[x]) & 0xffffu) == 0;
+            if (!keep) atomicAnd(&d.ul_bit[x >> 5], ~(1u << (x & 31)));
+        }
+        int pos;
+        int tot = block_excl_scan(S, keep, pos);
+        if (keep) { cov_stcg(&d.ul_idx[m + pos], x); cov_stcg(&d.ul_pk[m + pos], pk); }
+        m += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) d.st->ul_n = m;
+    __syncthreads();
+}
+
+__device__ void zero_acc(Smem &S)
+{
+    if (threadIdx.x == 0) { S.dunc = 0; S.accT = 0; }
+    if (threadIdx.x < COV_MAXN) S.accH[threadIdx.x] = 0;
+}
+
+// Plan one iteration up to the point where the entering-side counts are
+// needed.  Returns with S.opp set.
+__device__ void leader_plan(const CovSlot &d, Smem &S)
+{
+    const int tid = threadIdx.x;
+    const int n = d.n, R = d.R, M = d.M;
+    if (tid == 0) {
+        if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
+        int stop = S.status != 0 || S.unc <= 0 || S.moves_left <= 0 ||
+                   (S.target >= 0 && S.best_unc <= S.target) || gtimer() > S.t_deadline;
+        if (!stop && gtimer() > S.t_deadline) S.status = COV_ETIMEOUT;
+        S.ibc[0] = stop;
+        S.ibc[1] = !stop && !S.ul_valid && S.unc <= d.ul_cap / 2;
+    }
+    __syncthreads();
+    if (S.ibc[0]) {
+        if (tid == 0) { S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
+        return;
+    }
+    if (S.ibc[1]) {
+        if (tid == 0) {
+            d.st->ul_n = 0;
+            S.opp.op = OP_REBUILD_UL;
+            S.phase = PH_REBUILD_DONE;
+        }
+        return;
+    }
+    if (S.ul_valid && (long long)cov_ldcg(&d.st->ul_n) > 2 * S.unc + 64) leader_compact(d, S);
+    if (tid == 0) {
+        S.it++;
+        S.moves_left--;
+        memset(&S.rec, 0, sizeof(S.rec));
+        S.rec.it = S.it;
+    }
+    __syncthreads();
+    long long uw = leader_pick(d, S);
+    if (tid == 0) {
+        S.uw = uw;
+        if (uw < 0) S.status = COV_EDRIFT;
+        S.pu = uw >= 0 ? pk_of_idx(d, (uint32_t)uw) : 0;
+        S.rec.u = uw;
+    }
+    __syncthreads();
+    if (S.status) { if (tid == 0) { S.opp.op = OP_STOP; S.phase = PH_STOPPED; } return; }
+    const uint64_t pu = S.pu;
+
+    // distances to all codewords and the target distance (covsearch2e.c:1342-1351)
+    unsigned dm = 0xffffffffu;
+    for (int i = tid; i < M; i += NT) dm = min(dm, (unsigned)cov_dist(cov_ldcg(&d.code[i]), pu));
+    dm = block_min_u32(S, dm);
+    const int dtar = ((int)dm <= R + 1) ? R + 1 : (int)dm;
+    // ordered list of codewords at distance dtar (covsearch2e.c:1359-1376)
+    int cntL = 0;
+    for (int i = tid; i < M; i += NT) cntL += (cov_dist(cov_ldcg(&d.code[i]), pu) == dtar);
+    const int nL = block_sum_int(S, cntL);
+    const int Lsm = nL <= L_SM;
+    uint32_t *Lp = Lsm ? S.L : d.g_list;
+    {
+        int base = 0;
+        for (int c0 = 0; c0 < M; c0 += NT) {
+            int i = c0 + tid;
+            uint64_t pk = 0;
+            int f = 0;
+            if (i < M) { pk = cov_ldcg(&d.code[i]); f = cov_dist(pk, pu) == dtar; }
+            int pos;
+            int tot = block_excl_scan(S, f, pos);
+            if (f) { Lp[base + pos] = (uint32_t)i; if (Lsm) S.Lpk[base + pos] = pk; }
+            base += tot;
+        }
+    }
+    const int ncand = nL * dtar;
+    if (ncand == 0) {     // impossible for an uncovered target word
+        if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
+        return;
+    }
+    const int take = min(ncand, d.cand);
+    const int psm = ncand <= PERM_CAP;
+    uint32_t *perm = psm ? S.perm : d.g_perm;
+    int32_t *dval = psm ? S.dval : d.g_dval;
+    for (int c = tid; c < ncand; c += NT) perm[c] = (uint32_t)c;
+    // Fisher-Yates sample of `take` (covsearch2e.c:1383-1389): the draws are
+    // generated in order by one thread, reduced in parallel, applied in order.
+    for (int s0 = 0; s0 < take; s0 += RB) {
+        const int cnt = min(RB, take - s0);
+        __syncthreads();
+        if (tid == 0) {
+            CovRng r = S.rng;
+            for (int t = 0; t < cnt; t++) S.rbuf[t] = cov_rng_next(r);
+            S.rng = r;
+        }
+        __syncthreads();
+        for (int t = tid; t < cnt; t += NT) {
+            int s = s0 + t;
+            dval[s] = s + (int32_t)(S.rbuf[t] % (uint64_t)(ncand - s));
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < take; s++) {
+            int j = dval[s];
+            uint32_t tmp = perm[s]; perm[s] = perm[j]; perm[j] = tmp;
+        }
+    }
+    __syncthreads();
+    // distinct codewords among the sampled candidates (for the trace)
+    int ncw = nL;
+    if (take < ncand) {
+        int c = 0;
+        if (tid == 0) {
+            // small and rare: a quadratic-free count through the sorted ids
+            for (int s = 0; s < take; s++) {
+                int l = (int)(perm[s] / (uint32_t)dtar), dup = 0;
+                for (int t = 0; t < s; t++) if ((int)(perm[t] / (uint32_t)dtar) == l) { dup = 1; break; }
+                c += !dup;
+            }
+            S.ibc[2] = c;
+        }
+        __syncthreads();
+        ncw = S.ibc[2];
+    }
+    if (tid == 0) {
+        S.nL = nL; S.dtar = dtar; S.ncand = ncand; S.take = take;
+        S.rec.ncand = ncand; S.rec.ncw = ncw;
+    }
+    // entering side
+    const int nsm = nL <= L_SM;
+    int32_t *negp = nsm ? S.neg : d.g_neg;
+    for (int x = tid; x < nL * n; x += NT) negp[x] = 0;
+    zero_acc(S);
+    __syncthreads();
+    if (!S.ul_valid) {
+        if (tid == 0) {
+            OpParams &o = S.opp;
+            o.op = OP_NEGWALK; o.nL = nL; o.dtar = dtar; o.pu = pu;
+            o.L_sm = Lsm; o.neg_sm = nsm; o.ul_valid = 0;
+            S.phase = PH_SELECT;
+        }
+        return;
+    }
+    {
+        // covsearch2e.c:720-734 restricted to v = u_p (the only entries a
+        // non-wide candidate reads)
+        const int n0 = min(cov_ldcg(&d.st->ul_n), d.ul_cap);
+        const uint64_t nm = nibmask(n);
+        for (int e = tid; e < n0; e += NT) {
+            uint32_t x = cov_ldcg(&d.ul_idx[e]);
+            if ((cov_ldcg(&d.cw[x]) & 0xffffu) != 0) continue;
+            uint64_t px = cov_ldcg(&d.ul_pk[e]);
+            uint64_t eq = ~cov_spread(px ^ pu) & nm;
+            for (int l = 0; l < nL; l++) {
+                uint64_t pk = Lsm ? S.Lpk[l] : cov_ldcg(&d.code[Lp[l]]);
+                uint64_t D = cov_spread(px ^ pk);
+                if (__popcll(D) != R + 1) continue;
+                uint64_t m = D & eq;
+                while (m) {
+                    int j = (__ffsll((long long)m) - 1) >> 2;
+                    atomicAdd(&negp[l * n + j], 1);
+                    m &= m - 1;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0) S.phase = PH_SELECT;
+    S.opp.op = -1;   // no op yet: select follows
+}
+
+// Deltas of the sampled candidates and the tabu/aspiration/reservoir
+// selection of covsearch2e.c:1503-1518; emits OP_MOVE.
+__device__ void leader_select(const CovSlot &d, Smem &S)
+{
+    const int tid = threadIdx.x;
+    const int n = d.n, q = d.q;
+    const int nL = S.nL, dtar = S.dtar, ncand = S.ncand, take = S.take;
+    const uint64_t pu = S.pu;
+    const int psm = ncand <= PERM_CAP, Lsm = nL <= L_SM;
+    uint32_t *perm = psm ? S.perm : d.g_perm;
+    int32_t *dval = psm ? S.dval : d.g_dval;
+    uint32_t *Lp = Lsm ? S.L : d.g_list;
+    int32_t *negp = Lsm ? S.neg : d.g_neg;
+    // deltas and tabu flags in parallel (shared-memory case); the rare
+    // oversized case recomputes them inside the serial scan below
+    if (psm) {
+        for (int s = tid; s < take; s += NT) {
+            uint32_t c = perm[s];
+            int l = (int)(c / (uint32_t)dtar), r = (int)(c - (uint32_t)l * dtar);
+            int k = (int)Lp[l];
+            uint64_t pk = Lsm ? S.Lpk[l] : cov_ldcg(&d.code[k]);
+            int p = nth_set_pos(cov_spread(pk ^ pu), r);
+            int v = cov_nib(pu, p);
+            const int32_t *Pk = d.P + (size_t)k * (n + 1);
+            dval[s] = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
+            S.tflag[s] = (uint8_t)((long long)cov_ldcg(&d.tabu[((size_t)k * n + p) * q + v]) > S.it);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        long long bestd = 1LL << 60;
+        int nties = 0, bs = -1;
+        CovRng r = S.rng;
+        for (int s = 0; s < take; s++) {
+            long long dd;
+            int tb;
+            if (psm) { dd = dval[s]; tb = S.tflag[s]; }
+            else {
+                uint32_t c = perm[s];
+                int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
+                int k = (int)Lp[l];
+                uint64_t pk = cov_ldcg(&d.code[k]);
+                int p = nth_set_pos(cov_spread(pk ^ pu), rr);
+                int v = cov_nib(pu, p);
+                const int32_t *Pk = d.P + (size_t)k * (n + 1);
+                dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
+                tb = (long long)cov_ldcg(&d.tabu[((size_t)k * n + p) * q + v]) > S.it;
+            }
+            if (tb && S.unc + dd >= S.best_unc) continue;
+            if (dd < bestd) { bestd = dd; bs = s; nties = 1; }
+            else if (dd == bestd) {
+                nties++;
+                if (cov_rng_next(r) % (uint64_t)nties == 0) bs = s;
+            }
+        }
+        if (bs < 0) bs = (int)(cov_rng_next(r) % (uint64_t)take);
+        S.rng = r;
+        uint32_t c = perm[bs];
+        int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
+        int k = (int)Lp[l];
+        uint64_t pk = cov_ldcg(&d.code[k]);
+        int p = nth_set_pos(cov_spread(pk ^ pu), rr);
+        int v = cov_nib(pu, p);
+        const int32_t *Pk = d.P + (size_t)k * (n + 1);
+        long long dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
+        S.chosen_delta = dd;
+        OpParams &o = S.opp;
+        o.op = OP_MOVE;
+        o.mi = k; o.mp = p; o.mv = v; o.sgn = 0;
+        o.ul_valid = S.ul_valid;
+        o.pc = pk;
+        o.base = widx_pk(d, pk);
+        int oldv = cov_nib(pk, p);
+        o.dv = (uint32_t)((long long)(v - oldv) * (long long)d.pw[p]);
+        o.pcn = cov_setnib(pk, p, v);
+        o.basen = o.base + o.dv;
+        S.ibc[3] = oldv;
+        S.rec.i = k; S.rec.p = p; S.rec.v = v; S.rec.delta = dd;
+        S.phase = PH_FINISH_MOVE;
+    }
+}
+
+__device__ void write_trace(const CovSlot &d, Smem &S)
+{
+    if (d.trace && S.trace_n < d.trace_cap)
+        reinterpret_cast<cov_move_rec *>(d.trace)[S.trace_n] = S.rec;
+    if (d.trace) S.trace_n++;
+}
+
+__device__ void copy_best(const CovSlot &d)
+{
+    for (int i = threadIdx.x; i < d.M; i += NT) cov_stcg(&d.best[i], cov_ldcg(&d.code[i]));
+}
+
+// after OP_MOVE: covsearch2e.c:1525-1553
+__device__ void leader_finish_move(const CovSlot &d, Smem &S)
+{
+    const int tid = threadIdx.x;
+    const int n = d.n, q = d.q;
+    if (tid == 0) {
+        long long dunc = (long long)S.dunc;
+        S.unc += dunc;
+        if (dunc != S.chosen_delta) S.status = COV_EDRIFT;
+        const OpParams &o = S.opp;
+        cov_stcg(&d.code[o.mi], o.pcn);
+        int32_t *Pk = d.P + (size_t)o.mi * (n + 1);
+        cov_stcg(&Pk[0], S.accT);
+        for (int j = 0; j < n; j++) cov_stcg(&Pk[1 + j], S.accH[j]);
+        const int oldv = S.ibc[3];
+        uint64_t r4 = cov_rng_next(S.rng) % 4ull;
+        cov_stcg(&d.tabu[((size_t)o.mi * n + o.mp) * q + oldv], (int32_t)(S.it + d.tenure + (long long)r4));
+        S.rec.unc = S.unc;
+        S.improved = S.unc < S.best_unc;
+        S.dokick = 0;
+        if (S.improved) { S.best_unc = S.unc; S.since_improve = 0; }
+        else if (++S.since_improve > d.stall) S.dokick = 1;
+    }
+    __syncthreads();
+    if (S.improved) copy_best(d);
+    __syncthreads();
+    if (tid == 0) {
+        if (S.dokick) { S.kick_t = 0; S.phase = PH_KICK_START; }
+        else {
+            S.rec.unc_end = S.unc; S.rec.best = S.best_unc;
+            write_trace(d, S);
+            S.phase = PH_PLAN;
+        }
+    }
+    __syncthreads();
+}
+
+// one leader step: consume the result of the previous op, do the serial
+// work, and leave the next op in S.opp
+__device__ void leader_step(const CovSlot &d, Smem &S)
+{
+    const int tid = threadIdx.x;
+    for (int guard = 0; guard < 64; guard++) {
+        __syncthreads();
+        const int ph = S.phase;
+        __syncthreads();
+        if (ph == PH_STOPPED) { if (tid == 0) S.opp.op = OP_STOP; return; }
+        if (ph == PH_PLAN) {
+            if (S.mode == MODE_GREEDY) { if (tid == 0) S.phase = PH_GREEDY; continue; }
+            leader_plan(d, S);
+            __syncthreads();
+            if (S.phase == PH_SELECT && S.opp.op == -1) { leader_select(d, S); __syncthreads(); return; }
+            return;
+        }
+        if (ph == PH_SELECT) { leader_select(d, S); __syncthreads(); return; }
+        if (ph == PH_FINISH_MOVE) { leader_finish_move(d, S); continue; }
+        if (ph == PH_REBUILD_DONE) {
+            if (tid == 0) {
+                int cnt = cov_ldcg(&d.st->ul_n);
+                S.ul_valid = cnt <= d.ul_cap;
+                S.phase = PH_PLAN;
+            }
+            continue;
+        }
+        if (ph == PH_KICK_START) {
+            if (tid == 0) {
+                if (S.kick_t >= d.kick) {
+                    S.opp.op = OP_ZERO_TABU;
+                    S.phase = PH_KICK_DONE;
+                } else {
+                    if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
+                    int i = (int)(cov_rng_next(S.rng) % (uint64_t)d.M);
+                    uint64_t pk = cov_ldcg(&d.code[i]);
+                    OpParams &o = S.opp;
+                    o.op = OP_BALL; o.sgn = -1; o.mi = i; o.pc = pk; o.base = widx_pk(d, pk);
+                    o.ul_valid = S.ul_valid;
+                    S.dunc = 0;
+                    S.phase = PH_KICK_PICK;
+                }
+            }
+            __syncthreads();
+            return;
+        }
+        if (ph == PH_KICK_PICK) {
+            if (tid == 0) {
+                S.unc += (long long)S.dunc;
+                if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
+            }
+            __syncthreads();
+            long long w = leader_pick(d, S);
+            if (tid == 0) {
+                uint64_t pk;
+                if (w >= 0) {
+                    pk = pk_of_idx(d, (uint32_t)w);
+                    for (int t2 = 0; t2 < d.R; t2++) {
+                        // the value's draw precedes the position's draw, as
+                        // the reference binary evaluates covsearch2e.c:1567
+                        int val = (int)(cov_rng_next(S.rng) % (uint64_t)d.q);
+                        int pos = (int)(cov_rng_next(S.rng) % (uint64_t)d.n);
+                        pk = cov_setnib(pk, pos, val);
+                    }
+                } else {
+                    pk = 0;
+                    for (int j = 0; j < d.n; j++)
+                        pk = cov_setnib(pk, j, (int)(cov_rng_next(S.rng) % (uint64_t)d.q));
+                }
+                OpParams &o = S.opp;
+                cov_stcg(&d.code[o.mi], pk);
+                o.op = OP_BALL; o.sgn = +1; o.pc = pk; o.base = widx_pk(d, pk);
+                o.ul_valid = S.ul_valid;
+                S.dunc = 0;
+                S.phase = PH_KICK_RECOMP;
+            }
+            __syncthreads();
+            return;
+        }
+        if (ph == PH_KICK_RECOMP) {
+            if (tid == 0) {
+                S.unc += (long long)S.dunc;
+                OpParams &o = S.opp;
+                o.op = OP_RECOMPUTE;
+                o.basen = o.base; o.pcn = o.pc;
+                S.phase = PH_KICK_END;
+            }
+            zero_acc(S);
+            __syncthreads();
+            return;
+        }
+        if (ph == PH_KICK_END) {
+            if (tid == 0) {
+                const OpParams &o = S.opp;
+                int32_t *Pk = d.P + (size_t)o.mi * (d.n + 1);
+                cov_stcg(&Pk[0], S.accT);
+                for (int j = 0; j < d.n; j++) cov_stcg(&Pk[1 + j], S.accH[j]);
+                S.kick_t++;
+                S.phase = PH_KICK_START;
+            }
+            continue;
+        }
+        if (ph == PH_KICK_DONE) {
+            if (tid == 0) {
+                S.nkicks++;
+                S.since_improve = 0;
+                S.rec.kicked = 1;
+                S.rec.unc_end = S.unc;
+                S.rec.best = S.best_unc;
+                write_trace(d, S);
+                S.phase = PH_PLAN;
+            }
+            continue;
+        }
+        if (ph == PH_GREEDY) {
+            // greedy placement on uncovered words: covsearch2e.c:1210-1234
+            if (S.greedy_i >= d.M) {
+                if (tid == 0) { S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
+                __syncthreads();
+                return;
+            }
+            long long w = leader_pick(d, S);
+            if (tid == 0) {
+                if (w < 0) w = (long long)(cov_rng_next(S.rng) % (uint64_t)d.N);
+                uint64_t pk = pk_of_idx(d, (uint32_t)w);
+                int i = S.greedy_i;
+                cov_stcg(&d.code[i], pk);
+                OpParams &o = S.opp;
+                o.op = OP_BALL; o.sgn = +1; o.mi = i; o.pc = pk; o.base = (uint32_t)w;
+                o.ul_valid = 0;
+                S.dunc = 0;
+                S.phase = PH_GREEDY_NEXT;
+            }
+            __syncthreads();
+            return;
+        }
+        if (ph == PH_GREEDY_NEXT) {
+            if (tid == 0) {
+                S.unc += (long long)S.dunc;
+                S.greedy_i++;
+                S.phase = PH_GREEDY;
+            }
+            continue;
+        }
+        if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
+        __syncthreads();
+        return;
+    }
+    if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------- kernel -----
+__global__ void __launch_bounds__(NT, 1)
+cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluster_slot, int mode,
+               unsigned long long budget_ns, long long op_guard)
+{
+    extern __shared__ __align__(16) unsigned char cov_smem[];
+    Smem &S = *reinterpret_cast<Smem *>(cov_smem);
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int csize = (int)cl.num_blocks();
+    const int cid = blockIdx.x / csize;
+    if (threadIdx.x == 0) S.slot = slots[cluster_slot[cid]];
+    __syncthreads();
+    const CovSlot &d = S.slot;
+    const bool leader = rank == 0;
+    Smem *LS = cl.map_shared_rank(&S, 0);
+
+    if (leader && threadIdx.x == 0) {
+        CovSlotState *st = d.st;
+        for (int k = 0; k < 4; k++) S.rng.s[k] = st->rng[k];
+        S.it = st->it; S.unc = st->unc; S.best_unc = st->best_unc;
+        S.since_improve = st->since_improve; S.nkicks = st->nkicks;
+        S.moves_left = st->moves_left; S.target = st->target; S.trace_n = st->trace_n;
+        S.ul_valid = st->ul_valid; S.status = st->status; S.finished = st->finished;
+        S.mode = mode;
+        S.greedy_i = (int)st->moves_left;   // greedy: first codeword to place
+        S.phase = PH_PLAN;
+        S.t_deadline = gtimer() + budget_ns;
+        S.guard = 0;
+        S.opp.op = -1;
+    }
+    cl.sync();
+    for (;;) {
+        if (leader) {
+            leader_step(d, S);
+            // safety net: an op budget and the launch deadline bound every
+            // launch even if the phase machine never reaches a move boundary
+            if (threadIdx.x == 0 && S.opp.op != OP_STOP &&
+                (++S.guard > op_guard || gtimer() > S.t_deadline + 1000000000ull)) {
+                S.status = COV_ETIMEOUT;
+                S.opp.op = OP_STOP;
+                S.phase = PH_STOPPED;
+            }
+        }
+        cl.sync();
+        if (threadIdx.x == 0) S.opl = LS->opp;
+        __syncthreads();
+        const OpParams &P = S.opl;
+        const int op = P.op;
+        if (op == OP_STOP) break;
+        if (op == OP_MOVE) {
+            op_commit(d, P, LS, rank, csize);
+            cl.sync();
+            op_recompute(d, P.basen, P.pcn, S, LS, rank, csize);
+        } else if (op == OP_NEGWALK) {
+            op_negwalk(d, P, S, LS, rank, csize, cl);
+        } else if (op == OP_BALL) {
+            op_ball(d, P, LS, rank, csize);
+        } else if (op == OP_RECOMPUTE) {
+            op_recompute(d, P.basen, P.pcn, S, LS, rank, csize);
+        } else if (op == OP_ZERO_TABU) {
+            op_zero_tabu(d, rank, csize);
+        } else if (op == OP_REBUILD_UL) {
+            op_rebuild_ul(d, rank, csize, cl);
+        }
+        cl.sync();
+    }
+    // no CTA may leave while another can still read the leader's shared memory
+    cl.sync();
+    if (leader && threadIdx.x == 0) {
+        CovSlotState *st = d.st;
+        for (int k = 0; k < 4; k++) st->rng[k] = S.rng.s[k];
+        st->it = S.it; st->unc = S.unc; st->best_unc = S.best_unc;
+        st->since_improve = S.since_improve; st->nkicks = S.nkicks;
+        st->moves_left = S.moves_left; st->trace_n = S.trace_n;
+        st->ul_valid = S.ul_valid;
+        int s0 = atomicAdd(&st->status, 0);
+        st->status = S.status ? S.status : s0;
+        st->finished = S.unc <= 0;
+    }
+}
+
+// ------------------------------------------------------ init kernels -------
+// cnt|xid marking of every codeword's ball (ids first..first+count-1)
+__global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
+{
+    const int R = d.R;
+    uint32_t cum[COV_MAXN + 2];
+    cum[0] = 1;
+    for (int r = 1; r <= R; r++)
+        cum[r] = cum[r - 1] + sphere_items(d, r, d.ball_off[r + 1] - d.ball_off[r]);
+    const unsigned long long per = cum[R];
+    const unsigned long long total = per * (unsigned long long)count;
+    for (unsigned long long g = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (unsigned long long)gridDim.x * blockDim.x) {
+        const int i = first + (int)(g / per);
+        const uint32_t t = (uint32_t)(g - (unsigned long long)(i - first) * per);
+        const uint64_t pc = d.code[i];
+        const uint32_t base = widx_pk(d, pc);
+        const uint32_t add = (sgn > 0 ? 1u : 0xffffffffu);
+        const uint32_t x = (uint32_t)i << 16;
+        if (t == 0) { atomicAdd(&d.cw[base], add); atomicXor(&d.cw[base], x); continue; }
+        int r = 1;
+        while (t >= cum[r]) r++;
+        const uint8_t *subs = d.ball_sub + (size_t)d.ball_off[r] * d.rs;
+        CovItem it = cov_item(d, subs, r, t - cum[r - 1], base, pc);
+        for (int kk = 0; kk < d.q - 1; kk++) {
+            uint32_t w; uint64_t pk;
+            cov_item_word(d, it, kk, w, pk);
+            atomicAdd(&d.cw[w], add);
+            atomicXor(&d.cw[w], x);
+        }
+    }
+}
+
+__global__ void k_count_zero(const uint32_t *cw, uint32_t N, unsigned long long *out)
+{
+    unsigned long long c = 0;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+        c += (cw[x] & 0xffffu) == 0;
+    c = warp_sum(c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// P[k] = (T_k, H_k) for every codeword from scratch
+__global__ void k_private_all(CovSlot d)
+{
+    const int R = d.R, n = d.n;
+    const uint8_t *fs = d.ball_sub + (size_t)d.ball_off[R] * d.rs;
+    const uint32_t per = sphere_items(d, R, d.nfsub);
+    const unsigned long long total = (unsigned long long)per * d.M;
+    for (unsigned long long g = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (unsigned long long)gridDim.x * blockDim.x) {
+        const int k = (int)(g / per);
+        const uint32_t t = (uint32_t)(g - (unsigned long long)k * per);
+        const uint64_t pc = d.code[k];
+        const uint32_t base = widx_pk(d, pc);
+        int32_t *Pk = d.P + (size_t)k * (n + 1);
+        if (R == 0) {
+            if ((d.cw[base] & 0xffffu) == 1) atomicAdd(&Pk[0], 1);
+            continue;
+        }
+        CovItem it = cov_item(d, fs, R, t, base, pc);
+        int t1 = 0;
+        for (int kk = 0; kk < d.q - 1; kk++) {
+            uint32_t w; uint64_t pk;
+            cov_item_word(d, it, kk, w, pk);
+            t1 += (d.cw[w] & 0xffffu) == 1;
+        }
+        if (t1) {
+            atomicAdd(&Pk[0], t1);
+            for (int s = 0; s < R; s++) atomicAdd(&Pk[1 + it.ps[s]], t1);
+        }
+    }
+}
+
+// words of codeword i's ball that nothing else covers (covsearch2e.c:927-946)
+__global__ void k_unique_cover(CovSlot d, int count, int *out)
+{
+    const int R = d.R;
+    const int i = blockIdx.x;
+    if (i >= count) return;
+    uint32_t cum[COV_MAXN + 2];
+    cum[0] = 1;
+    for (int r = 1; r <= R; r++)
+        cum[r] = cum[r - 1] + sphere_items(d, r, d.ball_off[r + 1] - d.ball_off[r]);
+    const uint64_t pc = d.code[i];
+    const uint32_t base = widx_pk(d, pc);
+    int u = 0;
+    for (uint32_t t = threadIdx.x; t < cum[R]; t += blockDim.x) {
+        if (t == 0) { u += (d.cw[base] & 0xffffu) == 1; continue; }
+        int r = 1;
+        while (t >= cum[r]) r++;
+        const uint8_t *subs = d.ball_sub + (size_t)d.ball_off[r] * d.rs;
+        CovItem it = cov_item(d, subs, r, t - cum[r - 1], base, pc);
+        for (int kk = 0; kk < d.q - 1; kk++) {
+            uint32_t w; uint64_t pk;
+            cov_item_word(d, it, kk, w, pk);
+            u += (d.cw[w] & 0xffffu) == 1;
+        }
+    }
+    __shared__ int red[32];
+    u = warp_sum(u);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) s += red[w];
+        out[i] = s;
+    }
+}
+
+__global__ void k_unpack_cnt(const uint32_t *cw, uint32_t N, uint16_t *out)
+{
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+        out[x] = (uint16_t)(cw[x] & 0xffffu);
+}
+
+// =========================================================== host side =====
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
+    fprintf(stderr, "covgpu: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+    return -(100 + (int)e_); } } while (0)
+
+namespace {
+
+long long ipow_h(long long b, int e) { long long r = 1; while (e-- > 0) r *= b; return r; }
+long long binom_h(int a, int b)
+{
+    if (b < 0 || b > a) return 0;
+    if (b > a - b) b = a - b;
+    long long r = 1;
+    for (int i = 0; i < b; i++) r = r * (a - i) / (i + 1);
+    return r;
+}
+int fill_subsets_h(const int *pool, int np, int R, int rs, uint8_t *out)
+{
+    if (binom_h(np, R) <= 0) return 0;
+    int c[32], k = 0;
+    for (int t = 0; t < R; t++) c[t] = t;
+    for (;;) {
+        for (int t = 0; t < R; t++) out[(size_t)k * rs + t] = (uint8_t)pool[c[t]];
+        k++;
+        int t = R - 1;
+        while (t >= 0 && c[t] == np - R + t) t--;
+        if (t < 0) break;
+        c[t]++;
+        for (int s = t + 1; s < R; s++) c[s] = c[s - 1] + 1;
+    }
+    return k;
+}
+
+struct HostSlot {
+    bool used = false;
+    CovSlot d{};
+    CovSlotState *st = nullptr;
+    void *arena = nullptr;       // one device allocation for all arrays
+    size_t arena_bytes = 0;
+    int cluster = 1;
+    cov_params prm{};
+};
+
+}  // namespace
+
+struct cov_pool {
+    int max_slots = 0;
+    int cluster = 8;
+    std::vector<HostSlot> slots;
+    CovSlot *d_slots = nullptr;
+    int *d_map = nullptr;
+    CovSlotState *d_states = nullptr;
+    cudaStream_t stream = nullptr;
+    double budget_s = 30.0;
+    long long launch_moves = 0;      // move budget of the current launch
+};
+
+static int g_attr_done = 0;
+
+static int ensure_attrs()
+{
+    if (g_attr_done) return 0;
+    CK(cudaFuncSetAttribute(cov_run_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
+    CK(cudaFuncSetAttribute(cov_run_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    g_attr_done = 1;
+    return 0;
+}
+
+static int launch_run(cov_pool *pool, const std::vector<int> &active, int csize, int mode)
+{
+    if (active.empty()) return 0;
+    CK(cudaMemcpyAsync(pool->d_map, active.data(), sizeof(int) * active.size(), cudaMemcpyHostToDevice,
+                       pool->stream));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(active.size() * csize));
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = sizeof(Smem);
+    cfg.stream = pool->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    unsigned long long budget_ns = (unsigned long long)(pool->budget_s * 1e9);
+    // ops per move <= 2 (walk + move) + a kick's 3 per codeword + 2
+    int kmax = 0;
+    long long mmax = 0;
+    for (int s : active) {
+        kmax = std::max(kmax, pool->slots[s].d.kick);
+        mmax = std::max<long long>(mmax, pool->slots[s].d.M);
+    }
+    long long guard = mode == MODE_GREEDY ? 4 * mmax + 4096
+                                          : pool->launch_moves * (6 + 3LL * kmax) + 4096;
+    CK(cudaLaunchKernelEx(&cfg, cov_run_kernel, (const CovSlot *)pool->d_slots, (const int *)pool->d_map,
+                          mode, budget_ns, guard));
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static int push_slot(cov_pool *pool, int s)
+{
+    CK(cudaMemcpyAsync(pool->d_slots + s, &pool->slots[s].d, sizeof(CovSlot), cudaMemcpyHostToDevice,
+                       pool->stream));
+    return 0;
+}
+
+static int read_state(cov_pool *pool, int s, CovSlotState *out)
+{
+    CK(cudaMemcpyAsync(out, pool->slots[s].st, sizeof(CovSlotState), cudaMemcpyDeviceToHost, pool->stream));
+    CK(cudaStreamSynchronize(pool->stream));
+    return 0;
+}
+
+static int write_state(cov_pool *pool, int s, const CovSlotState *in)
+{
+    CK(cudaMemcpyAsync(pool->slots[s].st, in, sizeof(CovSlotState), cudaMemcpyHostToDevice, pool->stream));
+    CK(cudaStreamSynchronize(pool->stream));
+    return 0;
+}
+
+extern "C" {
+
+int cov_pool_create(int32_t max_slots, int32_t cluster, cov_pool **out)
+{
+    if (!out || max_slots < 1 || cluster < 1 || cluster > 16) return COV_EINVAL;
+    *out = nullptr;
+    int dev = 0, major = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    if (major < 10) return COV_ENODEV;
+    int rc = ensure_attrs();
+    if (rc) return rc;
+    cov_pool *p = new cov_pool();
+    p->max_slots = max_slots;
+    p->cluster = cluster;
+    p->slots.resize(max_slots);
+    if (cudaMalloc(&p->d_slots, sizeof(CovSlot) * max_slots) != cudaSuccess ||
+        cudaMalloc(&p->d_map, sizeof(int) * max_slots) != cudaSuccess ||
+        cudaMalloc(&p->d_states, sizeof(CovSlotState) * max_slots) != cudaSuccess) {
+        cudaFree(p->d_slots); cudaFree(p->d_map); cudaFree(p->d_states);
+        delete p;
+        return COV_ENOMEM;
+    }
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaFree(p->d_slots); cudaFree(p->d_map); cudaFree(p->d_states);
+        delete p;
+        return COV_ENOMEM;
+    }
+    *out = p;
+    return COV_OK;
+}
+
+int cov_pool_set_budget(cov_pool *pool, double seconds)
+{
+    if (!pool || !(seconds > 0)) return COV_EINVAL;
+    pool->budget_s = seconds;
+    return COV_OK;
+}
+
+int cov_pool_remove(cov_pool *pool, int32_t slot)
+{
+    if (!pool || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    HostSlot &h = pool->slots[slot];
+    cudaStreamSynchronize(pool->stream);
+    cudaFree(h.arena);
+    h = HostSlot();
+    return COV_OK;
+}
+
+int cov_pool_destroy(cov_pool *pool)
+{
+    if (!pool) return COV_OK;
+    cudaStreamSynchronize(pool->stream);
+    for (int s = 0; s < pool->max_slots; s++)
+        if (pool->slots[s].used) cudaFree(pool->slots[s].arena);
+    cudaFree(pool->d_slots); cudaFree(pool->d_map); cudaFree(pool->d_states);
+    cudaStreamDestroy(pool->stream);
+    delete pool;
+    return COV_OK;
+}
+
+size_t cov_slot_bytes(const cov_params *prm)
+{
+    if (!prm) return 0;
+    const int q = prm->q, n = prm->n, R = prm->R, M = prm->M;
+    if (q < 2 || q > 16 || n < 1 || n > 16 || R < 0 || M < 1 || M > 65535) return 0;
+    long long N = ipow_h(q, n);
+    size_t b = 0;
+    auto add = [&](size_t x) { b += (x + 255) / 256 * 256; };
+    add((size_t)N * 4);                              // cw
+    add((size_t)M * 8 * 2);                          // code, best
+    add((size_t)M * n * q * 4);                      // tabu
+    add((size_t)M * (n + 1) * 4);                    // P
+    add((size_t)UL_CAP_DEFAULT * 4);                 // ul_idx
+    add((size_t)UL_CAP_DEFAULT * 8);                 // ul_pk
+    add((size_t)((N + 31) / 32) * 4);                // ul_bit
+    add((size_t)M * n * 4 * 3 + (size_t)M * 4);      // g_perm, g_dval, g_neg, g_list
+    add(65536);                                      // subset tables
+    add(sizeof(CovSlotState));
+    if (prm->trace) add((size_t)prm->trace_cap * sizeof(cov_move_rec));
+    return b;
+}
+
+// Create an instance and initialise its code exactly as covsearch2e main()
+// does (covsearch2e.c:1156-1255): m == M -> rebuild; m < M -> greedy
+// placement (or --random-init digits); m > M -> remove-and-repair.
+int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int32_t m,
+                 int32_t random_init, int32_t *slot_out)
+{
+    if (!pool || !prm || (m > 0 && !code) || m < 0) return COV_EINVAL;
+    const int q = prm->q, n = prm->n, M = prm->M;
+    int R = prm->R;
+    if (q < 2 || q > 16 || n < 1 || n > 16 || R < 0 || M < 1 || M > 65535) return COV_EINVAL;
+    if (prm->cand < 1 || prm->kick < 0 || prm->stall < 0) return COV_EINVAL;
+    if (m > 65535) return COV_ERANGE;
+    long long N = ipow_h(q, n);
+    if (N >= (1LL << 32) - 1) return COV_EINVAL;
+    if (R > n) R = n;
+    for (long long i = 0; i < (long long)m * n; i++) if (code[i] >= q) return COV_EINVAL;
+    int s = -1;
+    for (int k = 0; k < pool->max_slots; k++) if (!pool->slots[k].used) { s = k; break; }
+    if (s < 0) return COV_ERANGE;
+    const int Mw = std::max(M, m);     // remove-and-repair works on m words first
+
+    HostSlot h;
+    h.prm = *prm;
+    h.cluster = pool->cluster;
+    CovSlot &d = h.d;
+    d.q = q; d.n = n; d.R = R; d.M = M;
+    d.N = (uint32_t)N;
+    for (int j = 0; j < n; j++) d.pw[j] = (uint32_t)ipow_h(q, n - 1 - j);
+    d.rs = R ? R : 1;
+    d.nsub = (int)binom_h(n - 1, R);
+    d.nfsub = (int)binom_h(n, R);
+    for (int k = 0; k <= COV_MAXN; k++) d.ppow[k] = (uint32_t)std::min<long long>(ipow_h(q - 1, k), 0xffffffffLL);
+    d.tenure = prm->tabu; d.kick = prm->kick; d.cand = prm->cand; d.stall = prm->stall;
+    d.ul_cap = UL_CAP_DEFAULT;
+    // subset tables
+    std::vector<uint8_t> subs((size_t)n * std::max(d.nsub, 1) * d.rs, 0);
+    for (int p = 0; p < n; p++) {
+        int pool_[32], np = 0;
+        for (int j = 0; j < n; j++) if (j != p) pool_[np++] = j;
+        fill_subsets_h(pool_, np, R, d.rs, subs.data() + (size_t)p * d.nsub * d.rs);
+    }
+    std::vector<uint8_t> balls;
+    {
+        int pool_[32];
+        for (int j = 0; j < n; j++) pool_[j] = j;
+        int off = 0;
+        for (int r = 0; r <= R; r++) {
+            d.ball_off[r] = off;
+            int cnt = (int)binom_h(n, r);
+            balls.resize((size_t)(off + cnt) * d.rs, 0);
+            if (r > 0) fill_subsets_h(pool_, n, r, d.rs, balls.data() + (size_t)off * d.rs);
+            off += cnt;
+        }
+        d.ball_off[R + 1] = off;
+    }
+    // one arena for everything
+    cov_params p2 = *prm;
+    p2.M = Mw;
+    size_t need = cov_slot_bytes(&p2) + subs.size() + balls.size() + 1024;
+    void *arena = nullptr;
+    if (cudaMalloc(&arena, need) != cudaSuccess) { cudaGetLastError(); return COV_ENOMEM; }
+    size_t off = 0;
+    auto take_ = [&](size_t x) { void *p = (char *)arena + off; off += (x + 255) / 256 * 256; return p; };
+    d.cw = (uint32_t *)take_((size_t)N * 4);
+    d.code = (uint64_t *)take_((size_t)Mw * 8);
+    d.best = (uint64_t *)take_((size_t)Mw * 8);
+    d.tabu = (int32_t *)take_((size_t)Mw * n * q * 4);
+    d.P = (int32_t *)take_((size_t)Mw * (n + 1) * 4);
+    d.ul_idx = (uint32_t *)take_((size_t)d.ul_cap * 4);
+    d.ul_pk = (uint64_t *)take_((size_t)d.ul_cap * 8);
+    d.ul_bit = (uint32_t *)take_((size_t)((N + 31) / 32) * 4);
+    d.g_perm = (uint32_t *)take_((size_t)Mw * n * 4);
+    d.g_dval = (int32_t *)take_((size_t)Mw * n * 4);
+    d.g_neg = (int32_t *)take_((size_t)Mw * n * 4);
+    d.g_list = (uint32_t *)take_((size_t)Mw * 4);
+    uint8_t *dsub = (uint8_t *)take_(subs.size());
+    uint8_t *dball = (uint8_t *)take_(balls.size());
+    d.sub = dsub; d.ball_sub = dball;
+    d.st = (CovSlotState *)take_(sizeof(CovSlotState));
+    d.trace = prm->trace ? take_((size_t)prm->trace_cap * sizeof(cov_move_rec)) : nullptr;
+    d.trace_cap = prm->trace ? prm->trace_cap : 0;
+    h.arena = arena;
+    h.arena_bytes = need;
+    h.st = d.st;
+    h.used = true;
+
+    cudaStream_t st = pool->stream;
+    auto fail = [&](int rc) { cudaFree(arena); return rc; };
+#define CKF(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
+    fprintf(stderr, "covgpu: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+    return fail(-(100 + (int)e_)); } } while (0)
+    CKF(cudaMemcpyAsync(dsub, subs.data(), subs.size(), cudaMemcpyHostToDevice, st));
+    CKF(cudaMemcpyAsync(dball, balls.data(), balls.size(), cudaMemcpyHostToDevice, st));
+    CKF(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
+    CKF(cudaMemsetAsync(d.tabu, 0, (size_t)Mw * n * q * 4, st));
+    CKF(cudaMemsetAsync(d.P, 0, (size_t)Mw * (n + 1) * 4, st));
+    CKF(cudaMemsetAsync(d.ul_bit, 0, (size_t)((N + 31) / 32) * 4, st));
+    CovSlotState hs;
+    memset(&hs, 0, sizeof hs);
+    CovRng rng;
+    cov_rng_seed(rng, prm->seed);
+
+    std::vector<uint64_t> pk((size_t)Mw, 0);
+    for (int i = 0; i < m; i++) {
+        uint64_t v = 0;
+        for (int j = 0; j < n; j++) v |= (uint64_t)code[(size_t)i * n + j] << (4 * j);
+        pk[i] = v;
+    }
+    int have = std::min(m, M);
+    const int grid = 152 * 8;
+    if (m > M) {
+        // remove-and-repair descent (covsearch2e.c:1163-1192): cnt of all m
+        // words, then repeatedly drop the first word with the fewest
+        // uniquely covered words.
+        CovSlot dm = d;
+        dm.M = m;
+        CKF(cudaMemcpyAsync(d.code, pk.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
+        k_mark_balls<<<grid, 256, 0, st>>>(dm, 0, m, +1);
+        CKF(cudaGetLastError());
+        int *d_u = d.g_list ? (int *)d.g_perm : nullptr;
+        std::vector<int> hu(m);
+        std::vector<uint64_t> cur(pk.begin(), pk.begin() + m);
+        int ms = m;
+        while (ms > M) {
+            dm.M = ms;
+            k_unique_cover<<<ms, 256, 0, st>>>(dm, ms, d_u);
+            CKF(cudaGetLastError());
+            CKF(cudaMemcpyAsync(hu.data(), d_u, sizeof(int) * ms, cudaMemcpyDeviceToHost, st));
+            CKF(cudaStreamSynchronize(st));
+            int worst = 0;
+            for (int i = 1; i < ms; i++) if (hu[i] < hu[worst]) worst = i;
+            k_mark_balls<<<grid, 256, 0, st>>>(dm, worst, 1, -1);
+            CKF(cudaGetLastError());
+            cur.erase(cur.begin() + worst);
+            ms--;
+            CKF(cudaMemcpyAsync(d.code, cur.data(), (size_t)ms * 8, cudaMemcpyHostToDevice, st));
+        }
+        for (int i = 0; i < M; i++) pk[i] = cur[i];
+        have = M;
+        CKF(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
+    }
+    if (have < M && !random_init) {
+        // greedy placement runs on the device (it samples uncovered words)
+        CKF(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
+        if (have > 0) {
+            k_mark_balls<<<grid, 256, 0, st>>>(d, 0, have, +1);
+            CKF(cudaGetLastError());
+        }
+        unsigned long long *d_z = (unsigned long long *)d.g_dval;
+        CKF(cudaMemsetAsync(d_z, 0, 8, st));
+        k_count_zero<<<grid, 256, 0, st>>>(d.cw, d.N, d_z);
+        CKF(cudaGetLastError());
+        unsigned long long z = 0;
+        CKF(cudaMemcpyAsync(&z, d_z, 8, cudaMemcpyDeviceToHost, st));
+        CKF(cudaStreamSynchronize(st));
+        for (int k = 0; k < 4; k++) hs.rng[k] = rng.s[k];
+        hs.unc = (long long)z;
+        hs.best_unc = hs.unc;
+        hs.moves_left = have;        // greedy mode: index of the first word to place
+        hs.target = -1;
+        CKF(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
+        pool->slots[s] = h;
+        int rc = push_slot(pool, s);
+        if (rc) { pool->slots[s] = HostSlot(); return fail(rc); }
+        std::vector<int> act{s};
+        double saved = pool->budget_s;
+        pool->budget_s = std::max(saved, 120.0);
+        rc = launch_run(pool, act, h.cluster, MODE_GREEDY);
+        pool->budget_s = saved;
+        if (rc) { pool->slots[s] = HostSlot(); return fail(rc); }
+        CKF(cudaStreamSynchronize(st));
+        CKF(cudaMemcpyAsync(&hs, d.st, sizeof hs, cudaMemcpyDeviceToHost, st));
+        CKF(cudaStreamSynchronize(st));
+        if (hs.status) { pool->slots[s] = HostSlot(); return fail(hs.status); }
+        for (int k = 0; k < 4; k++) rng.s[k] = hs.rng[k];
+        // rebuild cnt|xid from the final code so the xor ids are exact
+        CKF(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
+        k_mark_balls<<<grid, 256, 0, st>>>(d, 0, M, +1);
+        CKF(cudaGetLastError());
+    } else {
+        for (int i = have; i < M; i++) {
+            uint64_t v = 0;
+            for (int j = 0; j < n; j++) v |= (cov_rng_next(rng) % (uint64_t)q) << (4 * j);
+            pk[i] = v;
+        }
+        CKF(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
+        k_mark_balls<<<grid, 256, 0, st>>>(d, 0, M, +1);
+        CKF(cudaGetLastError());
+    }
+    // uncovered count, private counts, best code
+    unsigned long long *d_z = (unsigned long long *)d.g_dval;
+    CKF(cudaMemsetAsync(d_z, 0, 8, st));
+    k_count_zero<<<grid, 256, 0, st>>>(d.cw, d.N, d_z);
+    CKF(cudaGetLastError());
+    CKF(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
+    k_private_all<<<grid, 256, 0, st>>>(d);
+    CKF(cudaGetLastError());
+    CKF(cudaMemcpyAsync(d.best, d.code, (size_t)M * 8, cudaMemcpyDeviceToDevice, st));
+    unsigned long long z = 0;
+    CKF(cudaMemcpyAsync(&z, d_z, 8, cudaMemcpyDeviceToHost, st));
+    CKF(cudaStreamSynchronize(st));
+    memset(&hs, 0, sizeof hs);
+    for (int k = 0; k < 4; k++) hs.rng[k] = rng.s[k];
+    hs.unc = (long long)z;
+    hs.best_unc = hs.unc;
+    hs.target = -1;
+    hs.ul_valid = 0;
+    hs.finished = hs.unc == 0;
+    CKF(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
+    pool->slots[s] = h;
+    int rc = push_slot(pool, s);
+    if (rc) { pool->slots[s] = HostSlot(); return fail(rc); }
+    CKF(cudaStreamSynchronize(st));
+    if (slot_out) *slot_out = s;
+    return COV_OK;
+#undef CKF
+}
+
+// Advance every live instance by up to `moves` further moves (stopping
+// early at a full cover or when best <= target).  One launch, one cluster
+// per instance.
+int cov_pool_run(cov_pool *pool, int64_t moves, int64_t target)
+{
+    if (!pool || moves < 0) return COV_EINVAL;
+    std::vector<int> active;
+    for (int s = 0; s < pool->max_slots; s++) {
+        if (!pool->slots[s].used) continue;
+        CovSlotState hs;
+        int rc = read_state(pool, s, &hs);
+        if (rc) return rc;
+        if (hs.status || hs.unc <= 0) continue;
+        hs.moves_left = moves;
+        hs.target = target;
+        rc = write_state(pool, s, &hs);
+        if (rc) return rc;
+        active.push_back(s);
+    }
+    if (active.empty()) return COV_OK;
+    pool->launch_moves = moves;
+    int rc = launch_run(pool, active, pool->cluster, MODE_SEARCH);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(pool->stream));
+    return COV_OK;
+}
+
+int cov_pool_status(cov_pool *pool, int32_t slot, cov_status *out)
+{
+    if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    CovSlotState hs;
+    int rc = read_state(pool, slot, &hs);
+    if (rc) return rc;
+    memset(out, 0, sizeof *out);
+    out->it = hs.it;
+    out->uncovered = hs.unc;
+    out->best = hs.best_unc;
+    out->kicks = hs.nkicks;
+    out->status = hs.status;
+    out->finished = hs.unc <= 0;
+    out->ul_valid = hs.ul_valid;
+    out->ul_n = hs.ul_n;
+    out->trace_n = hs.trace_n;
+    return COV_OK;
+}
+
+static int get_packed(cov_pool *pool, int32_t slot, bool best, uint8_t *out)
+{
+    if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    const CovSlot &d = pool->slots[slot].d;
+    std::vector<uint64_t> pk(d.M);
+    CK(cudaMemcpyAsync(pk.data(), best ? d.best : d.code, (size_t)d.M * 8, cudaMemcpyDeviceToHost, pool->stream));
+    CK(cudaStreamSynchronize(pool->stream));
+    for (int i = 0; i < d.M; i++)
+        for (int j = 0; j < d.n; j++) out[(size_t)i * d.n + j] = (uint8_t)cov_nib(pk[i], j);
+    return COV_OK;
+}
+
+int cov_pool_get_code(cov_pool *pool, int32_t slot, uint8_t *out) { return get_packed(pool, slot, false, out); }
+int cov_pool_get_best(cov_pool *pool, int32_t slot, uint8_t *out) { return get_packed(pool, slot, true, out); }
+
+int cov_pool_get_cnt(cov_pool *pool, int32_t slot, uint16_t *out)
+{
+    if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    const CovSlot &d = pool->slots[slot].d;
+    uint16_t *tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, (size_t)d.N * 2, pool->stream));
+    k_unpack_cnt<<<152 * 4, 256, 0, pool->stream>>>(d.cw, d.N, tmp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, tmp, (size_t)d.N * 2, cudaMemcpyDeviceToHost, pool->stream));
+    CK(cudaFreeAsync(tmp, pool->stream));
+    CK(cudaStreamSynchronize(pool->stream));
+    return COV_OK;
+}
+
+int cov_pool_get_private(cov_pool *pool, int32_t slot, int32_t *out)
+{
+    if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    const CovSlot &d = pool->slots[slot].d;
+    CK(cudaMemcpyAsync(out, d.P, (size_t)d.M * (d.n + 1) * 4, cudaMemcpyDeviceToHost, pool->stream));
+    CK(cudaStreamSynchronize(pool->stream));
+    return COV_OK;
+}
+
+int cov_pool_get_trace(cov_pool *pool, int32_t slot, cov_move_rec *out, int64_t cap, int64_t *n_out)
+{
+    if (!pool || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    const CovSlot &d = pool->slots[slot].d;
+    CovSlotState hs;
+    int rc = read_state(pool, slot, &hs);
+    if (rc) return rc;
+    long long n = std::min<long long>(hs.trace_n, d.trace_cap);
+    if (out && cap > 0) {
+        long long k = std::min<long long>(n, cap);
+        if (k > 0)
+            CK(cudaMemcpyAsync(out, d.trace, (size_t)k * sizeof(cov_move_rec), cudaMemcpyDeviceToHost, pool->stream));
+        CK(cudaStreamSynchronize(pool->stream));
+    }
+    if (n_out) *n_out = n;
+    return COV_OK;
+}
+
+int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4)
+{
+    if (!pool || !out4 || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    CovSlotState hs;
+    int rc = read_state(pool, slot, &hs);
+    if (rc) return rc;
+    for (int k = 0; k < 4; k++) out4[k] = hs.rng[k];
+    return COV_OK;
+}
+
+int cov_pool_get_tabu(cov_pool *pool, int32_t slot, int32_t *out)
+{
+    if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    const CovSlot &d = pool->slots[slot].d;
+    CK(cudaMemcpyAsync(out, d.tabu, (size_t)d.M * d.n * d.q * 4, cudaMemcpyDeviceToHost, pool->stream));
+    CK(cudaStreamSynchronize(pool->stream));
+    return COV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,443 @@
+// cov_verify.cu -- GB300 (sm_103a) verification kernels for covering codes.
+//
+//   * exact per-word minimum distance to a code (the distance transform),
+//     computed as n axis passes of the line-min recurrence
+//         D'(x) = min(D(x), 1 + min_a D(x with x_j := a))
+//     over uint8 values.  After the passes over axes 0..n-1, D(x) is the
+//     Hamming distance from x to the nearest codeword -- the `best` array of
+//     cov/verify_independent.py:144-186 -- and #{x : D(x) > R} is the
+//     uncovered count that cov/verify_cov.py:109-230 returns.
+//     The n passes are grouped so that HBM is swept twice, not n times:
+//     the low axes of a contiguous tile, then the high axes of a column
+//     strip, each group worked in shared memory.  The histogram of D is
+//     folded into the last pass.
+//   * coverage multiplicity cnt[x] = #{i : d(x,c_i) <= R} by marking every
+//     codeword's ball (covsearch2e.c:353-380, 958-967), with 32-bit atomics
+//     on packed uint16 pairs.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include "cov_common.cuh"
+#include "../../include/covgpu.h"
+
+#define DT_TILE_MAX   65536    // bytes of the contiguous low-axes tile
+#define DT_STRIP_MAX  98304    // bytes of a high-axes strip
+#define DT_STRIP_W    32       // columns of a strip
+#define DT_NT         512
+
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
+    fprintf(stderr, "covgpu: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+    return -(100 + (int)e_); } } while (0)
+
+struct DtGeom {
+    int q, n;
+    uint32_t N;
+    uint32_t pw[COV_MAXN + 1];   // pw[k] = q^k
+    int inf;                     // n + 1
+};
+
+// --------------------------------------------------------- code bitmap ----
+__global__ void k_dt_bitmap(const uint8_t *__restrict__ code, int M, DtGeom g, uint32_t *bm)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+        uint32_t x = 0;
+        for (int j = 0; j < g.n; j++) x = x * (uint32_t)g.q + code[(size_t)i * g.n + j];
+        atomicOr(&bm[x >> 5], 1u << (x & 31));
+    }
+}
+
+// line-min along one axis of a shared-memory block: elements e = o*q*s +
+// a*s + i (a < q, i < s) for every outer o and inner i
+__device__ __forceinline__ void dt_axis_smem(uint8_t *t, int total, int q, int s, int inf)
+{
+    const int fibers = total / q;
+    for (int f = threadIdx.x; f < fibers; f += blockDim.x) {
+        int o = f / s, i = f - o * s;
+        uint8_t *b = t + (size_t)o * q * s + i;
+        int m = inf;
+        for (int a = 0; a < q; a++) m = min(m, (int)b[a * s]);
+        int c = min(m + 1, inf);
+        for (int a = 0; a < q; a++) if (b[a * s] > c) b[a * s] = (uint8_t)c;
+    }
+}
+
+// histogram update aggregated over the lanes holding the same value
+__device__ __forceinline__ void dt_hist_add(int *sh, int v)
+{
+    const unsigned act = __activemask();
+    const unsigned same = __match_any_sync(act, v);
+    if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&sh[v], __popc(same));
+}
+
+// Pass 1: tiles of q^k contiguous words, low k axes, from the code bitmap.
+// When k == n this is the whole transform and the histogram is taken here.
+__global__ void __launch_bounds__(DT_NT)
+k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__ D,
+         unsigned long long *hist)
+{
+    extern __shared__ __align__(16) uint8_t dt_sm[];
+    __shared__ int sh[COV_MAXN + 2];
+    const uint32_t T = g.pw[k];
+    const uint32_t ntile = g.N / T;
+    const bool last = (k == g.n) && hist != nullptr;
+    if (threadIdx.x < COV_MAXN + 2) sh[threadIdx.x] = 0;
+    for (uint32_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const uint32_t x0 = tile * T;
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
+            uint32_t x = x0 + e;
+            dt_sm[e] = ((__ldg(&bm[x >> 5]) >> (x & 31)) & 1u) ? 0 : (uint8_t)g.inf;
+        }
+        __syncthreads();
+        for (int j = 0; j < k; j++) {          // in-tile stride q^j
+            dt_axis_smem(dt_sm, (int)T, g.q, (int)g.pw[j], g.inf);
+            __syncthreads();
+        }
+        for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
+            uint8_t v = dt_sm[e];
+            D[x0 + e] = v;
+            if (last) dt_hist_add(sh, v);
+        }
+    }
+    __syncthreads();
+    if (last && threadIdx.x < g.n + 2 && sh[threadIdx.x])
+        atomicAdd(&hist[threadIdx.x], (unsigned long long)sh[threadIdx.x]);
+}
+
+// Pass 2+: the axes of group [j0, j0+gsz) (in-word strides q^j0 .. ), for a
+// strip of up to DT_STRIP_W consecutive positions below the group.
+__global__ void __launch_bounds__(DT_NT)
+k_dt_high(DtGeom g, int j0, int gsz, int last_, uint8_t *__restrict__ D, unsigned long long *hist)
+{
+    const bool last = last_ && hist != nullptr;
+    extern __shared__ __align__(16) uint8_t dt_sm[];
+    __shared__ int sh[COV_MAXN + 2];
+    const uint32_t s = g.pw[j0];                 // stride of the lowest axis in the group
+    const uint32_t rows = g.pw[gsz];
+    const uint32_t span = rows * s;              // words spanned by one value of the outer digits
+    const uint32_t outer = g.N / span;
+    const uint32_t nstrip = (s + DT_STRIP_W - 1) / DT_STRIP_W;
+    const unsigned long long ntiles = (unsigned long long)outer * nstrip;
+    if (threadIdx.x < COV_MAXN + 2) sh[threadIdx.x] = 0;
+    for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t o = (uint32_t)(tile / nstrip);
+        const uint32_t c0 = (uint32_t)(tile - (unsigned long long)o * nstrip) * DT_STRIP_W;
+        const int w = (int)min((uint32_t)DT_STRIP_W, s - c0);
+        const uint32_t base = o * span + c0;
+        __syncthreads();
+        // element (row r, column c) at base + r*s + c, kept at r*W + c
+        for (uint32_t e = threadIdx.x; e < rows * DT_STRIP_W; e += blockDim.x) {
+            uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
+            dt_sm[e] = (c < (uint32_t)w) ? D[base + r * s + c] : (uint8_t)g.inf;
+        }
+        __syncthreads();
+        for (int j = 0; j < gsz; j++) {          // row stride q^j, column width W
+            dt_axis_smem(dt_sm, (int)(rows * DT_STRIP_W), g.q, (int)g.pw[j] * DT_STRIP_W, g.inf);
+            __syncthreads();
+        }
+        for (uint32_t e = threadIdx.x; e < rows * DT_STRIP_W; e += blockDim.x) {
+            uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
+            if (c < (uint32_t)w) {
+                uint8_t v = dt_sm[e];
+                D[base + r * s + c] = v;
+                if (last) dt_hist_add(sh, v);
+            }
+        }
+    }
+    __syncthreads();
+    if (last && threadIdx.x < g.n + 2 && sh[threadIdx.x])
+        atomicAdd(&hist[threadIdx.x], (unsigned long long)sh[threadIdx.x]);
+}
+
+__global__ void k_count_above(const uint8_t *__restrict__ D, uint32_t N, int R, unsigned long long *out)
+{
+    unsigned long long c = 0;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+        c += D[x] > R;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// ball marking into uint16 counts (pairs updated with 32-bit atomics)
+__global__ void k_count_balls(CovSlot d, const uint8_t *__restrict__ code, int M, uint16_t *cnt)
+{
+    const int R = d.R;
+    uint32_t cum[COV_MAXN + 2];
+    cum[0] = 1;
+    for (int r = 1; r <= R; r++)
+        cum[r] = cum[r - 1] + (uint32_t)(d.ball_off[r + 1] - d.ball_off[r]) * d.ppow[r - 1];
+    const unsigned long long per = cum[R];
+    const unsigned long long total = per * (unsigned long long)M;
+    uint32_t *c32 = reinterpret_cast<uint32_t *>(cnt);
+    for (unsigned long long g = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (unsigned long long)gridDim.x * blockDim.x) {
+        const int i = (int)(g / per);
+        const uint32_t t = (uint32_t)(g - (unsigned long long)i * per);
+        uint64_t pc = 0;
+        uint32_t base = 0;
+        for (int j = 0; j < d.n; j++) {
+            int v = code[(size_t)i * d.n + j];
+            pc |= (uint64_t)v << (4 * j);
+            base += (uint32_t)v * d.pw[j];
+        }
+        if (t == 0) { atomicAdd(&c32[base >> 1], (base & 1) ? 65536u : 1u); continue; }
+        int r = 1;
+        while (t >= cum[r]) r++;
+        const uint8_t *subs = d.ball_sub + (size_t)d.ball_off[r] * d.rs;
+        CovItem it = cov_item(d, subs, r, t - cum[r - 1], base, pc);
+        for (int kk = 0; kk < d.q - 1; kk++) {
+            uint32_t w; uint64_t pk;
+            cov_item_word(d, it, kk, w, pk);
+            atomicAdd(&c32[w >> 1], (w & 1) ? 65536u : 1u);
+        }
+    }
+}
+
+// ============================================================ host ========
+namespace {
+
+long long ipw(long long b, int e) { long long r = 1; while (e-- > 0) r *= b; return r; }
+
+int geom(int q, int n, DtGeom &g)
+{
+    if (q < 2 || q > 16 || n < 1 || n > 16) return COV_EINVAL;
+    long long N = ipw(q, n);
+    if (N >= (1LL << 32) - 1) return COV_EINVAL;
+    g.q = q; g.n = n; g.N = (uint32_t)N; g.inf = n + 1;
+    for (int k = 0; k <= COV_MAXN; k++) g.pw[k] = (uint32_t)std::min<long long>(ipw(q, k), 0xffffffffLL);
+    return 0;
+}
+
+int g_dt_attr = 0;
+
+// the transform on device buffers; hist (device, n+2 entries) may be null
+int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned long long *d_hist,
+           uint32_t *d_bm, cudaStream_t st)
+{
+    if (!g_dt_attr) {
+        CK(cudaFuncSetAttribute(k_dt_low, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_TILE_MAX));
+        CK(cudaFuncSetAttribute(k_dt_high, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_STRIP_MAX));
+        g_dt_attr = 1;
+    }
+    CK(cudaMemsetAsync(d_bm, 0, (size_t)((g.N + 31) / 32) * 4, st));
+    if (M > 0) {
+        k_dt_bitmap<<<std::min(1024, (M + 255) / 256), 256, 0, st>>>(d_code, M, g, d_bm);
+        CK(cudaGetLastError());
+    }
+    // low group: as many axes as fit a tile
+    int k = 0;
+    while (k < g.n && (long long)g.pw[k + 1] <= DT_TILE_MAX) k++;
+    if (k == 0) k = 1;
+    const int sms = 152;
+    const uint32_t ntile = g.N / g.pw[k];
+    {
+        int grid = (int)std::min<uint32_t>(ntile, (uint32_t)sms * 4);
+        k_dt_low<<<grid, DT_NT, (size_t)g.pw[k], st>>>(g, k, d_bm, d_D, d_hist);
+        CK(cudaGetLastError());
+    }
+    // high groups
+    int j0 = k;
+    while (j0 < g.n) {
+        int gsz = 0;
+        while (j0 + gsz < g.n && (long long)g.pw[gsz + 1] * DT_STRIP_W <= DT_STRIP_MAX) gsz++;
+        if (gsz == 0) return COV_EINVAL;
+        int last = (j0 + gsz == g.n);
+        const uint32_t s = g.pw[j0];
+        const unsigned long long tiles = (unsigned long long)(g.N / (g.pw[gsz] * s)) * ((s + DT_STRIP_W - 1) / DT_STRIP_W);
+        int grid = (int)std::min<unsigned long long>(tiles, (unsigned long long)sms * 4);
+        k_dt_high<<<grid, DT_NT, (size_t)g.pw[gsz] * DT_STRIP_W, st>>>(g, j0, gsz, last, d_D, d_hist);
+        CK(cudaGetLastError());
+        j0 += gsz;
+    }
+    return 0;
+}
+
+void build_ball_tables(int n, int R, int rs, std::vector<uint8_t> &balls, int *ball_off)
+{
+    auto binom = [](int a, int b) -> long long {
+        if (b < 0 || b > a) return 0;
+        if (b > a - b) b = a - b;
+        long long r = 1;
+        for (int i = 0; i < b; i++) r = r * (a - i) / (i + 1);
+        return r;
+    };
+    int off = 0;
+    for (int r = 0; r <= R; r++) {
+        ball_off[r] = off;
+        int cnt = (int)binom(n, r);
+        balls.resize((size_t)(off + cnt) * rs, 0);
+        if (r > 0) {
+            int c[32], k = 0;
+            for (int t = 0; t < r; t++) c[t] = t;
+            for (;;) {
+                for (int t = 0; t < r; t++) balls[(size_t)(off + k) * rs + t] = (uint8_t)c[t];
+                k++;
+                int t = r - 1;
+                while (t >= 0 && c[t] == n - r + t) t--;
+                if (t < 0) break;
+                c[t]++;
+                for (int u = t + 1; u < r; u++) c[u] = c[u - 1] + 1;
+            }
+        }
+        off += cnt;
+    }
+    ball_off[R + 1] = off;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cov_mindist_dev(int32_t q, int32_t n, const uint8_t *d_code, int32_t M, uint8_t *d_dist, void *stream)
+{
+    DtGeom g;
+    int rc = geom(q, n, g);
+    if (rc) return rc;
+    if (M < 0 || (M > 0 && !d_code) || !d_dist) return COV_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t *bm = nullptr;
+    CK(cudaMallocAsync(&bm, (size_t)((g.N + 31) / 32) * 4, st));
+    rc = dt_run(g, d_code, M, d_dist, nullptr, bm, st);
+    cudaFreeAsync(bm, st);
+    return rc;
+}
+
+int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist, int32_t R, void *stream)
+{
+    DtGeom g;
+    int rc = geom(q, n, g);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned long long *d_c = nullptr, h = 0;
+    CK(cudaMallocAsync(&d_c, 8, st));
+    CK(cudaMemsetAsync(d_c, 0, 8, st));
+    k_count_above<<<152 * 8, 256, 0, st>>>(d_dist, g.N, R, d_c);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&h, d_c, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaFreeAsync(d_c, st));
+    CK(cudaStreamSynchronize(st));
+    return (int64_t)h;
+}
+
+int cov_mindist(int32_t q, int32_t n, const uint8_t *code, int32_t M, uint8_t *dist, int64_t *hist,
+                int32_t *radius)
+{
+    DtGeom g;
+    int rc = geom(q, n, g);
+    if (rc) return rc;
+    if (M < 0 || (M > 0 && !code)) return COV_EINVAL;
+    for (long long i = 0; i < (long long)M * n; i++) if (code[i] >= q) return COV_EINVAL;
+    cudaStream_t st = nullptr;
+    uint8_t *d_code = nullptr, *d_D = nullptr;
+    uint32_t *d_bm = nullptr;
+    unsigned long long *d_h = nullptr;
+    const size_t cb = (size_t)std::max(M, 1) * n;
+    if (cudaMalloc(&d_code, cb) != cudaSuccess || cudaMalloc(&d_D, g.N) != cudaSuccess ||
+        cudaMalloc(&d_bm, (size_t)((g.N + 31) / 32) * 4) != cudaSuccess ||
+        cudaMalloc(&d_h, 8 * (COV_MAXN + 2)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_code); cudaFree(d_D); cudaFree(d_bm); cudaFree(d_h);
+        return COV_ENOMEM;
+    }
+    auto done = [&](int r) { cudaFree(d_code); cudaFree(d_D); cudaFree(d_bm); cudaFree(d_h); return r; };
+    if (M > 0 && cudaMemcpy(d_code, code, (size_t)M * n, cudaMemcpyHostToDevice) != cudaSuccess) return done(-100);
+    if (cudaMemset(d_h, 0, 8 * (COV_MAXN + 2)) != cudaSuccess) return done(-100);
+    rc = dt_run(g, d_code, M, d_D, d_h, d_bm, st);
+    if (rc) return done(rc);
+    unsigned long long hh[COV_MAXN + 2];
+    cudaError_t e = cudaMemcpy(hh, d_h, 8 * (COV_MAXN + 2), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return done(-(100 + (int)e));
+    if (dist) {
+        e = cudaMemcpy(dist, d_D, g.N, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return done(-(100 + (int)e));
+    }
+    int rad = 0;
+    for (int v = 0; v <= n + 1; v++) {
+        if (hist) hist[v] = (int64_t)hh[v];
+        if (hh[v]) rad = v;
+    }
+    if (radius) *radius = rad;
+    return done(COV_OK);
+}
+
+int cov_verify(int32_t q, int32_t n, int32_t R, const uint8_t *code, int32_t M, int64_t *uncovered)
+{
+    if (R < 0) return COV_EINVAL;
+    int64_t hist[COV_MAXN + 2];
+    int rc = cov_mindist(q, n, code, M, nullptr, hist, nullptr);
+    if (rc) return rc;
+    int64_t u = 0;
+    for (int v = R + 1; v <= n + 1; v++) u += hist[v];
+    if (uncovered) *uncovered = u;
+    return COV_OK;
+}
+
+int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code, int32_t M, uint16_t *d_cnt,
+                  void *stream)
+{
+    DtGeom g;
+    int rc = geom(q, n, g);
+    if (rc) return rc;
+    if (R < 0 || M < 0 || M > 65535 || (M > 0 && !d_code) || !d_cnt) return COV_EINVAL;
+    if (R > n) R = n;
+    cudaStream_t st = (cudaStream_t)stream;
+    CovSlot d;
+    memset(&d, 0, sizeof d);
+    d.q = q; d.n = n; d.R = R; d.M = M; d.N = g.N;
+    for (int j = 0; j < n; j++) d.pw[j] = g.pw[n - 1 - j];
+    d.rs = R ? R : 1;
+    for (int k = 0; k <= COV_MAXN; k++) d.ppow[k] = (uint32_t)std::min<long long>(ipw(q - 1, k), 0xffffffffLL);
+    std::vector<uint8_t> balls;
+    build_ball_tables(n, R, d.rs, balls, d.ball_off);
+    uint8_t *d_b = nullptr;
+    CK(cudaMallocAsync(&d_b, std::max<size_t>(balls.size(), 1), st));
+    CK(cudaMemcpyAsync(d_b, balls.data(), balls.size(), cudaMemcpyHostToDevice, st));
+    d.ball_sub = d_b;
+    // the uint16 array is updated in aligned 32-bit pairs: pad to even
+    CK(cudaMemsetAsync(d_cnt, 0, (size_t)g.N * 2, st));
+    if (M > 0) {
+        k_count_balls<<<152 * 8, 256, 0, st>>>(d, d_code, M, d_cnt);
+        CK(cudaGetLastError());
+    }
+    // balls is host memory: wait before it goes out of scope
+    CK(cudaStreamSynchronize(st));
+    CK(cudaFreeAsync(d_b, st));
+    return COV_OK;
+}
+
+int cov_count(int32_t q, int32_t n, int32_t R, const uint8_t *code, int32_t M, uint16_t *cnt,
+              int64_t *uncovered)
+{
+    DtGeom g;
+    int rc = geom(q, n, g);
+    if (rc) return rc;
+    if (R < 0 || M < 0 || M > 65535 || (M > 0 && !code)) return COV_EINVAL;
+    for (long long i = 0; i < (long long)M * n; i++) if (code[i] >= q) return COV_EINVAL;
+    uint8_t *d_code = nullptr;
+    uint16_t *d_cnt = nullptr;
+    const size_t nb = ((size_t)g.N + 1) / 2 * 4;     // whole 32-bit pairs
+    if (cudaMalloc(&d_code, (size_t)std::max(M, 1) * n) != cudaSuccess ||
+        cudaMalloc(&d_cnt, nb) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_code); cudaFree(d_cnt);
+        return COV_ENOMEM;
+    }
+    auto done = [&](int r) { cudaFree(d_code); cudaFree(d_cnt); return r; };
+    if (M > 0 && cudaMemcpy(d_code, code, (size_t)M * n, cudaMemcpyHostToDevice) != cudaSuccess) return done(-100);
+    rc = cov_count_dev(q, n, R, d_code, M, d_cnt, nullptr);
+    if (rc) return done(rc);
+    std::vector<uint16_t> tmp;
+    uint16_t *h = cnt;
+    if (!h) { tmp.resize(g.N); h = tmp.data(); }
+    cudaError_t e = cudaMemcpy(h, d_cnt, (size_t)g.N * 2, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return done(-(100 + (int)e));
+    if (uncovered) {
+        int64_t u = 0;
+        for (uint32_t x = 0; x < g.N; x++) u += h[x] == 0;
+        *uncovered = u;
+    }
+    return done(COV_OK);
+}
+
+}  // extern "C"

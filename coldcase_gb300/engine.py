@@ -1,0 +1,184 @@
+"""Host side of the tabu engine: the covsearch2e search behind the C ABI.
+
+Search is one instance (what one `covsearch2e --preset p5b` process does,
+cov/engine/covsearch2e.c:1023-1621); Pool holds many instances that advance
+together in one launch (batched restarts, uneven cells, served requests).
+"""
+import ctypes
+
+import numpy as np
+
+from . import lib as L
+
+DEFAULTS = dict(seed=12345, tabu=0, kick=2, stall=5000, cand=100000)
+
+
+def make_params(q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000,
+                trace=0, trace_cap=0):
+    return L.CovParams(q=q, n=n, R=R, M=M, seed=seed, tabu=tabu, kick=kick, cand=cand,
+                       trace=1 if trace else 0, stall=stall, trace_cap=trace_cap if trace else 0)
+
+
+def slot_bytes(q, n, R, M, **kw):
+    lib = L.load()
+    p = make_params(q, n, R, M, **kw)
+    return int(lib.cov_slot_bytes(ctypes.byref(p)))
+
+
+class Pool:
+    """Up to `max_slots` independent searches, one thread-block cluster of
+    `cluster` CTAs each, advanced together by run()."""
+
+    def __init__(self, max_slots, cluster=1, budget_s=30.0):
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(self.lib.cov_pool_create(int(max_slots), int(cluster), ctypes.byref(h)), "cov_pool_create")
+        self.h = h
+        self.cluster = cluster
+        self.meta = {}
+        L.check(self.lib.cov_pool_set_budget(self.h, float(budget_s)), "cov_pool_set_budget")
+
+    def add(self, q, n, R, M, code=None, random_init=False, seed=12345, tabu=0, kick=2,
+            stall=5000, cand=100000, trace=0, trace_cap=0):
+        """Create an instance from `code` (m x n digits; m may be <, = or > M)."""
+        p = make_params(q, n, R, M, seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand,
+                        trace=trace, trace_cap=trace_cap)
+        if code is None:
+            arr = np.zeros((0, n), dtype=np.uint8)
+        else:
+            arr = L.as_code(code, q, n)
+        slot = ctypes.c_int32(-1)
+        ptr = L.u8ptr(arr) if arr.size else None
+        L.check(self.lib.cov_pool_add(self.h, ctypes.byref(p), ptr, int(arr.shape[0]),
+                                      1 if random_init else 0, ctypes.byref(slot)), "cov_pool_add")
+        self.meta[slot.value] = (q, n, R, M)
+        return slot.value
+
+    def run(self, moves, target=-1):
+        L.check(self.lib.cov_pool_run(self.h, int(moves), int(target)), "cov_pool_run")
+
+    def status(self, slot):
+        st = L.CovStatus()
+        L.check(self.lib.cov_pool_status(self.h, int(slot), ctypes.byref(st)), "cov_pool_status")
+        return {k: getattr(st, k) for k, _ in L.CovStatus._fields_}
+
+    def _digits(self, fn, slot):
+        q, n, R, M = self.meta[slot]
+        out = np.zeros((M, n), dtype=np.uint8)
+        L.check(fn(self.h, int(slot), L.u8ptr(out)), fn.__name__)
+        return out
+
+    def code(self, slot):
+        return self._digits(self.lib.cov_pool_get_code, slot)
+
+    def best(self, slot):
+        return self._digits(self.lib.cov_pool_get_best, slot)
+
+    def cnt(self, slot):
+        q, n, R, M = self.meta[slot]
+        out = np.zeros(q ** n, dtype=np.uint16)
+        L.check(self.lib.cov_pool_get_cnt(self.h, int(slot),
+                                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))),
+                "cov_pool_get_cnt")
+        return out
+
+    def private(self, slot):
+        q, n, R, M = self.meta[slot]
+        out = np.zeros((M, n + 1), dtype=np.int32)
+        L.check(self.lib.cov_pool_get_private(self.h, int(slot), out.ctypes.data_as(L._PI32)),
+                "cov_pool_get_private")
+        return out
+
+    def tabu(self, slot):
+        q, n, R, M = self.meta[slot]
+        out = np.zeros(M * n * q, dtype=np.int32)
+        L.check(self.lib.cov_pool_get_tabu(self.h, int(slot), out.ctypes.data_as(L._PI32)),
+                "cov_pool_get_tabu")
+        return out
+
+    def rng(self, slot):
+        out = np.zeros(4, dtype=np.uint64)
+        L.check(self.lib.cov_pool_get_rng(self.h, int(slot),
+                                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
+                "cov_pool_get_rng")
+        return out
+
+    def trace(self, slot):
+        n = ctypes.c_int64(0)
+        L.check(self.lib.cov_pool_get_trace(self.h, int(slot), None, 0, ctypes.byref(n)), "cov_pool_get_trace")
+        out = np.zeros(n.value, dtype=L.MOVE_DTYPE)
+        if n.value:
+            L.check(self.lib.cov_pool_get_trace(self.h, int(slot),
+                                                out.ctypes.data_as(ctypes.POINTER(L.CovMoveRec)),
+                                                n.value, ctypes.byref(n)), "cov_pool_get_trace")
+        return out
+
+    def remove(self, slot):
+        L.check(self.lib.cov_pool_remove(self.h, int(slot)), "cov_pool_remove")
+        self.meta.pop(slot, None)
+
+    def close(self):
+        if self.h:
+            self.lib.cov_pool_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Search:
+    """One covsearch2e instance on the GPU (a pool with a single slot).
+
+    Parameters are covsearch2e's: -q -n -R -M -s --tabu --kick --stall --cand.
+    """
+
+    def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000,
+                 cluster=8, trace=0, trace_cap=0, budget_s=30.0):
+        self.q, self.n, self.R, self.M = q, n, R, M
+        self.kw = dict(seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand,
+                       trace=trace, trace_cap=trace_cap)
+        self.pool = Pool(1, cluster=cluster, budget_s=budget_s)
+        self.slot = None
+
+    def load(self, code=None, random_init=False):
+        """Initial code as covsearch2e builds it from --in (see Pool.add)."""
+        self.slot = self.pool.add(self.q, self.n, self.R, self.M, code=code,
+                                  random_init=random_init, **self.kw)
+        return self.status()["uncovered"]
+
+    def run(self, moves, target=-1):
+        self.pool.run(moves, target)
+        return self.status()
+
+    def status(self):
+        return self.pool.status(self.slot)
+
+    def code(self):
+        return self.pool.code(self.slot)
+
+    def best(self):
+        return self.pool.best(self.slot)
+
+    def cnt(self):
+        return self.pool.cnt(self.slot)
+
+    def trace(self):
+        return self.pool.trace(self.slot)
+
+    def close(self):
+        self.pool.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -51,6 +51,100 @@ typedef struct {
     int32_t kicked;     /* 1 when the iteration ended in a kick             */
 } cov_move_rec;
 
+
+/* ------------------------------------------------------------------------
+ * Search instances.
+ *
+ * A pool holds up to max_slots independent searches ("slots"); every call
+ * to cov_pool_run advances all live slots together in one launch, one
+ * thread-block cluster of `cluster` CTAs per slot.  A single covsearch2e
+ * process is a pool with one slot and a wide cluster; batched restarts and
+ * served requests are pools with many slots.
+ *
+ * Replaces the process boundary covengine / campaign.py cross today
+ * (cov/engine/covengine:624-643, cov/campaign.py:54-86): the arguments are
+ * covsearch2e's -q -n -R -M -s --tabu --kick --stall --cand
+ * (cov/engine/covsearch2e.c:1042-1095).
+ * --------------------------------------------------------------------- */
+typedef struct cov_pool cov_pool;
+
+typedef struct {
+    int32_t q, n, R, M;
+    uint64_t seed;        /* -s       (covsearch2e default 12345)           */
+    int32_t tabu;         /* --tabu   tenure (default 0)                    */
+    int32_t kick;         /* --kick   codewords moved per kick (default 2)  */
+    int32_t cand;         /* --cand   candidate sample cap (default 100000) */
+    int32_t trace;        /* 1 = keep a cov_move_rec per move               */
+    int64_t stall;        /* --stall  moves without improvement (5000)      */
+    int64_t trace_cap;    /* records kept when trace = 1                    */
+} cov_params;
+
+typedef struct {
+    int64_t it;           /* iterations made (RESULT iters=)                */
+    int64_t uncovered;    /* current uncovered count                        */
+    int64_t best;         /* best uncovered count (RESULT uncovered=)       */
+    int64_t kicks;        /* RESULT kicks=                                  */
+    int64_t trace_n;      /* moves recorded so far                          */
+    int32_t status;       /* 0 or a COV_E* code                             */
+    int32_t finished;     /* 1 once the code covers                         */
+    int32_t ul_valid;     /* uncovered-word list currently valid            */
+    int32_t ul_n;         /* its length (including stale entries)           */
+} cov_status;
+
+/* cov/gemm2/chainsolve.cu:370-375 (chain_run) is the reference's batched
+ * GPU entry; cov_pool_* generalises it to uneven instances. */
+int cov_pool_create(int32_t max_slots, int32_t cluster, cov_pool **out);
+int cov_pool_set_budget(cov_pool *pool, double seconds);   /* per-launch wall limit */
+/* Device bytes one slot with these parameters occupies (0 = invalid). */
+size_t cov_slot_bytes(const cov_params *prm);
+/* Add an instance and build its initial state from `m` codewords
+ * (m*n digits): m == M rebuild, m < M greedy placement (or random digits
+ * when random_init), m > M remove-and-repair -- covsearch2e.c:1156-1255. */
+int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code,
+                 int32_t m, int32_t random_init, int32_t *slot);
+/* Advance every live slot by up to `moves` moves; stop a slot early when
+ * it covers or when best <= target (target < 0: none).
+ * covsearch2e.c:1304-1580. */
+int cov_pool_run(cov_pool *pool, int64_t moves, int64_t target);
+int cov_pool_status(cov_pool *pool, int32_t slot, cov_status *out);
+int cov_pool_get_code(cov_pool *pool, int32_t slot, uint8_t *out);  /* M*n current */
+int cov_pool_get_best(cov_pool *pool, int32_t slot, uint8_t *out);  /* M*n best    */
+int cov_pool_get_cnt(cov_pool *pool, int32_t slot, uint16_t *out);  /* q^n counts  */
+int cov_pool_get_private(cov_pool *pool, int32_t slot, int32_t *out); /* M*(n+1)   */
+int cov_pool_get_tabu(cov_pool *pool, int32_t slot, int32_t *out);  /* M*n*q       */
+int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4);
+int cov_pool_get_trace(cov_pool *pool, int32_t slot, cov_move_rec *out,
+                       int64_t cap, int64_t *n_out);
+int cov_pool_remove(cov_pool *pool, int32_t slot);
+int cov_pool_destroy(cov_pool *pool);
+
+/* ------------------------------------------------------------------------
+ * Verification and transforms (host buffers in, host buffers out; the
+ * *_dev forms take device pointers and a cudaStream_t passed as void*).
+ * --------------------------------------------------------------------- */
+/* Exact uncovered count of a code at radius R: cov/verify_cov.py:109-152
+ * (verify_pure) and :169-230 (verify_numpy) return the same number. */
+int cov_verify(int32_t q, int32_t n, int32_t R, const uint8_t *code, int32_t M,
+               int64_t *uncovered);
+/* Per-word minimum distance to the code (n+1 when M == 0), its histogram
+ * hist[0..n+1] and the covering radius: cov/verify_independent.py:144-186
+ * (run_mindist).  dist and hist may be NULL. */
+int cov_mindist(int32_t q, int32_t n, const uint8_t *code, int32_t M,
+                uint8_t *dist, int64_t *hist, int32_t *radius);
+/* Coverage multiplicity cnt[x] = #{i : d(x,c_i) <= R} over the code as a
+ * multiset, saturated at 65535: the cnt[] of covsearch2e.c:958-967 and the
+ * OUT=2 map of cov/gemm2/dct.cu:360-411. */
+int cov_count(int32_t q, int32_t n, int32_t R, const uint8_t *code, int32_t M,
+              uint16_t *cnt, int64_t *uncovered);
+int cov_mindist_dev(int32_t q, int32_t n, const uint8_t *d_code, int32_t M,
+                    uint8_t *d_dist, void *stream);
+/* d_cnt is updated in aligned 32-bit pairs: it must have room for q^n
+ * entries rounded up to an even number. */
+int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code,
+                  int32_t M, uint16_t *d_cnt, void *stream);
+int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist,
+                            int32_t R, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,183 @@
+"""ctypes wrapper of liboracle.so (test infrastructure only; see oracle.h)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+
+class MoveRec(ctypes.Structure):
+    _fields_ = [("it", ctypes.c_int64), ("u", ctypes.c_int64), ("delta", ctypes.c_int64),
+                ("unc", ctypes.c_int64), ("unc_end", ctypes.c_int64), ("best", ctypes.c_int64),
+                ("ncand", ctypes.c_int32), ("ncw", ctypes.c_int32), ("i", ctypes.c_int32),
+                ("p", ctypes.c_int32), ("v", ctypes.c_int32), ("kicked", ctypes.c_int32)]
+
+
+MOVE_DTYPE = np.dtype([("it", "<i8"), ("u", "<i8"), ("delta", "<i8"), ("unc", "<i8"),
+                       ("unc_end", "<i8"), ("best", "<i8"), ("ncand", "<i4"), ("ncw", "<i4"),
+                       ("i", "<i4"), ("p", "<i4"), ("v", "<i4"), ("kicked", "<i4")])
+
+
+def build():
+    """make -C oracle (the restatement; `ref` also when the reference tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return os.path.join(HERE, "liboracle.so")
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = os.path.join(HERE, "liboracle.so")
+    srcs = [os.path.join(HERE, f) for f in ("covoracle.c", "dtoracle.c", "oracle.h")]
+    if not os.path.exists(path) or any(os.path.getmtime(s) > os.path.getmtime(path) for s in srcs):
+        build()
+    lib = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    u8p = ctypes.POINTER(ctypes.c_uint8)
+    lib.orc_create.restype = P
+    lib.orc_create.argtypes = [ctypes.c_int] * 4 + [ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_longlong, ctypes.c_int, ctypes.c_int]
+    lib.orc_destroy.argtypes = [P]
+    lib.orc_init.restype = ctypes.c_longlong
+    lib.orc_init.argtypes = [P, u8p, ctypes.c_int, ctypes.c_int]
+    lib.orc_run.restype = ctypes.c_longlong
+    lib.orc_run.argtypes = [P, ctypes.c_longlong, ctypes.c_longlong, ctypes.POINTER(MoveRec)]
+    for f in ("orc_uncovered", "orc_best_uncovered", "orc_iters", "orc_kicks"):
+        getattr(lib, f).restype = ctypes.c_longlong
+        getattr(lib, f).argtypes = [P]
+    lib.orc_get_code.argtypes = [P, u8p]
+    lib.orc_get_best.argtypes = [P, u8p]
+    lib.orc_get_cnt.argtypes = [P, ctypes.POINTER(ctypes.c_uint16)]
+    lib.orc_get_tabu.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
+    lib.orc_get_rng.argtypes = [P, ctypes.POINTER(ctypes.c_uint64)]
+    lib.orc_eval_codeword.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+    lib.orc_distinct_code.restype = ctypes.c_int
+    lib.orc_distinct_code.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int, u8p]
+    lib.orc_cover_count.restype = ctypes.c_int
+    lib.orc_cover_count.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint16)]
+    lib.orc_verify_pure.restype = ctypes.c_longlong
+    lib.orc_verify_pure.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int]
+    lib.orc_mindist.restype = ctypes.c_int
+    lib.orc_mindist.argtypes = [ctypes.c_int, ctypes.c_int, u8p, ctypes.c_int, u8p, ctypes.c_int]
+    lib.orc_dilate.restype = ctypes.c_int
+    lib.orc_dilate.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int, u8p]
+    _lib = lib
+    return lib
+
+
+def _u8(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+class Oracle:
+    """One restated covsearch2e p5b search (covsearch2e.c:1023-1621)."""
+
+    def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000, threads=1):
+        self.lib = load()
+        self.q, self.n, self.R, self.M = q, n, R, M
+        self.h = self.lib.orc_create(q, n, R, M, seed, tabu, kick, stall, cand, threads)
+        if not self.h:
+            raise ValueError("oracle: bad parameters")
+
+    def init(self, code=None, random_init=False):
+        a = np.zeros((0, self.n), dtype=np.uint8) if code is None else \
+            np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, self.n))
+        return self.lib.orc_init(self.h, _u8(a) if a.size else None, a.shape[0], 1 if random_init else 0)
+
+    def run(self, moves, target=-1, trace=False):
+        tr = (MoveRec * max(1, int(moves)))() if trace else None
+        made = self.lib.orc_run(self.h, int(moves), int(target), tr)
+        if not trace:
+            return made
+        buf = np.frombuffer(tr, dtype=MOVE_DTYPE, count=max(1, int(moves)))[:made].copy()
+        return buf
+
+    def uncovered(self):
+        return self.lib.orc_uncovered(self.h)
+
+    def best_uncovered(self):
+        return self.lib.orc_best_uncovered(self.h)
+
+    def iters(self):
+        return self.lib.orc_iters(self.h)
+
+    def kicks(self):
+        return self.lib.orc_kicks(self.h)
+
+    def code(self):
+        out = np.zeros((self.M, self.n), dtype=np.uint8)
+        self.lib.orc_get_code(self.h, _u8(out))
+        return out
+
+    def best(self):
+        out = np.zeros((self.M, self.n), dtype=np.uint8)
+        self.lib.orc_get_best(self.h, _u8(out))
+        return out
+
+    def cnt(self):
+        out = np.zeros(self.q ** self.n, dtype=np.uint16)
+        self.lib.orc_get_cnt(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)))
+        return out
+
+    def tabu(self):
+        out = np.zeros(self.M * self.n * self.q, dtype=np.int32)
+        self.lib.orc_get_tabu(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+        return out
+
+    def rng(self):
+        out = np.zeros(4, dtype=np.uint64)
+        self.lib.orc_get_rng(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def distinct_code(code, q, n, M):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, n))
+    out = np.zeros((M, n), dtype=np.uint8)
+    m = lib.orc_distinct_code(q, n, M, _u8(a), a.shape[0], _u8(out))
+    return out[:m]
+
+
+def cover_count(code, q, n, R):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, n))
+    out = np.zeros(q ** n, dtype=np.uint16)
+    lib.orc_cover_count(q, n, R, _u8(a), a.shape[0], out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)))
+    return out
+
+
+def verify_pure(code, q, n, R):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, n))
+    return int(lib.orc_verify_pure(q, n, R, _u8(a), a.shape[0]))
+
+
+def mindist(code, q, n, threads=1):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, n))
+    out = np.zeros(q ** n, dtype=np.uint8)
+    lib.orc_mindist(q, n, _u8(a) if a.size else None, a.shape[0], _u8(out), threads)
+    return out
+
+
+def dilate(code, q, n, R):
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, n))
+    cov = np.zeros(q ** n, dtype=np.uint8)
+    ok = lib.orc_dilate(q, n, R, _u8(a), a.shape[0], _u8(cov))
+    return bool(ok), cov.astype(bool)

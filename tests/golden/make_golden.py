@@ -1,0 +1,182 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs in the build container only (it needs the reference checkout):
+  * engine_runs.json   -- the reference engine binary (oracle/_ref/covsearch2e,
+                          compiled from cov/engine/covsearch2e.c by
+                          `make -C oracle ref`) on a fixed list of runs: the
+                          cell list of cov/engine/selftest.sh:27-38 plus runs
+                          that exercise --in (exact M, fewer words = greedy
+                          top-up, more words = remove-and-repair), --tabu,
+                          small --stall (kicks) and --random-init.  Stored:
+                          arguments, input code, the RESULT fingerprint
+                          uncovered/iters/kicks and the --out file.
+  * verify_cases.json  -- codes with their uncovered counts from the
+                          reference verifiers verify_pure and verify_numpy
+                          (cov/verify_cov.py) and the distance histogram and
+                          covering radius printed by run_mindist
+                          (cov/verify_independent.py), including the known-
+                          answer cases of cov/test_verify.py (whole space,
+                          single word, perfect Hamming codes, direct sums).
+
+Usage: python3 tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import contextlib
+import io
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+DIG = "0123456789abcdefghijklmnopqrstuvwxyz"
+
+
+def code_text(c):
+    return "".join("".join(DIG[int(v)] for v in row) + "\n" for row in c)
+
+
+def run_ref(binary, args, inp_text):
+    with tempfile.TemporaryDirectory() as td:
+        cmd = [binary] + [str(a) for a in args] + ["--out", os.path.join(td, "out.txt"), "--quiet",
+                                                   "--preset", "p5b"]
+        if inp_text is not None:
+            with open(os.path.join(td, "in.txt"), "w") as f:
+                f.write(inp_text)
+            cmd += ["--in", os.path.join(td, "in.txt")]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        m = re.search(r"uncovered=(-?\d+) iters=(\d+) kicks=(\d+)", p.stdout)
+        if not m:
+            raise RuntimeError("no RESULT from %s: %s %s" % (cmd, p.stdout, p.stderr))
+        out = open(os.path.join(td, "out.txt")).read()
+        return dict(uncovered=int(m.group(1)), iters=int(m.group(2)), kicks=int(m.group(3)),
+                    out=out, rc=p.returncode)
+
+
+def engine_runs(binary):
+    runs = []
+    cells = [(2, 6, 2, 12, 300), (3, 6, 2, 12, 300), (5, 5, 2, 30, 200), (6, 6, 3, 41, 400),
+             (6, 6, 3, 45, 400), (7, 4, 1, 60, 300), (3, 11, 4, 81, 120), (6, 8, 4, 169, 40),
+             (4, 5, 0, 1024, 5), (5, 4, 3, 3, 50)]
+    for (q, n, R, M, it) in cells:
+        for s in (1, 2):
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=s, iters=it, tabu=0, stall=5000, kick=2,
+                             random_init=False, code=None))
+    for (q, n, R, M, it) in cells[:8]:
+        runs.append(dict(q=q, n=n, R=R, M=M, seed=3, iters=it, tabu=7, stall=20, kick=2,
+                         random_init=False, code=None))
+        runs.append(dict(q=q, n=n, R=R, M=M, seed=4, iters=it, tabu=3, stall=10, kick=3,
+                         random_init=True, code=None))
+    # --in: exact M, fewer (greedy top-up), more (remove-and-repair)
+    for (q, n, R, M, m, it) in [(4, 6, 1, 420, 420, 10000), (4, 6, 1, 420, 420, 10000),
+                                (6, 6, 3, 41, 41, 400), (5, 5, 2, 30, 20, 200),
+                                (3, 4, 1, 9, 12, 2000), (4, 5, 1, 40, 55, 300),
+                                (5, 5, 2, 20, 30, 300), (6, 6, 3, 41, 60, 200),
+                                (6, 7, 3, 100, 100, 300)]:
+        for s in (1, 2):
+            code = np.random.default_rng(1000 * q + 10 * n + m + s).integers(0, q, (m, n), dtype=np.uint8)
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=s, iters=it, tabu=10, stall=50, kick=2,
+                             random_init=False, code=code_text(code)))
+    # more than 2^19 uncovered words: the uncovered list is not valid, the
+    # entering side is walked and pick_uncovered scans (covsearch2e.c:1327,
+    # 735-753, 1004-1015); the second cell crosses into the valid regime
+    for (q, n, R, M, it) in [(6, 8, 2, 20, 25), (5, 9, 3, 60, 40), (4, 10, 2, 200, 300)]:
+        runs.append(dict(q=q, n=n, R=R, M=M, seed=5, iters=it, tabu=5, stall=5000, kick=2,
+                         random_init=True, code=None))
+    # the plain CPU configuration: q4 n6 R1 M420, tenure 10, uniform codes
+    for s in range(1, 6):
+        code = np.random.default_rng(s).integers(0, 4, (420, 6), dtype=np.uint8)
+        runs.append(dict(q=4, n=6, R=1, M=420, seed=s, iters=10000, tabu=10, stall=5000, kick=2,
+                         random_init=False, code=code_text(code)))
+    for r in runs:
+        args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"],
+                "--iters", r["iters"], "--tabu", r["tabu"], "--stall", r["stall"], "--kick", r["kick"]]
+        if r["random_init"]:
+            args.append("--random-init")
+        r["ref"] = run_ref(binary, args, r["code"])
+    return runs
+
+
+def verify_cases(ref):
+    sys.path.insert(0, os.path.join(ref, "cov"))
+    import verify_cov as V                   # noqa: E402  (the reference verifier)
+    import verify_independent as VI          # noqa: E402
+    import constructions as C                # noqa: E402
+
+    def mindist_report(code, q, n, R):
+        C_ = np.array(code, dtype=np.uint8)
+        buf = io.StringIO()
+        with contextlib.redirect_stdout(buf), contextlib.redirect_stderr(io.StringIO()):
+            ok = VI.run_mindist(C_, q, n, R, q ** n, len(C_), 1 << 20)
+        txt = buf.getvalue()
+        hist = [0] * (n + 2)
+        for d, c in re.findall(r"d=(\d+)\s*:\s*(\d+)", txt):
+            hist[int(d)] = int(c)
+        rad = int(re.search(r"covering radius \(exact\) = (\d+)", txt).group(1))
+        return hist, rad, bool(ok)
+
+    cases = []
+    rng = np.random.default_rng(20260818)
+    for (q, n) in [(2, 6), (3, 5), (3, 6), (4, 5), (5, 4), (6, 4), (7, 3), (2, 9), (4, 6), (6, 6),
+                   (7, 5), (5, 7)]:
+        for R in range(0, min(n, 4) + 1):
+            M = int(rng.integers(1, 13 if q ** n < 5000 else 60))
+            code = [tuple(int(v) for v in row) for row in rng.integers(0, q, (M, n))]
+            code = list(dict.fromkeys(code))
+            cases.append(dict(q=q, n=n, R=R, code=code, src="random"))
+    full = C.full_space(2, 5)
+    cases.append(dict(q=2, n=5, R=0, code=full, src="whole space Z_2^5"))
+    cases.append(dict(q=2, n=5, R=0, code=full[:-1], src="whole space minus one word"))
+    cases.append(dict(q=3, n=5, R=5, code=[tuple([0] * 5)], src="single word at R=n"))
+    cases.append(dict(q=3, n=5, R=4, code=[tuple([0] * 5)], src="single word at R=n-1"))
+    for q, r in [(2, 3), (3, 2), (4, 2), (5, 2)]:
+        H = C.hamming_code(q, r)
+        nn = (q ** r - 1) // (q - 1)
+        cases.append(dict(q=q, n=nn, R=1, code=H, src="Hamming q=%d r=%d" % (q, r)))
+        cases.append(dict(q=q, n=nn, R=1, code=H[:-1], src="Hamming q=%d r=%d minus one" % (q, r)))
+    cases.append(dict(q=3, n=6, R=1, code=C.direct_sum(C.hamming_code(3, 2), C.full_space(3, 2)),
+                      src="direct sum (4,1)+(2,0)"))
+    cases.append(dict(q=3, n=6, R=3, code=C.direct_sum(C.hamming_code(3, 2), [tuple([0, 0])]),
+                      src="direct sum (4,1)+(2,2)"))
+    out = []
+    for c in cases:
+        q, n, R, code = c["q"], c["n"], c["R"], [tuple(int(v) for v in w) for w in c["code"]]
+        pure = V.verify_pure(code, n, q, R, want_witness=False)[0]
+        nump = V.verify_numpy(code, n, q, R, want_witness=False)[0]
+        hist, rad, ok = mindist_report(code, q, n, R)
+        assert pure == nump, c["src"]
+        out.append(dict(q=q, n=n, R=R, src=c["src"], code=[list(w) for w in code], uncovered=pure,
+                        hist=hist, radius=rad, covers=ok))
+    # a recorded cover from the reference's results, verified by both methods there
+    rec = os.path.join(ref, "cov", "results", "K6_9_4_M660.txt")
+    if os.path.exists(rec):
+        code, _ = V.parse_code(rec, 6, 9)
+        out.append(dict(q=6, n=9, R=4, src="cov/results/K6_9_4_M660.txt", code=[list(w) for w in code],
+                        uncovered=V.verify_numpy(code, 9, 6, 4, want_witness=False)[0],
+                        hist=None, radius=None, covers=True))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=%s" % a.ref], check=True)
+    binary = os.path.join(REPO, "oracle", "_ref", "covsearch2e")
+    runs = engine_runs(binary)
+    with open(os.path.join(HERE, "engine_runs.json"), "w") as f:
+        json.dump(runs, f)
+    vc = verify_cases(a.ref)
+    with open(os.path.join(HERE, "verify_cases.json"), "w") as f:
+        json.dump(vc, f)
+    print("engine runs: %d, verify cases: %d" % (len(runs), len(vc)))
+
+
+if __name__ == "__main__":
+    main()

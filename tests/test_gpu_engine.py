@@ -1,0 +1,121 @@
+"""CUDA tabu engine vs the oracle and the reference's golden runs.
+
+Bit-exact: every move record (picked word, candidate count, committed move,
+delta, uncovered counts), the final RNG state, tabu table, coverage counts
+and the best code must equal the oracle's; fingerprints and --out files must
+equal the reference binary's.
+"""
+import numpy as np
+import pytest
+
+from coldcase_gb300 import codefile
+from coldcase_gb300.engine import Pool
+from tests.util import code_from_text, oracle_run
+
+pytestmark = pytest.mark.gpu
+
+
+def private_counts(cnt, code, q, n, R):
+    """(T_k, H_k[j]) of every codeword from a coverage array (small N only)."""
+    N = q ** n
+    pw = q ** np.arange(n - 1, -1, -1, dtype=np.int64)
+    digits = (np.arange(N, dtype=np.int64)[:, None] // pw[None, :]) % q
+    one = cnt == 1
+    out = np.zeros((len(code), n + 1), dtype=np.int64)
+    for k, c in enumerate(code):
+        diff = digits != c[None, :].astype(np.int64)
+        on = one & (diff.sum(axis=1) == R)
+        out[k, 0] = on.sum()
+        out[k, 1:] = diff[on].sum(axis=0)
+    return out
+
+
+def gpu_run(run, cluster):
+    pool = Pool(1, cluster=cluster)
+    code = code_from_text(run["code"], run["n"]) if run["code"] else None
+    s = pool.add(run["q"], run["n"], run["R"], run["M"], code=code, random_init=run["random_init"],
+                 seed=run["seed"], tabu=run["tabu"], kick=run["kick"], stall=run["stall"],
+                 trace=1, trace_cap=max(1, run["iters"]))
+    pool.run(run["iters"])
+    return pool, s
+
+
+def first_diff(a, b):
+    for k in range(min(len(a), len(b))):
+        if a[k].tobytes() != b[k].tobytes():
+            return k, a[k], b[k]
+    return min(len(a), len(b)), None, None
+
+
+@pytest.mark.parametrize("cluster", [1, 4])
+def test_golden_runs_bit_exact(covlib, golden, cluster):
+    runs, _ = golden
+    bad = []
+    for r in runs:
+        pool, s = gpu_run(r, cluster)
+        st = pool.status(s)
+        o, otr = oracle_run(r)
+        gtr = pool.trace(s)
+        ref = r["ref"]
+        assert st["status"] == 0, (r, st)
+        got = (st["best"], st["it"], st["kicks"])
+        want = (ref["uncovered"], ref["iters"], ref["kicks"])
+        out = codefile.format_code(codefile.distinct_code(pool.best(s), r["q"], r["n"], r["M"]), r["q"])
+        ok = got == want and out == ref["out"] and gtr.tobytes() == otr.tobytes()
+        ok = ok and (pool.rng(s) == o.rng()).all() and (pool.tabu(s) == o.tabu()).all()
+        ok = ok and (pool.code(s) == o.code()).all() and (pool.cnt(s) == o.cnt()).all()
+        if not ok:
+            k, g1, o1 = first_diff(gtr, otr)
+            bad.append(dict(cell=(r["q"], r["n"], r["R"], r["M"], r["seed"]), got=got, want=want,
+                            out_ok=out == ref["out"], ntr=(len(gtr), len(otr)), first=k,
+                            gpu=None if g1 is None else g1.tolist(),
+                            orc=None if o1 is None else o1.tolist()))
+        pool.close()
+    assert not bad, bad[:3]
+
+
+def test_private_counts_exact(covlib, golden):
+    runs, _ = golden
+    for r in [x for x in runs if x["q"] ** x["n"] <= 50000 and x["R"] > 0][:12]:
+        pool, s = gpu_run(r, 2)
+        P = pool.private(s)
+        want = private_counts(pool.cnt(s), pool.code(s), r["q"], r["n"], r["R"])
+        assert (P == want).all(), (r["q"], r["n"], r["R"], r["M"])
+        pool.close()
+
+
+def test_plain_q6_n9_parity(covlib):
+    """The single-instance GPU configuration (q6 n9 R4 M700, tenure 20):
+    2000 moves compared move by move with the oracle."""
+    from oracle.pyoracle import Oracle
+    from coldcase_gb300.workloads import uniform_code
+    q, n, R, M = 6, 9, 4, 700
+    code = uniform_code(q, n, M, 1)
+    o = Oracle(q, n, R, M, seed=1, tabu=20, threads=8)
+    o.init(code)
+    otr = o.run(2000, trace=True)
+    pool = Pool(1, cluster=8)
+    s = pool.add(q, n, R, M, code=code, seed=1, tabu=20, trace=1, trace_cap=2000)
+    for _ in range(4):
+        pool.run(500)
+    gtr = pool.trace(s)
+    k, g1, o1 = first_diff(gtr, otr)
+    assert len(gtr) == len(otr) and k == len(otr), (k, g1, o1)
+    assert (pool.cnt(s) == o.cnt()).all()
+    assert (pool.best(s) == o.best()).all()
+
+
+def test_chunked_runs_equal_one_run(covlib, golden):
+    runs, _ = golden
+    r = [x for x in runs if x["q"] == 6 and x["n"] == 6 and x["code"]][0]
+    a, sa = gpu_run(r, 2)
+    b = Pool(1, cluster=2)
+    code = code_from_text(r["code"], r["n"])
+    sb = b.add(r["q"], r["n"], r["R"], r["M"], code=code, seed=r["seed"], tabu=r["tabu"],
+               kick=r["kick"], stall=r["stall"], trace=1, trace_cap=r["iters"])
+    left = r["iters"]
+    while left > 0:
+        k = min(left, 37)
+        b.run(k)
+        left -= k
+    assert a.trace(sa).tobytes() == b.trace(sb).tobytes()

@@ -1,0 +1,24 @@
+"""Helpers shared by the tests."""
+import numpy as np
+
+DIG = "0123456789abcdefghijklmnopqrstuvwxyz"
+
+
+def code_from_text(text, n):
+    rows = [[DIG.index(c) for c in line.strip()] for line in text.splitlines() if line.strip()]
+    return np.array(rows, dtype=np.uint8).reshape(-1, n)
+
+
+def text_from_code(code):
+    return "".join("".join(DIG[int(v)] for v in row) + "\n" for row in code)
+
+
+def oracle_run(run, threads=1):
+    """Replay one golden run on the oracle; returns (oracle, trace)."""
+    from oracle.pyoracle import Oracle
+    o = Oracle(run["q"], run["n"], run["R"], run["M"], seed=run["seed"], tabu=run["tabu"],
+               kick=run["kick"], stall=run["stall"], threads=threads)
+    code = code_from_text(run["code"], run["n"]) if run["code"] else None
+    o.init(code, random_init=run["random_init"])
+    tr = o.run(run["iters"], trace=True)
+    return o, tr
