@@ -1,0 +1,406 @@
+#!/usr/bin/env python3
+"""Headline benchmark: tabu moves/s and coverage words/s at q=7, n=9, R=4.
+
+Workload (one "step"): 64 independent restarts of the q7 n9 R4 M1500
+search (tenure 20, uniform random codes from per-restart seeds), each
+advanced by --moves moves in one launch of the batched engine.  The state
+of the 64 restarts (64 x 40.35M-word counter arrays, ~11 GB) is far larger
+than L2, so no flush is needed between steps.
+
+Printed (rank 0, one JSON line):
+  value        aggregate tabu moves/s of the batched engine, device-timed with
+               CUDA events on the engine's stream over K steps, state resident
+  plain        the same search as one instance on one wide cluster, same GPU
+  coverage     words/s of the uint8 distance transform and of the coverage
+               count over the 7^9 words
+  e2e          moves/s through the public Python API with host buffers: each
+               step re-seeds every restart from a pinned host code (H2D),
+               builds its state, runs --moves moves and reads every best code
+               back (D2H)
+  roofline     the batched kernel's algorithmic bytes / its time vs the
+               measured HBM copy bandwidth
+  cpu_baseline the oracle restatement of the reference engine timed on this
+               host's cores (independent restarts, one per core)
+--impl reference times that CPU path alone (the reference arm).
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "tabu moves/s & coverage words/s (q7,n9,R4); batched/served vs plain, same GPU"
+Q, N_, R_, M_, TENURE, RESTARTS = 7, 9, 4, 1500, 20, 64
+BASE_SEED = 1
+
+
+def workload_name(restarts, moves):
+    return "batched %d restarts q7 n9 R4 M1500 tenure20, %d moves per restart per step" % (restarts, moves)
+
+
+# ------------------------------------------------------------------ CPU ----
+def _cpu_worker(args):
+    """One restart on the oracle (single thread): untimed init, then the
+    timed steps; each step starts at a shared barrier."""
+    idx, steps, moves, barrier = args
+    sys.path.insert(0, HERE)
+    from oracle.pyoracle import Oracle
+    from coldcase_gb300.workloads import uniform_code, instance_seed
+    seed = instance_seed(BASE_SEED, idx)
+    o = Oracle(Q, N_, R_, M_, seed=seed, tabu=TENURE, threads=1)
+    o.init(uniform_code(Q, N_, M_, seed))
+    out = []
+    for _ in range(steps):
+        barrier.wait()
+        t0 = time.monotonic()
+        made = o.run(moves)
+        out.append((made, t0, time.monotonic()))
+    o.close()
+    return out
+
+
+def cpu_measure(warmup, steps, moves, cores=None):
+    """Aggregate moves/s of `cores` concurrent single-thread restarts."""
+    if cores is None:
+        cores = len(os.sched_getaffinity(0))
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "oracle")], check=True)
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    barrier = mgr.Barrier(cores)
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(i, warmup + steps, moves, barrier) for i in range(cores)])
+    mgr.shutdown()
+    rates = []
+    total_m, total_t = 0, 0.0
+    for k in range(warmup, warmup + steps):
+        m = sum(r[k][0] for r in res)
+        t = max(r[k][2] for r in res) - min(r[k][1] for r in res)
+        total_m += m
+        total_t += t
+        rates.append(m / t)
+    return dict(value=total_m / total_t, cores=cores, moves=total_m, seconds=total_t,
+                sample="%d concurrent restarts x %d moves x %d steps (after untimed init)"
+                       % (cores, moves, steps))
+
+
+# --------------------------------------------------------------- clocks ----
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.idx = gpu_index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=["nvidia-smi unavailable"])
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=["no samples"])
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                    reasons=reasons, samples=len(rows))
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-move DRAM bytes of the batched kernel from the committed ncu
+    summary, when one exists (profiles/engine_batched_q7n9.json)."""
+    p = os.path.join(HERE, "profiles", "engine_batched_q7n9.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get("dram_bytes_per_move")
+
+
+def algo_bytes_per_move(q, n, R, M):
+    """Bytes one move of this engine must touch (word granularity):
+    commit  2 S' counter words read + written (4 B each, S' = C(n-1,R)(q-1)^R)
+    sphere  S_R counter words read for the moved codeword (S_R = C(n,R)(q-1)^R)
+    scan    M packed codewords (8 B) for the candidate distances."""
+    Sp = math.comb(n - 1, R) * (q - 1) ** R
+    SR = math.comb(n, R) * (q - 1) ** R
+    return 2 * Sp * 8 + SR * 4 + M * 8
+
+
+# ------------------------------------------------------------------ GPU ----
+def gpu_bench(args, rank, world, dist):
+    import numpy as np
+    import torch
+    from coldcase_gb300 import lib as L
+    from coldcase_gb300.engine import Pool, Search
+    from coldcase_gb300.workloads import uniform_code, instance_seed
+
+    L.load(build_if_missing=True)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    S = args.moves
+    seeds = [instance_seed(BASE_SEED + 7919 * rank, i) for i in range(args.restarts)]
+    codes = [uniform_code(Q, N_, M_, sd) for sd in seeds]
+
+    # ---------------- batched: device-resident state, events on its stream
+    pool = Pool(args.restarts, cluster=args.cluster, budget_s=120.0)
+    stream = torch.cuda.Stream(device=dev)
+    pool.set_stream(stream.cuda_stream)
+    slots = [pool.add(Q, N_, R_, M_, code=codes[i], seed=seeds[i], tabu=TENURE) for i in range(args.restarts)]
+    for _ in range(args.warmup):
+        pool.run(S)
+    it0 = sum(s["it"] for s in pool.status_all(args.restarts))
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    e_all0, e_all1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_all0.record(stream)
+    for k in range(args.steps):
+        evs[k][0].record(stream)
+        if args.graph:
+            pool.graph_run(S, 1)
+        else:
+            pool.run_async(S)
+        evs[k][1].record(stream)
+    e_all1.record(stream)
+    stream.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    st = pool.status_all(args.restarts)
+    moves = sum(s["it"] for s in st) - it0
+    errs = [s["status"] for s in st if s["status"] != 0]
+    if errs:
+        raise RuntimeError("engine status %s" % errs[:4])
+    ms = e_all0.elapsed_time(e_all1)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    t = torch.tensor([ms, float(moves)], dtype=torch.float64, device=dev)
+    if dist:
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms_max, moves_all = float(tmax[0]), float(t[1])
+    else:
+        ms_max, moves_all = ms, float(moves)
+    value = moves_all / (ms_max / 1e3)
+    finished = sum(1 for s in st if s["finished"])
+    best_unc = [s["best"] for s in st]
+
+    # ---------------- e2e: host buffers through the public API
+    e2e = None
+    if not args.no_e2e:
+        pinned = [torch.from_numpy(c).pin_memory() for c in codes]
+        e_moves, e_t = 0, 0.0
+        h2d = sum(int(c.numel()) for c in pinned)
+        d2h = args.restarts * M_ * N_
+        for k in range(args.e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.monotonic()
+            for i, sl in enumerate(slots):
+                pool.load(sl, code=pinned[i].numpy(), seed=seeds[i] + 1 + k)
+            pool.run(S)
+            stt = pool.status_all(args.restarts)
+            for sl in slots:
+                pool.best(sl)
+            e_t += time.monotonic() - t0
+            e_moves += sum(s["it"] for s in stt)
+        e2e = dict(value=e_moves / e_t, unit="moves/s", h2d_bytes_per_step=h2d,
+                   d2h_bytes_per_step=d2h + args.restarts * 72,
+                   note="per step: %d restarts re-seeded from pinned host codes (state build included), "
+                        "%d moves each, every best code read back" % (args.restarts, S))
+    pool.close()
+
+    # ---------------- plain: one instance, one wide cluster, same GPU
+    plain = None
+    if not args.no_plain and rank == 0:
+        eng = Search(Q, N_, R_, M_, seed=seeds[0], tabu=TENURE, cluster=args.plain_cluster, budget_s=120.0)
+        eng.load(codes[0])
+        ps = torch.cuda.Stream(device=dev)
+        eng.pool.set_stream(ps.cuda_stream)
+        for _ in range(args.warmup):
+            eng.pool.run(args.plain_moves)
+        i0 = eng.status()["it"]
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(ps)
+        for _ in range(args.steps):
+            eng.pool.run_async(args.plain_moves)
+        b.record(ps)
+        ps.synchronize()
+        pm = eng.status()["it"] - i0
+        plain = dict(value=pm / (a.elapsed_time(b) / 1e3), unit="moves/s", cluster=args.plain_cluster,
+                     moves=pm)
+        eng.close()
+
+    # ---------------- coverage words/s: distance transform and count
+    cov = None
+    if rank == 0 and not args.no_cov:
+        lib = L.load()
+        code_d = torch.from_numpy(codes[0]).to(dev)
+        Nw = Q ** N_
+        dist_d = torch.empty(Nw, dtype=torch.uint8, device=dev)
+        cnt_d = torch.empty(Nw + 1, dtype=torch.int16, device=dev)
+        cs = torch.cuda.current_stream(dev).cuda_stream
+        for _ in range(3):
+            L.check(lib.cov_mindist_dev(Q, N_, code_d.data_ptr(), M_, dist_d.data_ptr(), cs))
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(5, args.steps)
+        a.record()
+        for _ in range(reps):
+            L.check(lib.cov_mindist_dev(Q, N_, code_d.data_ptr(), M_, dist_d.data_ptr(), cs))
+        b.record()
+        torch.cuda.synchronize()
+        dt_ms = a.elapsed_time(b) / reps
+        for _ in range(2):
+            L.check(lib.cov_count_dev(Q, N_, R_, code_d.data_ptr(), M_, cnt_d.data_ptr(), cs))
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(3):
+            L.check(lib.cov_count_dev(Q, N_, R_, code_d.data_ptr(), M_, cnt_d.data_ptr(), cs))
+        b.record()
+        torch.cuda.synchronize()
+        ct_ms = a.elapsed_time(b) / 3
+        unc_dt = int((dist_d > R_).sum())
+        unc_ct = int((cnt_d[:Nw] == 0).sum())
+        if unc_dt != unc_ct:
+            raise RuntimeError("distance transform and count disagree: %d vs %d" % (unc_dt, unc_ct))
+        cov = dict(dt_words_s=Nw / (dt_ms / 1e3), dt_ms=dt_ms, count_words_s=Nw / (ct_ms / 1e3), count_ms=ct_ms,
+                   dt_traffic_bytes=int(Nw * 3.25), uncovered=unc_dt)
+    return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
+                plain=plain, cov=cov, finished=finished, best_unc=best_unc)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--moves", type=int, default=1000, help="moves per restart per step")
+    ap.add_argument("--restarts", type=int, default=RESTARTS)
+    ap.add_argument("--cluster", type=int, default=2, help="CTAs per restart (batched)")
+    ap.add_argument("--plain-cluster", type=int, default=16)
+    ap.add_argument("--plain-moves", type=int, default=1000)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-moves", type=int, default=12)
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--graph", action="store_true", help="replay each step from a captured CUDA graph")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cov", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        r = cpu_measure(args.warmup, args.steps, args.cpu_moves)
+        line = dict(metric=METRIC, value=r["value"], unit="moves/s", n_gpus=args.gpus, steps=args.steps,
+                    warmup=args.warmup, ms_per_step=1e3 * r["seconds"] / args.steps, higher_is_better=True,
+                    scaling="weak", vs_baseline=None, dtype="int64", data="synthetic: uniform random codes, seeded",
+                    impl="reference",
+                    config=dict(workload=workload_name(args.restarts, args.moves), q=Q, n=N_, R=R_, M=M_,
+                                tenure=TENURE, cpu_sample=r["sample"]),
+                    cpu_baseline=dict(value=r["value"], unit="moves/s", cores=r["cores"], kind="port",
+                                      sample=r["sample"]),
+                    e2e=dict(value=r["value"], unit="moves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        print(json.dumps(line))
+        return 0
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_measure(1, args.cpu_steps, args.cpu_moves)   # before any GPU call
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        dist = tdist
+    r = gpu_bench(args, rank, world, dist)
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        bpm = algo_bytes_per_move(Q, N_, R_, M_)
+        launch_ms = statistics.mean(r["step_ms"])
+        moves_per_launch = r["moves"] / max(1, args.steps) / max(1, world)
+        achieved = bpm * moves_per_launch / (launch_ms / 1e3) / 1e9
+        tpm = profiled_traffic()
+        line = dict(
+            metric=METRIC, value=r["value"], unit="moves/s", n_gpus=world, steps=args.steps, warmup=args.warmup,
+            ms_per_step=r["ms"] / args.steps, higher_is_better=True, scaling="weak", vs_baseline=None,
+            dtype="int32", data="synthetic: uniform random codes, seeded (numpy default_rng)",
+            config=dict(workload=workload_name(args.restarts, args.moves), q=Q, n=N_, R=R_, M=M_,
+                        tenure=TENURE, restarts_per_gpu=args.restarts, moves_per_step=args.moves,
+                        cluster=args.cluster, graph=bool(args.graph),
+                        l2="inputs larger than L2: 64 x 161 MB counter arrays per GPU"),
+            roofline=dict(bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
+                          traffic=(tpm * moves_per_launch) if tpm else None,
+                          peak_source=peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                          algorithmic_bytes_per_move=bpm, kernel="cov_run_kernel"),
+            clocks=r["clocks"],
+            e2e=r["e2e"],
+            gpu_launches=2 * args.steps,
+            plain=r["plain"],
+            batched_over_plain=(r["value"] / world / r["plain"]["value"]) if r["plain"] else None,
+            coverage=r["cov"],
+            finished_restarts=r["finished"],
+        )
+        if cpu:
+            line["cpu_baseline"] = dict(value=cpu["value"], unit="moves/s", cores=cpu["cores"], kind="port",
+                                        sample=cpu["sample"])
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -234,10 +234,11 @@ __device__ __forceinline__ void ul_insert(const CovSlot &d, int ul_valid, uint32
     }
 }
 
-// word w loses coverage by codeword i (leaving side of a commit / -1 ball)
-__device__ __forceinline__ long long word_dec(const CovSlot &d, int ul_valid, int i, uint32_t w, uint64_t pk)
+// word w loses coverage by codeword i (leaving side of a commit / -1 ball);
+// o is the word's counter as loaded
+__device__ __forceinline__ long long word_dec_v(const CovSlot &d, int ul_valid, int i, uint32_t w,
+                                                uint64_t pk, uint32_t o)
 {
-    uint32_t o = cov_ldcg(&d.cw[w]);
     uint32_t c = o & 0xffffu;
     if (c == 0) { set_error(d, COV_EDRIFT); return 0; }
     uint32_t nw = (o - 1u) ^ ((uint32_t)i << 16);
@@ -248,9 +249,9 @@ __device__ __forceinline__ long long word_dec(const CovSlot &d, int ul_valid, in
 }
 
 // word w gains coverage by codeword i (entering side / +1 ball)
-__device__ __forceinline__ long long word_inc(const CovSlot &d, int i, uint32_t w, uint64_t pk)
+__device__ __forceinline__ long long word_inc_v(const CovSlot &d, int i, uint32_t w, uint64_t pk,
+                                                uint32_t o)
 {
-    uint32_t o = cov_ldcg(&d.cw[w]);
     uint32_t c = o & 0xffffu;
     if (c == 0xffffu) { set_error(d, COV_EDRIFT); return 0; }
     uint32_t nw = (o + 1u) ^ ((uint32_t)i << 16);
@@ -258,6 +259,15 @@ __device__ __forceinline__ long long word_inc(const CovSlot &d, int i, uint32_t 
     if (c == 0) return -1;
     if (c == 1) private_adjust(d, (int)(o >> 16), pk, -1);
     return 0;
+}
+
+__device__ __forceinline__ long long word_dec(const CovSlot &d, int ul_valid, int i, uint32_t w, uint64_t pk)
+{
+    return word_dec_v(d, ul_valid, i, w, pk, cov_ldcg(&d.cw[w]));
+}
+__device__ __forceinline__ long long word_inc(const CovSlot &d, int i, uint32_t w, uint64_t pk)
+{
+    return word_inc_v(d, i, w, pk, cov_ldcg(&d.cw[w]));
 }
 
 // ------------------------------------------------------ cluster ops --------
@@ -279,12 +289,28 @@ __device__ void op_commit(const CovSlot &d, const OpParams &P, Smem *LS, int ran
             dunc += word_dec(d, P.ul_valid, P.mi, P.base, P.pc);
             dunc += word_inc(d, P.mi, P.base + P.dv, cov_setnib(P.pc, P.mp, P.mv));
         } else {
+            // every word of the item is distinct, so all 2(q-1) counters are
+            // loaded before any is written: the loads are in flight together
             CovItem it = cov_item(d, subp, R, t, P.base, P.pc);
-            for (int kk = 0; kk < d.q - 1; kk++) {
-                uint32_t a; uint64_t pka;
-                cov_item_word(d, it, kk, a, pka);
-                dunc += word_dec(d, P.ul_valid, P.mi, a, pka);
-                dunc += word_inc(d, P.mi, a + P.dv, cov_setnib(pka, P.mp, P.mv));
+            uint32_t oa[COV_MAXQ - 1], ob[COV_MAXQ - 1];
+            const int qm1 = d.q - 1;
+#pragma unroll
+            for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
+                if (kk < qm1) {
+                    uint32_t a; uint64_t pka;
+                    cov_item_word(d, it, kk, a, pka);
+                    oa[kk] = cov_ldcg(&d.cw[a]);
+                    ob[kk] = cov_ldcg(&d.cw[a + P.dv]);
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
+                if (kk < qm1) {
+                    uint32_t a; uint64_t pka;
+                    cov_item_word(d, it, kk, a, pka);
+                    dunc += word_dec_v(d, P.ul_valid, P.mi, a, pka, oa[kk]);
+                    dunc += word_inc_v(d, P.mi, a + P.dv, cov_setnib(pka, P.mp, P.mv), ob[kk]);
+                }
             }
         }
     }
@@ -1168,6 +1194,19 @@ __global__ void k_unique_cover(CovSlot d, int count, int *out)
     }
 }
 
+// per-launch budget of every listed slot, set on the device so that a run
+// needs no host round trip (and can be captured in a graph)
+__global__ void k_set_budget(CovSlotState *states, const int *map, int nslots, long long moves,
+                             long long target)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nslots) {
+        CovSlotState &s = states[map[k]];
+        s.moves_left = moves;
+        s.target = target;
+    }
+}
+
 __global__ void k_unpack_cnt(const uint32_t *cw, uint32_t N, uint16_t *out)
 {
     for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
@@ -1214,6 +1253,7 @@ struct HostSlot {
     void *arena = nullptr;       // one device allocation for all arrays
     size_t arena_bytes = 0;
     int cluster = 1;
+    int cap = 0;                 // codewords the storage holds
     cov_params prm{};
 };
 
@@ -1224,11 +1264,20 @@ struct cov_pool {
     int cluster = 8;
     std::vector<HostSlot> slots;
     CovSlot *d_slots = nullptr;
-    int *d_map = nullptr;
+    int *d_map = nullptr;            // scratch list for single-slot launches
+    int *d_all = nullptr;            // every used slot
+    int n_all = 0;
+    bool all_dirty = true;
     CovSlotState *d_states = nullptr;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // the pool's own stream
+    cudaStream_t ext = nullptr;      // caller's stream, when set
+    bool use_ext = false;
     double budget_s = 30.0;
     long long launch_moves = 0;      // move budget of the current launch
+    cudaGraphExec_t gexec = nullptr; // captured multi-step run
+    long long g_moves = -1, g_target = -2;
+    int g_steps = 0;
+    cudaStream_t cur_stream() const { return use_ext ? ext : stream; }
 };
 
 static int g_attr_done = 0;
@@ -1242,16 +1291,16 @@ static int ensure_attrs()
     return 0;
 }
 
-static int launch_run(cov_pool *pool, const std::vector<int> &active, int csize, int mode)
+// one cluster per listed slot; d_list holds `count` slot indices on the device
+static int launch_kernel(cov_pool *pool, const int *d_list, int count, int csize, int mode,
+                         long long moves)
 {
-    if (active.empty()) return 0;
-    CK(cudaMemcpyAsync(pool->d_map, active.data(), sizeof(int) * active.size(), cudaMemcpyHostToDevice,
-                       pool->stream));
+    if (count <= 0) return 0;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(active.size() * csize));
+    cfg.gridDim = dim3((unsigned)(count * csize));
     cfg.blockDim = dim3(NT);
     cfg.dynamicSmemBytes = sizeof(Smem);
-    cfg.stream = pool->stream;
+    cfg.stream = pool->cur_stream();
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = (unsigned)csize;
@@ -1263,38 +1312,66 @@ static int launch_run(cov_pool *pool, const std::vector<int> &active, int csize,
     // ops per move <= 2 (walk + move) + a kick's 3 per codeword + 2
     int kmax = 0;
     long long mmax = 0;
-    for (int s : active) {
+    for (int s = 0; s < pool->max_slots; s++) {
+        if (!pool->slots[s].used) continue;
         kmax = std::max(kmax, pool->slots[s].d.kick);
         mmax = std::max<long long>(mmax, pool->slots[s].d.M);
     }
-    long long guard = mode == MODE_GREEDY ? 4 * mmax + 4096
-                                          : pool->launch_moves * (6 + 3LL * kmax) + 4096;
-    CK(cudaLaunchKernelEx(&cfg, cov_run_kernel, (const CovSlot *)pool->d_slots, (const int *)pool->d_map,
-                          mode, budget_ns, guard));
+    long long guard = mode == MODE_GREEDY ? 4 * mmax + 4096 : moves * (6 + 3LL * kmax) + 4096;
+    CK(cudaLaunchKernelEx(&cfg, cov_run_kernel, (const CovSlot *)pool->d_slots, d_list, mode, budget_ns,
+                          guard));
     CK(cudaGetLastError());
     return 0;
+}
+
+// launch for an explicit host list of slots (initialisation paths)
+static int launch_run(cov_pool *pool, const std::vector<int> &active, int csize, int mode)
+{
+    if (active.empty()) return 0;
+    CK(cudaMemcpyAsync(pool->d_map, active.data(), sizeof(int) * active.size(), cudaMemcpyHostToDevice,
+                       pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
+    return launch_kernel(pool, pool->d_map, (int)active.size(), csize, mode, pool->launch_moves);
+}
+
+// device list of every used slot, refreshed after add/remove
+static int refresh_all(cov_pool *pool)
+{
+    if (!pool->all_dirty) return 0;
+    std::vector<int> all;
+    for (int s = 0; s < pool->max_slots; s++) if (pool->slots[s].used) all.push_back(s);
+    if (!all.empty())
+        CK(cudaMemcpy(pool->d_all, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice));
+    pool->n_all = (int)all.size();
+    pool->all_dirty = false;
+    if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+    return 0;
+}
+
+// budget + run for every used slot, enqueued on the current stream
+static int enqueue_step(cov_pool *pool, long long moves, long long target)
+{
+    if (pool->n_all == 0) return 0;
+    k_set_budget<<<(pool->n_all + 127) / 128, 128, 0, pool->cur_stream()>>>(pool->d_states, pool->d_all,
+                                                                          pool->n_all, moves, target);
+    CK(cudaGetLastError());
+    return launch_kernel(pool, pool->d_all, pool->n_all, pool->cluster, MODE_SEARCH, moves);
 }
 
 static int push_slot(cov_pool *pool, int s)
 {
     CK(cudaMemcpyAsync(pool->d_slots + s, &pool->slots[s].d, sizeof(CovSlot), cudaMemcpyHostToDevice,
-                       pool->stream));
+                       pool->cur_stream()));
     return 0;
 }
 
 static int read_state(cov_pool *pool, int s, CovSlotState *out)
 {
-    CK(cudaMemcpyAsync(out, pool->slots[s].st, sizeof(CovSlotState), cudaMemcpyDeviceToHost, pool->stream));
-    CK(cudaStreamSynchronize(pool->stream));
+    CK(cudaMemcpyAsync(out, pool->slots[s].st, sizeof(CovSlotState), cudaMemcpyDeviceToHost, pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
     return 0;
 }
 
-static int write_state(cov_pool *pool, int s, const CovSlotState *in)
-{
-    CK(cudaMemcpyAsync(pool->slots[s].st, in, sizeof(CovSlotState), cudaMemcpyHostToDevice, pool->stream));
-    CK(cudaStreamSynchronize(pool->stream));
-    return 0;
-}
 
 extern "C" {
 
@@ -1314,8 +1391,9 @@ int cov_pool_create(int32_t max_slots, int32_t cluster, cov_pool **out)
     p->slots.resize(max_slots);
     if (cudaMalloc(&p->d_slots, sizeof(CovSlot) * max_slots) != cudaSuccess ||
         cudaMalloc(&p->d_map, sizeof(int) * max_slots) != cudaSuccess ||
+        cudaMalloc(&p->d_all, sizeof(int) * max_slots) != cudaSuccess ||
         cudaMalloc(&p->d_states, sizeof(CovSlotState) * max_slots) != cudaSuccess) {
-        cudaFree(p->d_slots); cudaFree(p->d_map); cudaFree(p->d_states);
+        cudaFree(p->d_slots); cudaFree(p->d_map); cudaFree(p->d_all); cudaFree(p->d_states);
         delete p;
         return COV_ENOMEM;
     }
@@ -1339,19 +1417,21 @@ int cov_pool_remove(cov_pool *pool, int32_t slot)
 {
     if (!pool || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
     HostSlot &h = pool->slots[slot];
-    cudaStreamSynchronize(pool->stream);
+    cudaStreamSynchronize(pool->cur_stream());
     cudaFree(h.arena);
     h = HostSlot();
+    pool->all_dirty = true;
     return COV_OK;
 }
 
 int cov_pool_destroy(cov_pool *pool)
 {
     if (!pool) return COV_OK;
-    cudaStreamSynchronize(pool->stream);
+    cudaStreamSynchronize(pool->cur_stream());
     for (int s = 0; s < pool->max_slots; s++)
         if (pool->slots[s].used) cudaFree(pool->slots[s].arena);
-    cudaFree(pool->d_slots); cudaFree(pool->d_map); cudaFree(pool->d_states);
+    if (pool->gexec) cudaGraphExecDestroy(pool->gexec);
+    cudaFree(pool->d_slots); cudaFree(pool->d_map); cudaFree(pool->d_all); cudaFree(pool->d_states);
     cudaStreamDestroy(pool->stream);
     delete pool;
     return COV_OK;
@@ -1379,30 +1459,27 @@ size_t cov_slot_bytes(const cov_params *prm)
     return b;
 }
 
-// Create an instance and initialise its code exactly as covsearch2e main()
-// does (covsearch2e.c:1156-1255): m == M -> rebuild; m < M -> greedy
-// placement (or --random-init digits); m > M -> remove-and-repair.
-int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int32_t m,
-                 int32_t random_init, int32_t *slot_out)
+// Allocate slot storage for up to `cap` codewords (cap >= M; remove-and-
+// repair needs the whole oversized seed) and fill the descriptor.
+static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out)
 {
-    if (!pool || !prm || (m > 0 && !code) || m < 0) return COV_EINVAL;
     const int q = prm->q, n = prm->n, M = prm->M;
     int R = prm->R;
     if (q < 2 || q > 16 || n < 1 || n > 16 || R < 0 || M < 1 || M > 65535) return COV_EINVAL;
-    if (prm->cand < 1 || prm->kick < 0 || prm->stall < 0) return COV_EINVAL;
-    if (m > 65535) return COV_ERANGE;
+    if (prm->cand < 1 || prm->kick < 0 || prm->stall < 0 || prm->trace_cap < 0) return COV_EINVAL;
+    if (cap > 65535) return COV_ERANGE;
     long long N = ipow_h(q, n);
     if (N >= (1LL << 32) - 1) return COV_EINVAL;
     if (R > n) R = n;
-    for (long long i = 0; i < (long long)m * n; i++) if (code[i] >= q) return COV_EINVAL;
     int s = -1;
     for (int k = 0; k < pool->max_slots; k++) if (!pool->slots[k].used) { s = k; break; }
     if (s < 0) return COV_ERANGE;
-    const int Mw = std::max(M, m);     // remove-and-repair works on m words first
+    const int Mw = std::max(M, cap);
 
     HostSlot h;
     h.prm = *prm;
     h.cluster = pool->cluster;
+    h.cap = Mw;
     CovSlot &d = h.d;
     d.q = q; d.n = n; d.R = R; d.M = M;
     d.N = (uint32_t)N;
@@ -1413,7 +1490,6 @@ int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int
     for (int k = 0; k <= COV_MAXN; k++) d.ppow[k] = (uint32_t)std::min<long long>(ipow_h(q - 1, k), 0xffffffffLL);
     d.tenure = prm->tabu; d.kick = prm->kick; d.cand = prm->cand; d.stall = prm->stall;
     d.ul_cap = UL_CAP_DEFAULT;
-    // subset tables
     std::vector<uint8_t> subs((size_t)n * std::max(d.nsub, 1) * d.rs, 0);
     for (int p = 0; p < n; p++) {
         int pool_[32], np = 0;
@@ -1434,7 +1510,6 @@ int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int
         }
         d.ball_off[R + 1] = off;
     }
-    // one arena for everything
     cov_params p2 = *prm;
     p2.M = Mw;
     size_t need = cov_slot_bytes(&p2) + subs.size() + balls.size() + 1024;
@@ -1457,31 +1532,46 @@ int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int
     uint8_t *dsub = (uint8_t *)take_(subs.size());
     uint8_t *dball = (uint8_t *)take_(balls.size());
     d.sub = dsub; d.ball_sub = dball;
-    d.st = (CovSlotState *)take_(sizeof(CovSlotState));
+    d.st = pool->d_states + s;
     d.trace = prm->trace ? take_((size_t)prm->trace_cap * sizeof(cov_move_rec)) : nullptr;
     d.trace_cap = prm->trace ? prm->trace_cap : 0;
     h.arena = arena;
     h.arena_bytes = need;
     h.st = d.st;
     h.used = true;
+    cudaStream_t st = pool->cur_stream();
+    cudaError_t e = cudaMemcpyAsync(dsub, subs.data(), subs.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dball, balls.data(), balls.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { cudaFree(arena); return -(100 + (int)e); }
+    pool->slots[s] = h;
+    pool->all_dirty = true;
+    *s_out = s;
+    return COV_OK;
+}
 
-    cudaStream_t st = pool->stream;
-    auto fail = [&](int rc) { cudaFree(arena); return rc; };
-#define CKF(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
-    fprintf(stderr, "covgpu: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
-    return fail(-(100 + (int)e_)); } } while (0)
-    CKF(cudaMemcpyAsync(dsub, subs.data(), subs.size(), cudaMemcpyHostToDevice, st));
-    CKF(cudaMemcpyAsync(dball, balls.data(), balls.size(), cudaMemcpyHostToDevice, st));
-    CKF(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
-    CKF(cudaMemsetAsync(d.tabu, 0, (size_t)Mw * n * q * 4, st));
-    CKF(cudaMemsetAsync(d.P, 0, (size_t)Mw * (n + 1) * 4, st));
-    CKF(cudaMemsetAsync(d.ul_bit, 0, (size_t)((N + 31) / 32) * 4, st));
+// (Re)initialise slot s from `m` codewords exactly as covsearch2e main()
+// does (covsearch2e.c:1156-1255): m == M -> rebuild; m < M -> greedy
+// placement (or --random-init digits); m > M -> remove-and-repair.
+static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, int m, int random_init)
+{
+    HostSlot &h = pool->slots[s];
+    CovSlot &d = h.d;
+    const int q = d.q, n = d.n, M = d.M;
+    const long long N = d.N;
+    if (m < 0 || (m > 0 && !code) || m > h.cap) return COV_EINVAL;
+    for (long long i = 0; i < (long long)m * n; i++) if (code[i] >= q) return COV_EINVAL;
+    cudaStream_t st = pool->cur_stream();
+    if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+    CK(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
+    CK(cudaMemsetAsync(d.tabu, 0, (size_t)M * n * q * 4, st));
+    CK(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
+    CK(cudaMemsetAsync(d.ul_bit, 0, (size_t)((N + 31) / 32) * 4, st));
     CovSlotState hs;
     memset(&hs, 0, sizeof hs);
     CovRng rng;
-    cov_rng_seed(rng, prm->seed);
-
-    std::vector<uint64_t> pk((size_t)Mw, 0);
+    cov_rng_seed(rng, seed);
+    std::vector<uint64_t> pk((size_t)std::max(M, m), 0);
     for (int i = 0; i < m; i++) {
         uint64_t v = 0;
         for (int j = 0; j < n; j++) v |= (uint64_t)code[(size_t)i * n + j] << (4 * j);
@@ -1495,91 +1585,89 @@ int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int
         // uniquely covered words.
         CovSlot dm = d;
         dm.M = m;
-        CKF(cudaMemcpyAsync(d.code, pk.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d.code, pk.data(), (size_t)m * 8, cudaMemcpyHostToDevice, st));
         k_mark_balls<<<grid, 256, 0, st>>>(dm, 0, m, +1);
-        CKF(cudaGetLastError());
-        int *d_u = d.g_list ? (int *)d.g_perm : nullptr;
+        CK(cudaGetLastError());
+        int *d_u = (int *)d.g_perm;
         std::vector<int> hu(m);
         std::vector<uint64_t> cur(pk.begin(), pk.begin() + m);
         int ms = m;
         while (ms > M) {
             dm.M = ms;
             k_unique_cover<<<ms, 256, 0, st>>>(dm, ms, d_u);
-            CKF(cudaGetLastError());
-            CKF(cudaMemcpyAsync(hu.data(), d_u, sizeof(int) * ms, cudaMemcpyDeviceToHost, st));
-            CKF(cudaStreamSynchronize(st));
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(hu.data(), d_u, sizeof(int) * ms, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
             int worst = 0;
             for (int i = 1; i < ms; i++) if (hu[i] < hu[worst]) worst = i;
             k_mark_balls<<<grid, 256, 0, st>>>(dm, worst, 1, -1);
-            CKF(cudaGetLastError());
+            CK(cudaGetLastError());
             cur.erase(cur.begin() + worst);
             ms--;
-            CKF(cudaMemcpyAsync(d.code, cur.data(), (size_t)ms * 8, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(d.code, cur.data(), (size_t)ms * 8, cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));
         }
         for (int i = 0; i < M; i++) pk[i] = cur[i];
         have = M;
-        CKF(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
+        CK(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
     }
+    unsigned long long *d_z = (unsigned long long *)d.g_dval;
     if (have < M && !random_init) {
         // greedy placement runs on the device (it samples uncovered words)
-        CKF(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
         if (have > 0) {
             k_mark_balls<<<grid, 256, 0, st>>>(d, 0, have, +1);
-            CKF(cudaGetLastError());
+            CK(cudaGetLastError());
         }
-        unsigned long long *d_z = (unsigned long long *)d.g_dval;
-        CKF(cudaMemsetAsync(d_z, 0, 8, st));
+        CK(cudaMemsetAsync(d_z, 0, 8, st));
         k_count_zero<<<grid, 256, 0, st>>>(d.cw, d.N, d_z);
-        CKF(cudaGetLastError());
+        CK(cudaGetLastError());
         unsigned long long z = 0;
-        CKF(cudaMemcpyAsync(&z, d_z, 8, cudaMemcpyDeviceToHost, st));
-        CKF(cudaStreamSynchronize(st));
+        CK(cudaMemcpyAsync(&z, d_z, 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
         for (int k = 0; k < 4; k++) hs.rng[k] = rng.s[k];
         hs.unc = (long long)z;
         hs.best_unc = hs.unc;
         hs.moves_left = have;        // greedy mode: index of the first word to place
         hs.target = -1;
-        CKF(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
-        pool->slots[s] = h;
+        CK(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
         int rc = push_slot(pool, s);
-        if (rc) { pool->slots[s] = HostSlot(); return fail(rc); }
+        if (rc) return rc;
         std::vector<int> act{s};
         double saved = pool->budget_s;
         pool->budget_s = std::max(saved, 120.0);
         rc = launch_run(pool, act, h.cluster, MODE_GREEDY);
         pool->budget_s = saved;
-        if (rc) { pool->slots[s] = HostSlot(); return fail(rc); }
-        CKF(cudaStreamSynchronize(st));
-        CKF(cudaMemcpyAsync(&hs, d.st, sizeof hs, cudaMemcpyDeviceToHost, st));
-        CKF(cudaStreamSynchronize(st));
-        if (hs.status) { pool->slots[s] = HostSlot(); return fail(hs.status); }
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(&hs, d.st, sizeof hs, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hs.status) return hs.status;
         for (int k = 0; k < 4; k++) rng.s[k] = hs.rng[k];
-        // rebuild cnt|xid from the final code so the xor ids are exact
-        CKF(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
+        // cnt|xid again from the final code so the xor ids are those of M words
+        CK(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
         k_mark_balls<<<grid, 256, 0, st>>>(d, 0, M, +1);
-        CKF(cudaGetLastError());
+        CK(cudaGetLastError());
     } else {
         for (int i = have; i < M; i++) {
             uint64_t v = 0;
             for (int j = 0; j < n; j++) v |= (cov_rng_next(rng) % (uint64_t)q) << (4 * j);
             pk[i] = v;
         }
-        CKF(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
         k_mark_balls<<<grid, 256, 0, st>>>(d, 0, M, +1);
-        CKF(cudaGetLastError());
+        CK(cudaGetLastError());
     }
     // uncovered count, private counts, best code
-    unsigned long long *d_z = (unsigned long long *)d.g_dval;
-    CKF(cudaMemsetAsync(d_z, 0, 8, st));
+    CK(cudaMemsetAsync(d_z, 0, 8, st));
     k_count_zero<<<grid, 256, 0, st>>>(d.cw, d.N, d_z);
-    CKF(cudaGetLastError());
-    CKF(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
     k_private_all<<<grid, 256, 0, st>>>(d);
-    CKF(cudaGetLastError());
-    CKF(cudaMemcpyAsync(d.best, d.code, (size_t)M * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(d.best, d.code, (size_t)M * 8, cudaMemcpyDeviceToDevice, st));
     unsigned long long z = 0;
-    CKF(cudaMemcpyAsync(&z, d_z, 8, cudaMemcpyDeviceToHost, st));
-    CKF(cudaStreamSynchronize(st));
+    CK(cudaMemcpyAsync(&z, d_z, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     memset(&hs, 0, sizeof hs);
     for (int k = 0; k < 4; k++) hs.rng[k] = rng.s[k];
     hs.unc = (long long)z;
@@ -1587,40 +1675,132 @@ int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int
     hs.target = -1;
     hs.ul_valid = 0;
     hs.finished = hs.unc == 0;
-    CKF(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
-    pool->slots[s] = h;
+    CK(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
     int rc = push_slot(pool, s);
-    if (rc) { pool->slots[s] = HostSlot(); return fail(rc); }
-    CKF(cudaStreamSynchronize(st));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(st));
+    return COV_OK;
+}
+
+int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code, int32_t m,
+                 int32_t random_init, int32_t *slot_out)
+{
+    if (!pool || !prm || (m > 0 && !code) || m < 0) return COV_EINVAL;
+    int s = -1;
+    int rc = slot_alloc(pool, prm, std::max(m, prm->M), &s);
+    if (rc) return rc;
+    rc = slot_init(pool, s, prm->seed, code, m, random_init);
+    if (rc) {
+        cudaFree(pool->slots[s].arena);
+        pool->slots[s] = HostSlot();
+        pool->all_dirty = true;
+        return rc;
+    }
     if (slot_out) *slot_out = s;
     return COV_OK;
-#undef CKF
+}
+
+// Re-initialise a live slot with a new seed and code, keeping its storage
+// (same q, n, R, M and search parameters).
+int cov_pool_load(cov_pool *pool, int32_t slot, uint64_t seed, const uint8_t *code, int32_t m,
+                  int32_t random_init)
+{
+    if (!pool || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    int rc = slot_init(pool, slot, seed, code, m, random_init);
+    if (rc) {
+        CovSlotState hs;
+        memset(&hs, 0, sizeof hs);
+        hs.status = rc < 0 && rc > -100 ? rc : COV_ESTATE;
+        cudaMemcpy(pool->slots[slot].st, &hs, sizeof hs, cudaMemcpyHostToDevice);
+    }
+    return rc;
 }
 
 // Advance every live instance by up to `moves` further moves (stopping
 // early at a full cover or when best <= target).  One launch, one cluster
-// per instance.
-int cov_pool_run(cov_pool *pool, int64_t moves, int64_t target)
+// per instance; finished instances return at once.  Asynchronous: the work
+// is queued on the pool's current stream.
+int cov_pool_run_async(cov_pool *pool, int64_t moves, int64_t target)
 {
     if (!pool || moves < 0) return COV_EINVAL;
-    std::vector<int> active;
-    for (int s = 0; s < pool->max_slots; s++) {
-        if (!pool->slots[s].used) continue;
-        CovSlotState hs;
-        int rc = read_state(pool, s, &hs);
-        if (rc) return rc;
-        if (hs.status || hs.unc <= 0) continue;
-        hs.moves_left = moves;
-        hs.target = target;
-        rc = write_state(pool, s, &hs);
-        if (rc) return rc;
-        active.push_back(s);
-    }
-    if (active.empty()) return COV_OK;
-    pool->launch_moves = moves;
-    int rc = launch_run(pool, active, pool->cluster, MODE_SEARCH);
+    int rc = refresh_all(pool);
     if (rc) return rc;
-    CK(cudaStreamSynchronize(pool->stream));
+    pool->launch_moves = moves;
+    return enqueue_step(pool, moves, target);
+}
+
+int cov_pool_sync(cov_pool *pool)
+{
+    if (!pool) return COV_EINVAL;
+    CK(cudaStreamSynchronize(pool->cur_stream()));
+    return COV_OK;
+}
+
+int cov_pool_run(cov_pool *pool, int64_t moves, int64_t target)
+{
+    int rc = cov_pool_run_async(pool, moves, target);
+    if (rc) return rc;
+    return cov_pool_sync(pool);
+}
+
+// `steps` consecutive runs of `moves` moves captured once as a CUDA graph
+// and replayed: one host call per batch of steps.  Asynchronous.
+int cov_pool_graph_run(cov_pool *pool, int64_t moves, int64_t target, int32_t steps)
+{
+    if (!pool || moves < 0 || steps < 1) return COV_EINVAL;
+    int rc = refresh_all(pool);
+    if (rc) return rc;
+    if (pool->n_all == 0) return COV_OK;
+    cudaStream_t st = pool->cur_stream();
+    if (!pool->gexec || pool->g_moves != moves || pool->g_target != target || pool->g_steps != steps) {
+        if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        pool->launch_moves = moves;
+        for (int k = 0; k < steps; k++) {
+            rc = enqueue_step(pool, moves, target);
+            if (rc) { cudaStreamEndCapture(st, &g); if (g) cudaGraphDestroy(g); return rc; }
+        }
+        CK(cudaStreamEndCapture(st, &g));
+        cudaError_t e = cudaGraphInstantiate(&pool->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { pool->gexec = nullptr; return -(100 + (int)e); }
+        pool->g_moves = moves; pool->g_target = target; pool->g_steps = steps;
+    }
+    CK(cudaGraphLaunch(pool->gexec, st));
+    return COV_OK;
+}
+
+// Run on the caller's stream (a cudaStream_t passed as void*); NULL returns
+// to the pool's own stream.
+int cov_pool_set_stream(cov_pool *pool, void *stream)
+{
+    if (!pool) return COV_EINVAL;
+    CK(cudaStreamSynchronize(pool->cur_stream()));
+    pool->ext = (cudaStream_t)stream;
+    pool->use_ext = stream != nullptr;
+    if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+    return COV_OK;
+}
+
+// statuses of slots 0..n-1 in one device-to-host copy (unused slots: status
+// COV_ESTATE)
+int cov_pool_status_all(cov_pool *pool, cov_status *out, int32_t n)
+{
+    if (!pool || !out || n < 0 || n > pool->max_slots) return COV_EINVAL;
+    std::vector<CovSlotState> hs(pool->max_slots);
+    CK(cudaMemcpyAsync(hs.data(), pool->d_states, sizeof(CovSlotState) * pool->max_slots,
+                       cudaMemcpyDeviceToHost, pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
+    for (int s = 0; s < n; s++) {
+        cov_status &o = out[s];
+        memset(&o, 0, sizeof o);
+        if (!pool->slots[s].used) { o.status = COV_ESTATE; continue; }
+        const CovSlotState &h = hs[s];
+        o.it = h.it; o.uncovered = h.unc; o.best = h.best_unc; o.kicks = h.nkicks;
+        o.status = h.status; o.finished = h.unc <= 0; o.ul_valid = h.ul_valid; o.ul_n = h.ul_n;
+        o.trace_n = h.trace_n;
+    }
     return COV_OK;
 }
 
@@ -1648,8 +1828,8 @@ static int get_packed(cov_pool *pool, int32_t slot, bool best, uint8_t *out)
     if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
     const CovSlot &d = pool->slots[slot].d;
     std::vector<uint64_t> pk(d.M);
-    CK(cudaMemcpyAsync(pk.data(), best ? d.best : d.code, (size_t)d.M * 8, cudaMemcpyDeviceToHost, pool->stream));
-    CK(cudaStreamSynchronize(pool->stream));
+    CK(cudaMemcpyAsync(pk.data(), best ? d.best : d.code, (size_t)d.M * 8, cudaMemcpyDeviceToHost, pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
     for (int i = 0; i < d.M; i++)
         for (int j = 0; j < d.n; j++) out[(size_t)i * d.n + j] = (uint8_t)cov_nib(pk[i], j);
     return COV_OK;
@@ -1663,12 +1843,12 @@ int cov_pool_get_cnt(cov_pool *pool, int32_t slot, uint16_t *out)
     if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
     const CovSlot &d = pool->slots[slot].d;
     uint16_t *tmp = nullptr;
-    CK(cudaMallocAsync(&tmp, (size_t)d.N * 2, pool->stream));
-    k_unpack_cnt<<<152 * 4, 256, 0, pool->stream>>>(d.cw, d.N, tmp);
+    CK(cudaMallocAsync(&tmp, (size_t)d.N * 2, pool->cur_stream()));
+    k_unpack_cnt<<<152 * 4, 256, 0, pool->cur_stream()>>>(d.cw, d.N, tmp);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(out, tmp, (size_t)d.N * 2, cudaMemcpyDeviceToHost, pool->stream));
-    CK(cudaFreeAsync(tmp, pool->stream));
-    CK(cudaStreamSynchronize(pool->stream));
+    CK(cudaMemcpyAsync(out, tmp, (size_t)d.N * 2, cudaMemcpyDeviceToHost, pool->cur_stream()));
+    CK(cudaFreeAsync(tmp, pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
     return COV_OK;
 }
 
@@ -1676,8 +1856,8 @@ int cov_pool_get_private(cov_pool *pool, int32_t slot, int32_t *out)
 {
     if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
     const CovSlot &d = pool->slots[slot].d;
-    CK(cudaMemcpyAsync(out, d.P, (size_t)d.M * (d.n + 1) * 4, cudaMemcpyDeviceToHost, pool->stream));
-    CK(cudaStreamSynchronize(pool->stream));
+    CK(cudaMemcpyAsync(out, d.P, (size_t)d.M * (d.n + 1) * 4, cudaMemcpyDeviceToHost, pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
     return COV_OK;
 }
 
@@ -1692,8 +1872,8 @@ int cov_pool_get_trace(cov_pool *pool, int32_t slot, cov_move_rec *out, int64_t 
     if (out && cap > 0) {
         long long k = std::min<long long>(n, cap);
         if (k > 0)
-            CK(cudaMemcpyAsync(out, d.trace, (size_t)k * sizeof(cov_move_rec), cudaMemcpyDeviceToHost, pool->stream));
-        CK(cudaStreamSynchronize(pool->stream));
+            CK(cudaMemcpyAsync(out, d.trace, (size_t)k * sizeof(cov_move_rec), cudaMemcpyDeviceToHost, pool->cur_stream()));
+        CK(cudaStreamSynchronize(pool->cur_stream()));
     }
     if (n_out) *n_out = n;
     return COV_OK;
@@ -1713,8 +1893,8 @@ int cov_pool_get_tabu(cov_pool *pool, int32_t slot, int32_t *out)
 {
     if (!pool || !out || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
     const CovSlot &d = pool->slots[slot].d;
-    CK(cudaMemcpyAsync(out, d.tabu, (size_t)d.M * d.n * d.q * 4, cudaMemcpyDeviceToHost, pool->stream));
-    CK(cudaStreamSynchronize(pool->stream));
+    CK(cudaMemcpyAsync(out, d.tabu, (size_t)d.M * d.n * d.q * 4, cudaMemcpyDeviceToHost, pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
     return COV_OK;
 }
 

@@ -54,8 +54,35 @@ class Pool:
         self.meta[slot.value] = (q, n, R, M)
         return slot.value
 
+    def load(self, slot, code=None, seed=12345, random_init=False):
+        """Re-initialise a slot with a new seed and code, keeping its storage."""
+        q, n, R, M = self.meta[slot]
+        arr = np.zeros((0, n), dtype=np.uint8) if code is None else L.as_code(code, q, n)
+        L.check(self.lib.cov_pool_load(self.h, int(slot), int(seed), L.u8ptr(arr) if arr.size else None,
+                                       int(arr.shape[0]), 1 if random_init else 0), "cov_pool_load")
+
     def run(self, moves, target=-1):
         L.check(self.lib.cov_pool_run(self.h, int(moves), int(target)), "cov_pool_run")
+
+    def run_async(self, moves, target=-1):
+        L.check(self.lib.cov_pool_run_async(self.h, int(moves), int(target)), "cov_pool_run_async")
+
+    def graph_run(self, moves, steps, target=-1):
+        L.check(self.lib.cov_pool_graph_run(self.h, int(moves), int(target), int(steps)), "cov_pool_graph_run")
+
+    def sync(self):
+        L.check(self.lib.cov_pool_sync(self.h), "cov_pool_sync")
+
+    def set_stream(self, stream_handle):
+        """Queue work on an external cudaStream_t (int handle, e.g.
+        torch.cuda.Stream().cuda_stream); None returns to the pool's own."""
+        L.check(self.lib.cov_pool_set_stream(self.h, ctypes.c_void_p(stream_handle) if stream_handle else None),
+                "cov_pool_set_stream")
+
+    def status_all(self, n):
+        arr = (L.CovStatus * n)()
+        L.check(self.lib.cov_pool_status_all(self.h, arr, int(n)), "cov_pool_status_all")
+        return [{k: getattr(a, k) for k, _ in L.CovStatus._fields_} for a in arr]
 
     def status(self, slot):
         st = L.CovStatus()

@@ -71,7 +71,13 @@ SIGNATURES = {
     "cov_pool_set_budget": (ctypes.c_int, [_P, ctypes.c_double]),
     "cov_slot_bytes": (ctypes.c_size_t, [ctypes.POINTER(CovParams)]),
     "cov_pool_add": (ctypes.c_int, [_P, ctypes.POINTER(CovParams), _PU8, _I32, _I32, _PI32]),
+    "cov_pool_load": (ctypes.c_int, [_P, _I32, ctypes.c_uint64, _PU8, _I32, _I32]),
     "cov_pool_run": (ctypes.c_int, [_P, _I64, _I64]),
+    "cov_pool_run_async": (ctypes.c_int, [_P, _I64, _I64]),
+    "cov_pool_graph_run": (ctypes.c_int, [_P, _I64, _I64, _I32]),
+    "cov_pool_sync": (ctypes.c_int, [_P]),
+    "cov_pool_set_stream": (ctypes.c_int, [_P, _P]),
+    "cov_pool_status_all": (ctypes.c_int, [_P, ctypes.POINTER(CovStatus), _I32]),
     "cov_pool_status": (ctypes.c_int, [_P, _I32, ctypes.POINTER(CovStatus)]),
     "cov_pool_get_code": (ctypes.c_int, [_P, _I32, _PU8]),
     "cov_pool_get_best": (ctypes.c_int, [_P, _I32, _PU8]),

@@ -102,10 +102,25 @@ size_t cov_slot_bytes(const cov_params *prm);
  * when random_init), m > M remove-and-repair -- covsearch2e.c:1156-1255. */
 int cov_pool_add(cov_pool *pool, const cov_params *prm, const uint8_t *code,
                  int32_t m, int32_t random_init, int32_t *slot);
+/* Re-initialise a live slot from a new seed and code (m <= the number of
+ * codewords the slot was created for), reusing its device storage. */
+int cov_pool_load(cov_pool *pool, int32_t slot, uint64_t seed,
+                  const uint8_t *code, int32_t m, int32_t random_init);
 /* Advance every live slot by up to `moves` moves; stop a slot early when
  * it covers or when best <= target (target < 0: none).
  * covsearch2e.c:1304-1580. */
 int cov_pool_run(cov_pool *pool, int64_t moves, int64_t target);
+/* The same, queued on the pool's stream without waiting; cov_pool_sync
+ * waits.  cov_pool_graph_run queues `steps` such runs captured once as a
+ * CUDA graph (re-captured when moves/target/steps or the slot set change). */
+int cov_pool_run_async(cov_pool *pool, int64_t moves, int64_t target);
+int cov_pool_graph_run(cov_pool *pool, int64_t moves, int64_t target, int32_t steps);
+int cov_pool_sync(cov_pool *pool);
+/* Queue the pool's work on the caller's cudaStream_t (passed as void*);
+ * NULL returns to the pool's own stream. */
+int cov_pool_set_stream(cov_pool *pool, void *stream);
+/* Statuses of slots 0..n-1 in one copy (unused slots report COV_ESTATE). */
+int cov_pool_status_all(cov_pool *pool, cov_status *out, int32_t n);
 int cov_pool_status(cov_pool *pool, int32_t slot, cov_status *out);
 int cov_pool_get_code(cov_pool *pool, int32_t slot, uint8_t *out);  /* M*n current */
 int cov_pool_get_best(cov_pool *pool, int32_t slot, uint8_t *out);  /* M*n best    */
