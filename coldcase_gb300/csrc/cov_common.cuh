@@ -90,6 +90,8 @@ struct CovSlot {
     uint32_t *ul_bit;            // [ceil(N/32)] list membership
     int ul_cap;
     const uint8_t *sub;          // [n][nsub][rs]
+    const uint8_t *sub1;         // [n][nsub1][rs]: (R-1)-subsets avoiding one position
+    int nsub1;                   // C(n-1,R-1)
     const uint8_t *ball_sub;     // concatenated r-subset tables, r = 0..R
     int ball_off[COV_MAXN + 2];  // start (in subsets) of radius r in ball_sub
     // per-slot global scratch for the rare large cases
@@ -117,8 +119,12 @@ struct CovSlotState {
     int ul_valid;
     int status;                  // 0 ok, negative = COV_E*
     int finished;                // 1 once uncovered reached 0
-    long long stat_ul_pairs;     // diagnostics
+    long long stat_ul_pairs;     // uncovered-list x candidate-codeword pairs tested
     long long stat_commit_words;
+    // cycle counts of the leader's phases, accumulated over launches:
+    // 0 pick, 1 candidates + sample, 2 entering side, 3 select, 4 move op
+    // (commit + sphere), 5 finish, 6 list compaction, 7 other ops
+    unsigned long long prof[8];
 };
 
 // Generic enumeration unit of a sphere of radius r >= 1 around a word:

@@ -42,9 +42,12 @@ namespace cg = cooperative_groups;
 #define PERM_CAP  4096         // candidates kept in shared memory
 #define L_SM      256          // candidate codewords kept in shared memory
 #define RB        1024         // RNG outputs generated per batch
+#define INV_N     1024         // moduli with a reciprocal in shared memory
+#define CODE_SM   4096         // codewords mirrored in the leader's shared memory
+#define NEG_CLUSTER_PAIRS 32768 // list x candidate pairs above which the whole cluster helps
 #define UL_CAP_DEFAULT (1 << 20)
 
-enum { OP_STOP = 0, OP_MOVE, OP_NEGWALK, OP_BALL, OP_RECOMPUTE, OP_ZERO_TABU, OP_REBUILD_UL };
+enum { OP_STOP = 0, OP_MOVE, OP_NEGWALK, OP_BALL, OP_RECOMPUTE, OP_ZERO_TABU, OP_REBUILD_UL, OP_NEG };
 enum {
     PH_PLAN = 0, PH_SELECT, PH_FINISH_MOVE, PH_KICK_START, PH_KICK_PICK, PH_KICK_RECOMP,
     PH_KICK_END, PH_KICK_DONE, PH_REBUILD_DONE, PH_GREEDY, PH_GREEDY_NEXT, PH_STOPPED
@@ -85,6 +88,8 @@ struct Smem {
     uint64_t pu;
     long long uw;
     cov_move_rec rec;
+    unsigned long long prof[8];
+    long long ul_pairs;
     // scratch
     int red_i[NWARP];
     unsigned red_u[NWARP];
@@ -101,6 +106,10 @@ struct Smem {
     uint64_t Lpk[L_SM];
     int32_t neg[L_SM * COV_MAXN];
     uint32_t lbits[L_SM / 32];
+    uint64_t Loh[L_SM][2];     // one-hot digit masks of the candidate codewords
+    uint64_t inv[INV_N + 1];   // floor((2^64-1)/m), m = 1..INV_N
+    uint64_t code_sm[CODE_SM]; // leader's mirror of the packed code (M <= CODE_SM)
+    uint8_t dist8[CODE_SM];    // distances to the sampled word
 };
 
 // ------------------------------------------------------------ helpers -----
@@ -201,6 +210,42 @@ __device__ int block_excl_scan(Smem &S, int flag, int &pos)
     return tot;
 }
 
+// x mod m, exact: a shared-memory reciprocal for small m (at most two
+// corrections), the generic 64-bit remainder otherwise
+__device__ __forceinline__ uint64_t fastmod(const Smem &S, uint64_t x, uint64_t m)
+{
+    if (m <= INV_N) {
+        uint64_t qe = __umul64hi(x, S.inv[m]);
+        uint64_t r = x - qe * m;
+        while (r >= m) r -= m;
+        return r;
+    }
+    return x % m;
+}
+
+// one-hot digit masks: bit j*q + w_j set for every position (q*n <= 128);
+// d(a, b) = n - popc(oh_a & oh_b)
+__device__ __forceinline__ void onehot(uint64_t pk, int n, int q, uint64_t &lo, uint64_t &hi)
+{
+    lo = 0; hi = 0;
+    for (int j = 0; j < n; j++) {
+        int b = j * q + cov_nib(pk, j);
+        if (b < 64) lo |= 1ull << b;
+        else hi |= 1ull << (b - 64);
+    }
+}
+
+__device__ __forceinline__ uint64_t leader_code(const CovSlot &d, const Smem &S, int i)
+{
+    return d.M <= CODE_SM ? S.code_sm[i] : cov_ldcg(&d.code[i]);
+}
+
+__device__ __forceinline__ void leader_set_code(const CovSlot &d, Smem &S, int i, uint64_t pk)
+{
+    cov_stcg(&d.code[i], pk);
+    if (d.M <= CODE_SM) S.code_sm[i] = pk;
+}
+
 // ------------------------------------------------ private-count upkeep -----
 // Word w (packed pkw) just became (s=+1) or stopped being (s=-1) privately
 // covered by codeword k.  If w sits on k's distance-R sphere, T_k and H_k[j]
@@ -208,7 +253,10 @@ __device__ int block_excl_scan(Smem &S, int flag, int &pos)
 __device__ __forceinline__ void private_adjust(const CovSlot &d, int k, uint64_t pkw, int s)
 {
     if (k < 0 || k >= d.M) { set_error(d, COV_EDRIFT); return; }
-    uint64_t D = cov_spread(pkw ^ cov_ldcg(&d.code[k]));
+    extern __shared__ __align__(16) unsigned char cov_smem[];
+    const uint64_t ck = d.M <= CODE_SM ? reinterpret_cast<const Smem *>(cov_smem)->code_sm[k]
+                                       : cov_ldcg(&d.code[k]);
+    uint64_t D = cov_spread(pkw ^ ck);
     if (__popcll(D) != d.R) return;
     int32_t *Pk = d.P + (size_t)k * (d.n + 1);
     atomicAdd(&Pk[0], s);
@@ -276,80 +324,197 @@ __device__ __forceinline__ uint32_t sphere_items(const CovSlot &d, int r, int ns
     return r == 0 ? 1u : (uint32_t)nsubs * d.ppow[r - 1];
 }
 
-// Commit of move (i: p -> v): covsearch2e.c:450-493 (mode 1), 562-590.
-__device__ void op_commit(const CovSlot &d, const OpParams &P, Smem *LS, int rank, int csize)
+// the CTA's share of a change in the uncovered count: reduced in the CTA,
+// then one atomic into the leader's shared memory
+__device__ __forceinline__ void cta_add_dunc(long long dunc, Smem *LS)
 {
-    const int R = d.R;
-    const uint8_t *subp = d.sub + (size_t)P.mp * d.nsub * d.rs;
-    const uint32_t nit = sphere_items(d, R, d.nsub);
+    __shared__ long long cta_dunc;
+    if (threadIdx.x == 0) cta_dunc = 0;
+    __syncthreads();
+    dunc = warp_sum(dunc);
+    if ((threadIdx.x & 31) == 0 && dunc != 0) atomicAdd((unsigned long long *)&cta_dunc, (unsigned long long)dunc);
+    __syncthreads();
+    if (threadIdx.x == 0 && cta_dunc != 0) atomicAdd(&LS->dunc, (unsigned long long)cta_dunc);
+}
+
+// add v to the shared counter of every position of a subset, once per group
+// of lanes holding the same subset
+__device__ __forceinline__ void group_add_h(int *partH, int key, int v, const uint8_t *ps, int r, int extra)
+{
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, key);
+    const int tot = __reduce_add_sync(grp, v);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1 && tot) {
+        for (int s2 = 0; s2 < r; s2++) atomicAdd(&partH[ps[s2]], tot);
+        if (extra >= 0) atomicAdd(&partH[extra], tot);
+    }
+}
+
+// One move (i: p -> v) in a single pass over the cluster.
+//  * Commit, covsearch2e.c:450-493 (mode 1) / 562-590: for every pattern
+//    of R positions avoiding p, the leaving word a (d(a,c)=R, a_p=c_p) loses
+//    codeword i and the entering word b = a + dv gains it.
+//  * The private counts of i follow the move exactly without a new sphere
+//    walk: d(w,c') = d(w,c) + [w_p == c_p] - [w_p == v], so only words with
+//    w_p in {c_p, v} change sphere membership -- the leaving words (out),
+//    the entering words (in), X = {w_p = v, d(w,c) = R} (out) and
+//    Y = {w_p = c_p, d(w,c) = R-1} (in); X = Y + dv.  The counts of X and Y
+//    are not changed by the move, so they are read in the same pass.
+// The change of T_i / H_i goes to the leader's accT / accH.
+__device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank, int csize)
+{
+    const int R = d.R, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) S.partT = 0;
+    if (threadIdx.x < COV_MAXN) S.partH[threadIdx.x] = 0;
+    __syncthreads();
     long long dunc = 0;
-    const uint32_t stride = (uint32_t)csize * NT;
-    for (uint32_t t = (uint32_t)rank * NT + threadIdx.x; t < nit; t += stride) {
-        if (R == 0) {
-            dunc += word_dec(d, P.ul_valid, P.mi, P.base, P.pc);
-            dunc += word_inc(d, P.mi, P.base + P.dv, cov_setnib(P.pc, P.mp, P.mv));
-        } else {
-            // every word of the item is distinct, so all 2(q-1) counters are
-            // loaded before any is written: the loads are in flight together
-            CovItem it = cov_item(d, subp, R, t, P.base, P.pc);
-            uint32_t oa[COV_MAXQ - 1], ob[COV_MAXQ - 1];
-            const int qm1 = d.q - 1;
+    int T = 0;
+    const uint32_t wid = (uint32_t)rank * NWARP + (threadIdx.x >> 5);
+    const uint32_t wstride = (uint32_t)csize * NWARP * 32;
+    if (R == 0) {
+        if (rank == 0 && threadIdx.x == 0) {
+            const uint32_t oa = cov_ldcg(&d.cw[P.base]);
+            const uint32_t ob = cov_ldcg(&d.cw[P.base + P.dv]);
+            T -= (oa & 0xffffu) == 1;
+            T += (ob & 0xffffu) == 0;
+            dunc += word_dec_v(d, P.ul_valid, P.mi, P.base, P.pc, oa);
+            dunc += word_inc_v(d, P.mi, P.base + P.dv, P.pcn, ob);
+        }
+    } else {
+        // leaving / entering pairs
+        const uint8_t *subp = d.sub + (size_t)P.mp * d.nsub * d.rs;
+        const uint32_t nit = (uint32_t)d.nsub * d.ppow[R - 1];
+        const uint32_t nstep = (nit + 31) / 32 * 32;
+        const int qm1 = d.q - 1;
+        for (uint32_t t0 = wid * 32; t0 < nstep; t0 += wstride) {
+            const uint32_t t = t0 + lane;
+            int dt = 0;
+            int key = -1;
+            const uint8_t *ps = subp;
+            if (t < nit) {
+                // every word of the item is distinct: all 2(q-1) counters are
+                // loaded before any is written, so the loads are in flight together
+                CovItem it = cov_item(d, subp, R, t, P.base, P.pc);
+                key = (int)(t / d.ppow[R - 1]);
+                ps = it.ps;
+                uint32_t oa[COV_MAXQ - 1], ob[COV_MAXQ - 1];
 #pragma unroll
-            for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
-                if (kk < qm1) {
-                    uint32_t a; uint64_t pka;
-                    cov_item_word(d, it, kk, a, pka);
-                    oa[kk] = cov_ldcg(&d.cw[a]);
-                    ob[kk] = cov_ldcg(&d.cw[a + P.dv]);
+                for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
+                    if (kk < qm1) {
+                        uint32_t a; uint64_t pka;
+                        cov_item_word(d, it, kk, a, pka);
+                        oa[kk] = cov_ldcg(&d.cw[a]);
+                        ob[kk] = cov_ldcg(&d.cw[a + P.dv]);
+                    }
+                }
+#pragma unroll
+                for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
+                    if (kk < qm1) {
+                        uint32_t a; uint64_t pka;
+                        cov_item_word(d, it, kk, a, pka);
+                        dt -= (oa[kk] & 0xffffu) == 1;
+                        dt += (ob[kk] & 0xffffu) == 0;
+                        dunc += word_dec_v(d, P.ul_valid, P.mi, a, pka, oa[kk]);
+                        dunc += word_inc_v(d, P.mi, a + P.dv, cov_setnib(pka, P.mp, P.mv), ob[kk]);
+                    }
                 }
             }
+            T += dt;
+            if (t0 < nit) group_add_h(S.partH, key, dt, ps, R, -1);
+        }
+        // X / Y pairs: (R-1)-subsets avoiding p
+        if (R == 1) {
+            if (rank == 0 && threadIdx.x == 0) {
+                const int dy = (int)((cov_ldcg(&d.cw[P.base]) & 0xffffu) == 1) -
+                               (int)((cov_ldcg(&d.cw[P.base + P.dv]) & 0xffffu) == 1);
+                T += dy;
+                if (dy) atomicAdd(&S.partH[P.mp], dy);
+            }
+        } else {
+            const uint8_t *subq = d.sub1 + (size_t)P.mp * d.nsub1 * d.rs;
+            const uint32_t pq = d.ppow[R - 2];
+            const uint32_t nxy = (uint32_t)d.nsub1 * pq;
+            const uint32_t nstep2 = (nxy + 31) / 32 * 32;
+            for (uint32_t t0 = wid * 32; t0 < nstep2; t0 += wstride) {
+                const uint32_t t = t0 + lane;
+                int dy = 0;
+                int key = -1;
+                const uint8_t *ps = subq;
+                if (t < nxy) {
+                    CovItem it = cov_item(d, subq, R - 1, t, P.base, P.pc);
+                    key = (int)(t / pq);
+                    ps = it.ps;
+                    uint32_t cy[COV_MAXQ - 1], cx[COV_MAXQ - 1];
 #pragma unroll
-            for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
-                if (kk < qm1) {
-                    uint32_t a; uint64_t pka;
-                    cov_item_word(d, it, kk, a, pka);
-                    dunc += word_dec_v(d, P.ul_valid, P.mi, a, pka, oa[kk]);
-                    dunc += word_inc_v(d, P.mi, a + P.dv, cov_setnib(pka, P.mp, P.mv), ob[kk]);
+                    for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
+                        if (kk < qm1) {
+                            uint32_t y; uint64_t pky;
+                            cov_item_word(d, it, kk, y, pky);
+                            cy[kk] = cov_ldcg(&d.cw[y]);
+                            cx[kk] = cov_ldcg(&d.cw[y + P.dv]);
+                        }
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < COV_MAXQ - 1; kk++)
+                        if (kk < qm1) dy += (int)((cy[kk] & 0xffffu) == 1) - (int)((cx[kk] & 0xffffu) == 1);
                 }
+                T += dy;
+                if (t0 < nxy) group_add_h(S.partH, key, dy, ps, R - 1, P.mp);
             }
         }
     }
-    dunc = warp_sum(dunc);
-    if ((threadIdx.x & 31) == 0 && dunc != 0) atomicAdd(&LS->dunc, (unsigned long long)dunc);
+    cta_add_dunc(dunc, LS);
+    T = warp_sum(T);
+    if (lane == 0 && T) atomicAdd(&S.partT, T);
+    __syncthreads();
+    if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
+    if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
 }
 
 // T and H of the codeword with packed digits pc at word index base: one
 // walk of its distance-R sphere (covsearch2e.c:621-650, read side only).
+// Work unit: one R-subset and a block of 32 assignments of its first R-1
+// positions, one per lane, so that the warp shares the subset and adds its
+// count to the R position counters once.
 __device__ void op_recompute(const CovSlot &d, uint32_t base, uint64_t pc, Smem &S, Smem *LS,
                              int rank, int csize)
 {
     const int R = d.R;
+    const int lane = threadIdx.x & 31;
     if (threadIdx.x == 0) S.partT = 0;
     if (threadIdx.x < COV_MAXN) S.partH[threadIdx.x] = 0;
     __syncthreads();
-    const uint8_t *fs = d.ball_sub + (size_t)d.ball_off[R] * d.rs;
-    const uint32_t nit = sphere_items(d, R, d.nfsub);
-    const uint32_t stride = (uint32_t)csize * NT;
     int T = 0;
-    for (uint32_t t = (uint32_t)rank * NT + threadIdx.x; t < nit; t += stride) {
-        if (R == 0) {
-            T += (cnt_of(d, base) == 1);
-        } else {
-            CovItem it = cov_item(d, fs, R, t, base, pc);
+    if (R == 0) {
+        if (rank == 0 && threadIdx.x == 0) T = (cnt_of(d, base) == 1);
+    } else {
+        const uint8_t *fs = d.ball_sub + (size_t)d.ball_off[R] * d.rs;
+        const uint32_t pp = d.ppow[R - 1];
+        const uint32_t nblk = (pp + 31) / 32;
+        const uint32_t units = (uint32_t)d.nfsub * nblk;
+        const uint32_t gw = (uint32_t)rank * NWARP + (threadIdx.x >> 5);
+        const uint32_t wstride = (uint32_t)csize * NWARP;
+        for (uint32_t u = gw; u < units; u += wstride) {
+            const uint32_t sub = u / nblk;
+            const uint32_t r = (u - sub * nblk) * 32 + lane;
             int t1 = 0;
-            for (int kk = 0; kk < d.q - 1; kk++) {
-                uint32_t w; uint64_t pk;
-                cov_item_word(d, it, kk, w, pk);
-                t1 += (cnt_of(d, w) == 1);
+            if (r < pp) {
+                CovItem it = cov_item(d, fs, R, sub * pp + r, base, pc);
+                for (int kk = 0; kk < d.q - 1; kk++) {
+                    uint32_t w; uint64_t pk;
+                    cov_item_word(d, it, kk, w, pk);
+                    t1 += (cnt_of(d, w) == 1);
+                }
             }
-            if (t1) {
+            t1 = warp_sum(t1);
+            if (lane == 0 && t1) {
                 T += t1;
-                for (int s = 0; s < R; s++) atomicAdd(&S.partH[it.ps[s]], t1);
+                const uint8_t *ps = fs + (size_t)sub * d.rs;
+                for (int s2 = 0; s2 < R; s2++) atomicAdd(&S.partH[ps[s2]], t1);
             }
         }
     }
-    T = warp_sum(T);
-    if ((threadIdx.x & 31) == 0 && T) atomicAdd(&S.partT, T);
+    if (lane == 0 && T) atomicAdd(&S.partT, T);
     __syncthreads();
     if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
     if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
@@ -383,8 +548,7 @@ __device__ void op_ball(const CovSlot &d, const OpParams &P, Smem *LS, int rank,
             else dunc += word_inc(d, P.mi, w, pk);
         }
     }
-    dunc = warp_sum(dunc);
-    if ((threadIdx.x & 31) == 0 && dunc != 0) atomicAdd(&LS->dunc, (unsigned long long)dunc);
+    cta_add_dunc(dunc, LS);
 }
 
 // Entering-side counts by walking, used while the uncovered list is not
@@ -443,6 +607,73 @@ __device__ void op_rebuild_ul(const CovSlot &d, int rank, int csize, cg::cluster
     cl.sync();
     for (uint32_t x = (uint32_t)rank * NT + threadIdx.x; x < d.N; x += (uint32_t)csize * NT) {
         if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) ul_insert(d, 1, x, pk_of_idx(d, x));
+    }
+}
+
+// Entering side from the uncovered-word list (covsearch2e.c:720-734),
+// restricted to v = u_p, the only entries a non-wide candidate reads: for
+// every listed x that is still uncovered and every candidate codeword c with
+// d(x,c) = R+1, neg[c][j] += 1 for each j in D(x,c) with x_j = u_j.
+// Entries first, first+stride, ... of the list.
+__device__ void ul_pass(const CovSlot &d, uint64_t pu, int nL, const uint64_t *Lpk,
+                        const uint64_t (*Loh)[2], int32_t *negp, uint32_t first, uint32_t stride,
+                        bool use_oh)
+{
+    const int n = d.n, q = d.q, R = d.R;
+    const uint32_t n0 = (uint32_t)min(cov_ldcg(&d.st->ul_n), d.ul_cap);
+    const uint64_t nm = nibmask(n);
+    const int match = n - (R + 1);          // positions shared at distance R+1
+    for (uint32_t e = first; e < n0; e += stride) {
+        const uint32_t x = cov_ldcg(&d.ul_idx[e]);
+        const uint64_t px = cov_ldcg(&d.ul_pk[e]);
+        if ((cov_ldcg(&d.cw[x]) & 0xffffu) != 0) continue;     // stale entry
+        const uint64_t eq = ~cov_spread(px ^ pu) & nm;
+        if (use_oh) {
+            uint64_t lo, hi;
+            onehot(px, n, q, lo, hi);
+            for (int l = 0; l < nL; l++) {
+                if (__popcll(lo & Loh[l][0]) + __popcll(hi & Loh[l][1]) != match) continue;
+                uint64_t m = cov_spread(px ^ Lpk[l]) & eq;
+                while (m) {
+                    int j = (__ffsll((long long)m) - 1) >> 2;
+                    atomicAdd(&negp[l * n + j], 1);
+                    m &= m - 1;
+                }
+            }
+        } else {
+            for (int l = 0; l < nL; l++) {
+                uint64_t D = cov_spread(px ^ Lpk[l]);
+                if (__popcll(D) != R + 1) continue;
+                uint64_t m = D & eq;
+                while (m) {
+                    int j = (__ffsll((long long)m) - 1) >> 2;
+                    atomicAdd(&negp[l * n + j], 1);
+                    m &= m - 1;
+                }
+            }
+        }
+    }
+}
+
+// the list pass shared by the whole cluster: every CTA takes a slice of
+// the list; the followers accumulate locally and add into the leader's counts
+__device__ void op_neg(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank, int csize)
+{
+    const int nL = P.nL, n = d.n;
+    if (rank != 0) {
+        for (int l = threadIdx.x; l < nL; l += NT) {
+            S.Lpk[l] = LS->Lpk[l];
+            S.Loh[l][0] = LS->Loh[l][0];
+            S.Loh[l][1] = LS->Loh[l][1];
+        }
+        for (int x = threadIdx.x; x < nL * n; x += NT) S.neg[x] = 0;
+        __syncthreads();
+    }
+    ul_pass(d, P.pu, nL, S.Lpk, S.Loh, S.neg, (uint32_t)rank * NT + threadIdx.x, (uint32_t)csize * NT, true);
+    if (rank != 0) {
+        __syncthreads();
+        for (int x = threadIdx.x; x < nL * n; x += NT)
+            if (S.neg[x]) atomicAdd(&LS->neg[x], S.neg[x]);
     }
 }
 
@@ -554,7 +785,7 @@ __device__ void zero_acc(Smem &S)
 
 // Plan one iteration up to the point where the entering-side counts are
 // needed.  Returns with S.opp set.
-__device__ void leader_plan(const CovSlot &d, Smem &S)
+__device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
 {
     const int tid = threadIdx.x;
     const int n = d.n, R = d.R, M = d.M;
@@ -579,8 +810,12 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
         }
         return;
     }
+    long long t0 = clock64();
     if (S.ul_valid && (long long)cov_ldcg(&d.st->ul_n) > 2 * S.unc + 64) leader_compact(d, S);
     if (tid == 0) {
+        long long t1 = clock64();
+        S.prof[6] += t1 - t0;
+        t0 = t1;
         S.it++;
         S.moves_left--;
         memset(&S.rec, 0, sizeof(S.rec));
@@ -589,6 +824,9 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
     __syncthreads();
     long long uw = leader_pick(d, S);
     if (tid == 0) {
+        long long t1 = clock64();
+        S.prof[0] += t1 - t0;
+        t0 = t1;
         S.uw = uw;
         if (uw < 0) S.status = COV_EDRIFT;
         S.pu = uw >= 0 ? pk_of_idx(d, (uint32_t)uw) : 0;
@@ -599,29 +837,42 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
     const uint64_t pu = S.pu;
 
     // distances to all codewords and the target distance (covsearch2e.c:1342-1351)
+    const bool csm = M <= CODE_SM;
     unsigned dm = 0xffffffffu;
-    for (int i = tid; i < M; i += NT) dm = min(dm, (unsigned)cov_dist(cov_ldcg(&d.code[i]), pu));
+    for (int i = tid; i < M; i += NT) {
+        int dd = cov_dist(leader_code(d, S, i), pu);
+        if (csm) S.dist8[i] = (uint8_t)dd;
+        dm = min(dm, (unsigned)dd);
+    }
     dm = block_min_u32(S, dm);
     const int dtar = ((int)dm <= R + 1) ? R + 1 : (int)dm;
-    // ordered list of codewords at distance dtar (covsearch2e.c:1359-1376)
-    int cntL = 0;
-    for (int i = tid; i < M; i += NT) cntL += (cov_dist(cov_ldcg(&d.code[i]), pu) == dtar);
-    const int nL = block_sum_int(S, cntL);
+    // ordered list of codewords at distance dtar (covsearch2e.c:1359-1376):
+    // always in global memory, the first L_SM also in shared memory with
+    // their packed codes and one-hot masks
+    int nL = 0;
+    for (int c0 = 0; c0 < M; c0 += NT) {
+        int i = c0 + tid;
+        uint64_t pk = 0;
+        int f = 0;
+        if (i < M) {
+            pk = leader_code(d, S, i);
+            f = (csm ? (int)S.dist8[i] : cov_dist(pk, pu)) == dtar;
+        }
+        int pos;
+        int tot = block_excl_scan(S, f, pos);
+        if (f) {
+            const int at = nL + pos;
+            d.g_list[at] = (uint32_t)i;
+            if (at < L_SM) {
+                S.L[at] = (uint32_t)i;
+                S.Lpk[at] = pk;
+                onehot(pk, n, d.q, S.Loh[at][0], S.Loh[at][1]);
+            }
+        }
+        nL += tot;
+    }
     const int Lsm = nL <= L_SM;
     uint32_t *Lp = Lsm ? S.L : d.g_list;
-    {
-        int base = 0;
-        for (int c0 = 0; c0 < M; c0 += NT) {
-            int i = c0 + tid;
-            uint64_t pk = 0;
-            int f = 0;
-            if (i < M) { pk = cov_ldcg(&d.code[i]); f = cov_dist(pk, pu) == dtar; }
-            int pos;
-            int tot = block_excl_scan(S, f, pos);
-            if (f) { Lp[base + pos] = (uint32_t)i; if (Lsm) S.Lpk[base + pos] = pk; }
-            base += tot;
-        }
-    }
     const int ncand = nL * dtar;
     if (ncand == 0) {     // impossible for an uncovered target word
         if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
@@ -645,7 +896,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
         __syncthreads();
         for (int t = tid; t < cnt; t += NT) {
             int s = s0 + t;
-            dval[s] = s + (int32_t)(S.rbuf[t] % (uint64_t)(ncand - s));
+            dval[s] = s + (int32_t)fastmod(S, S.rbuf[t], (uint64_t)(ncand - s));
         }
     }
     __syncthreads();
@@ -661,7 +912,6 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
     if (take < ncand) {
         int c = 0;
         if (tid == 0) {
-            // small and rare: a quadratic-free count through the sorted ids
             for (int s = 0; s < take; s++) {
                 int l = (int)(perm[s] / (uint32_t)dtar), dup = 0;
                 for (int t = 0; t < s; t++) if ((int)(perm[t] / (uint32_t)dtar) == l) { dup = 1; break; }
@@ -675,6 +925,9 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
     if (tid == 0) {
         S.nL = nL; S.dtar = dtar; S.ncand = ncand; S.take = take;
         S.rec.ncand = ncand; S.rec.ncw = ncw;
+        long long t1 = clock64();
+        S.prof[1] += t1 - t0;
+        t0 = t1;
     }
     // entering side
     const int nsm = nL <= L_SM;
@@ -691,9 +944,23 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
         }
         return;
     }
-    {
-        // covsearch2e.c:720-734 restricted to v = u_p (the only entries a
-        // non-wide candidate reads)
+    const bool use_oh = d.q * n <= 128;
+    const long long pairs = (long long)min(cov_ldcg(&d.st->ul_n), d.ul_cap) * nL;
+    if (csize > 1 && Lsm && use_oh && pairs >= NEG_CLUSTER_PAIRS) {
+        if (tid == 0) {
+            OpParams &o = S.opp;
+            o.op = OP_NEG; o.nL = nL; o.dtar = dtar; o.pu = pu;
+            o.L_sm = 1; o.neg_sm = 1; o.ul_valid = 1;
+            S.phase = PH_SELECT;
+            S.prof[2] += clock64() - t0;
+            S.ul_pairs += pairs;
+        }
+        return;
+    }
+    if (Lsm) {
+        ul_pass(d, pu, nL, S.Lpk, S.Loh, negp, tid, NT, use_oh);
+    } else {
+        // oversized candidate list: codes from global memory, nibble test
         const int n0 = min(cov_ldcg(&d.st->ul_n), d.ul_cap);
         const uint64_t nm = nibmask(n);
         for (int e = tid; e < n0; e += NT) {
@@ -702,7 +969,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
             uint64_t px = cov_ldcg(&d.ul_pk[e]);
             uint64_t eq = ~cov_spread(px ^ pu) & nm;
             for (int l = 0; l < nL; l++) {
-                uint64_t pk = Lsm ? S.Lpk[l] : cov_ldcg(&d.code[Lp[l]]);
+                uint64_t pk = cov_ldcg(&d.code[Lp[l]]);
                 uint64_t D = cov_spread(px ^ pk);
                 if (__popcll(D) != R + 1) continue;
                 uint64_t m = D & eq;
@@ -715,7 +982,11 @@ __device__ void leader_plan(const CovSlot &d, Smem &S)
         }
     }
     __syncthreads();
-    if (tid == 0) S.phase = PH_SELECT;
+    if (tid == 0) {
+        S.phase = PH_SELECT;
+        S.prof[2] += clock64() - t0;
+        S.ul_pairs += (long long)min(cov_ldcg(&d.st->ul_n), d.ul_cap) * nL;
+    }
     S.opp.op = -1;   // no op yet: select follows
 }
 
@@ -732,6 +1003,7 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
     int32_t *dval = psm ? S.dval : d.g_dval;
     uint32_t *Lp = Lsm ? S.L : d.g_list;
     int32_t *negp = Lsm ? S.neg : d.g_neg;
+    const long long t0 = clock64();
     // deltas and tabu flags in parallel (shared-memory case); the rare
     // oversized case recomputes them inside the serial scan below
     if (psm) {
@@ -771,10 +1043,10 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
             if (dd < bestd) { bestd = dd; bs = s; nties = 1; }
             else if (dd == bestd) {
                 nties++;
-                if (cov_rng_next(r) % (uint64_t)nties == 0) bs = s;
+                if (fastmod(S, cov_rng_next(r), (uint64_t)nties) == 0) bs = s;
             }
         }
-        if (bs < 0) bs = (int)(cov_rng_next(r) % (uint64_t)take);
+        if (bs < 0) bs = (int)fastmod(S, cov_rng_next(r), (uint64_t)take);
         S.rng = r;
         uint32_t c = perm[bs];
         int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
@@ -798,6 +1070,7 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
         S.ibc[3] = oldv;
         S.rec.i = k; S.rec.p = p; S.rec.v = v; S.rec.delta = dd;
         S.phase = PH_FINISH_MOVE;
+        S.prof[3] += clock64() - t0;
     }
 }
 
@@ -818,15 +1091,16 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
 {
     const int tid = threadIdx.x;
     const int n = d.n, q = d.q;
+    const long long t0 = clock64();
     if (tid == 0) {
         long long dunc = (long long)S.dunc;
         S.unc += dunc;
         if (dunc != S.chosen_delta) S.status = COV_EDRIFT;
         const OpParams &o = S.opp;
-        cov_stcg(&d.code[o.mi], o.pcn);
+        leader_set_code(d, S, o.mi, o.pcn);
         int32_t *Pk = d.P + (size_t)o.mi * (n + 1);
-        cov_stcg(&Pk[0], S.accT);
-        for (int j = 0; j < n; j++) cov_stcg(&Pk[1 + j], S.accH[j]);
+        cov_stcg(&Pk[0], cov_ldcg(&Pk[0]) + S.accT);
+        for (int j = 0; j < n; j++) cov_stcg(&Pk[1 + j], cov_ldcg(&Pk[1 + j]) + S.accH[j]);
         const int oldv = S.ibc[3];
         uint64_t r4 = cov_rng_next(S.rng) % 4ull;
         cov_stcg(&d.tabu[((size_t)o.mi * n + o.mp) * q + oldv], (int32_t)(S.it + d.tenure + (long long)r4));
@@ -846,13 +1120,14 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
             write_trace(d, S);
             S.phase = PH_PLAN;
         }
+        S.prof[5] += clock64() - t0;
     }
     __syncthreads();
 }
 
 // one leader step: consume the result of the previous op, do the serial
 // work, and leave the next op in S.opp
-__device__ void leader_step(const CovSlot &d, Smem &S)
+__device__ void leader_step(const CovSlot &d, Smem &S, int csize)
 {
     const int tid = threadIdx.x;
     for (int guard = 0; guard < 64; guard++) {
@@ -862,7 +1137,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S)
         if (ph == PH_STOPPED) { if (tid == 0) S.opp.op = OP_STOP; return; }
         if (ph == PH_PLAN) {
             if (S.mode == MODE_GREEDY) { if (tid == 0) S.phase = PH_GREEDY; continue; }
-            leader_plan(d, S);
+            leader_plan(d, S, csize);
             __syncthreads();
             if (S.phase == PH_SELECT && S.opp.op == -1) { leader_select(d, S); __syncthreads(); return; }
             return;
@@ -884,8 +1159,8 @@ __device__ void leader_step(const CovSlot &d, Smem &S)
                     S.phase = PH_KICK_DONE;
                 } else {
                     if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
-                    int i = (int)(cov_rng_next(S.rng) % (uint64_t)d.M);
-                    uint64_t pk = cov_ldcg(&d.code[i]);
+                    int i = (int)fastmod(S, cov_rng_next(S.rng), (uint64_t)d.M);
+                    uint64_t pk = leader_code(d, S, i);
                     OpParams &o = S.opp;
                     o.op = OP_BALL; o.sgn = -1; o.mi = i; o.pc = pk; o.base = widx_pk(d, pk);
                     o.ul_valid = S.ul_valid;
@@ -920,7 +1195,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S)
                         pk = cov_setnib(pk, j, (int)(cov_rng_next(S.rng) % (uint64_t)d.q));
                 }
                 OpParams &o = S.opp;
-                cov_stcg(&d.code[o.mi], pk);
+                leader_set_code(d, S, o.mi, pk);
                 o.op = OP_BALL; o.sgn = +1; o.pc = pk; o.base = widx_pk(d, pk);
                 o.ul_valid = S.ul_valid;
                 S.dunc = 0;
@@ -976,7 +1251,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S)
                 if (w < 0) w = (long long)(cov_rng_next(S.rng) % (uint64_t)d.N);
                 uint64_t pk = pk_of_idx(d, (uint32_t)w);
                 int i = S.greedy_i;
-                cov_stcg(&d.code[i], pk);
+                leader_set_code(d, S, i, pk);
                 OpParams &o = S.opp;
                 o.op = OP_BALL; o.sgn = +1; o.mi = i; o.pc = pk; o.base = (uint32_t)w;
                 o.ul_valid = 0;
@@ -1019,6 +1294,11 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
     const bool leader = rank == 0;
     Smem *LS = cl.map_shared_rank(&S, 0);
 
+    if (leader)
+        for (int m = threadIdx.x; m <= INV_N; m += NT)
+            S.inv[m] = m ? 0xffffffffffffffffull / (uint64_t)m : 0;
+    if (d.M <= CODE_SM)
+        for (int i = threadIdx.x; i < d.M; i += NT) S.code_sm[i] = cov_ldcg(&d.code[i]);
     if (leader && threadIdx.x == 0) {
         CovSlotState *st = d.st;
         for (int k = 0; k < 4; k++) S.rng.s[k] = st->rng[k];
@@ -1032,11 +1312,13 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         S.t_deadline = gtimer() + budget_ns;
         S.guard = 0;
         S.opp.op = -1;
+        for (int k = 0; k < 8; k++) S.prof[k] = st->prof[k];
+        S.ul_pairs = st->stat_ul_pairs;
     }
     cl.sync();
     for (;;) {
         if (leader) {
-            leader_step(d, S);
+            leader_step(d, S, csize);
             // safety net: an op budget and the launch deadline bound every
             // launch even if the phase machine never reaches a move boundary
             if (threadIdx.x == 0 && S.opp.op != OP_STOP &&
@@ -1052,13 +1334,18 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         const OpParams &P = S.opl;
         const int op = P.op;
         if (op == OP_STOP) break;
+        const long long top = clock64();
         if (op == OP_MOVE) {
-            op_commit(d, P, LS, rank, csize);
-            cl.sync();
-            op_recompute(d, P.basen, P.pcn, S, LS, rank, csize);
+            op_move(d, P, S, LS, rank, csize);
+            if (d.M <= CODE_SM && threadIdx.x == 0) S.code_sm[P.mi] = P.pcn;
         } else if (op == OP_NEGWALK) {
             op_negwalk(d, P, S, LS, rank, csize, cl);
+        } else if (op == OP_NEG) {
+            op_neg(d, P, S, LS, rank, csize);
         } else if (op == OP_BALL) {
+            // a +1 ball places the slot's new codeword: mirror it first
+            if (P.sgn > 0 && d.M <= CODE_SM && threadIdx.x == 0) S.code_sm[P.mi] = P.pc;
+            __syncthreads();
             op_ball(d, P, LS, rank, csize);
         } else if (op == OP_RECOMPUTE) {
             op_recompute(d, P.basen, P.pcn, S, LS, rank, csize);
@@ -1068,6 +1355,12 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
             op_rebuild_ul(d, rank, csize, cl);
         }
         cl.sync();
+        if (leader && threadIdx.x == 0) {
+            const long long dt = clock64() - top;
+            if (op == OP_MOVE) S.prof[4] += dt;
+            else if (op == OP_NEGWALK || op == OP_NEG) S.prof[2] += dt;
+            else S.prof[7] += dt;
+        }
     }
     // no CTA may leave while another can still read the leader's shared memory
     cl.sync();
@@ -1078,6 +1371,8 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         st->since_improve = S.since_improve; st->nkicks = S.nkicks;
         st->moves_left = S.moves_left; st->trace_n = S.trace_n;
         st->ul_valid = S.ul_valid;
+        for (int k = 0; k < 8; k++) st->prof[k] = S.prof[k];
+        st->stat_ul_pairs = S.ul_pairs;
         int s0 = atomicAdd(&st->status, 0);
         st->status = S.status ? S.status : s0;
         st->finished = S.unc <= 0;
@@ -1126,34 +1421,45 @@ __global__ void k_count_zero(const uint32_t *cw, uint32_t N, unsigned long long 
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
-// P[k] = (T_k, H_k) for every codeword from scratch
+// P[k] = (T_k, H_k) for every codeword from scratch; one warp per
+// (codeword, R-subset, block of 32 prefix assignments)
 __global__ void k_private_all(CovSlot d)
 {
     const int R = d.R, n = d.n;
+    const int lane = threadIdx.x & 31;
     const uint8_t *fs = d.ball_sub + (size_t)d.ball_off[R] * d.rs;
-    const uint32_t per = sphere_items(d, R, d.nfsub);
-    const unsigned long long total = (unsigned long long)per * d.M;
-    for (unsigned long long g = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
-         g += (unsigned long long)gridDim.x * blockDim.x) {
-        const int k = (int)(g / per);
-        const uint32_t t = (uint32_t)(g - (unsigned long long)k * per);
+    const uint32_t pp = R ? d.ppow[R - 1] : 1;
+    const uint32_t nblk = (pp + 31) / 32;
+    const unsigned long long per = (unsigned long long)(R ? d.nfsub : 1) * nblk;
+    const unsigned long long units = per * d.M;
+    const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long wstride = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long u = gw; u < units; u += wstride) {
+        const int k = (int)(u / per);
+        const uint32_t rest = (uint32_t)(u - (unsigned long long)k * per);
         const uint64_t pc = d.code[k];
         const uint32_t base = widx_pk(d, pc);
         int32_t *Pk = d.P + (size_t)k * (n + 1);
         if (R == 0) {
-            if ((d.cw[base] & 0xffffu) == 1) atomicAdd(&Pk[0], 1);
+            if (lane == 0 && (d.cw[base] & 0xffffu) == 1) atomicAdd(&Pk[0], 1);
             continue;
         }
-        CovItem it = cov_item(d, fs, R, t, base, pc);
+        const uint32_t sub = rest / nblk;
+        const uint32_t r = (rest - sub * nblk) * 32 + lane;
         int t1 = 0;
-        for (int kk = 0; kk < d.q - 1; kk++) {
-            uint32_t w; uint64_t pk;
-            cov_item_word(d, it, kk, w, pk);
-            t1 += (d.cw[w] & 0xffffu) == 1;
+        if (r < pp) {
+            CovItem it = cov_item(d, fs, R, sub * pp + r, base, pc);
+            for (int kk = 0; kk < d.q - 1; kk++) {
+                uint32_t w; uint64_t pk;
+                cov_item_word(d, it, kk, w, pk);
+                t1 += (d.cw[w] & 0xffffu) == 1;
+            }
         }
-        if (t1) {
+        t1 = warp_sum(t1);
+        if (lane == 0 && t1) {
             atomicAdd(&Pk[0], t1);
-            for (int s = 0; s < R; s++) atomicAdd(&Pk[1 + it.ps[s]], t1);
+            const uint8_t *ps = fs + (size_t)sub * d.rs;
+            for (int s2 = 0; s2 < R; s2++) atomicAdd(&Pk[1 + ps[s2]], t1);
         }
     }
 }
@@ -1496,6 +1802,15 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
         for (int j = 0; j < n; j++) if (j != p) pool_[np++] = j;
         fill_subsets_h(pool_, np, R, d.rs, subs.data() + (size_t)p * d.nsub * d.rs);
     }
+    d.nsub1 = R >= 1 ? (int)binom_h(n - 1, R - 1) : 0;
+    std::vector<uint8_t> subs1((size_t)n * std::max(d.nsub1, 1) * d.rs, 0);
+    if (R >= 2) {
+        for (int p = 0; p < n; p++) {
+            int pool_[32], np = 0;
+            for (int j = 0; j < n; j++) if (j != p) pool_[np++] = j;
+            fill_subsets_h(pool_, np, R - 1, d.rs, subs1.data() + (size_t)p * d.nsub1 * d.rs);
+        }
+    }
     std::vector<uint8_t> balls;
     {
         int pool_[32];
@@ -1512,7 +1827,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     }
     cov_params p2 = *prm;
     p2.M = Mw;
-    size_t need = cov_slot_bytes(&p2) + subs.size() + balls.size() + 1024;
+    size_t need = cov_slot_bytes(&p2) + subs.size() + subs1.size() + balls.size() + 1536;
     void *arena = nullptr;
     if (cudaMalloc(&arena, need) != cudaSuccess) { cudaGetLastError(); return COV_ENOMEM; }
     size_t off = 0;
@@ -1531,7 +1846,8 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.g_list = (uint32_t *)take_((size_t)Mw * 4);
     uint8_t *dsub = (uint8_t *)take_(subs.size());
     uint8_t *dball = (uint8_t *)take_(balls.size());
-    d.sub = dsub; d.ball_sub = dball;
+    uint8_t *dsub1 = (uint8_t *)take_(subs1.size());
+    d.sub = dsub; d.ball_sub = dball; d.sub1 = dsub1;
     d.st = pool->d_states + s;
     d.trace = prm->trace ? take_((size_t)prm->trace_cap * sizeof(cov_move_rec)) : nullptr;
     d.trace_cap = prm->trace ? prm->trace_cap : 0;
@@ -1542,6 +1858,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     cudaStream_t st = pool->cur_stream();
     cudaError_t e = cudaMemcpyAsync(dsub, subs.data(), subs.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dball, balls.data(), balls.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dsub1, subs1.data(), subs1.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { cudaFree(arena); return -(100 + (int)e); }
     pool->slots[s] = h;
@@ -1886,6 +2203,18 @@ int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4)
     int rc = read_state(pool, slot, &hs);
     if (rc) return rc;
     for (int k = 0; k < 4; k++) out4[k] = hs.rng[k];
+    return COV_OK;
+}
+
+// leader phase cycle counts (8) followed by the list-pair counter
+int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out9)
+{
+    if (!pool || !out9 || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    CovSlotState hs;
+    int rc = read_state(pool, slot, &hs);
+    if (rc) return rc;
+    for (int k = 0; k < 8; k++) out9[k] = hs.prof[k];
+    out9[8] = (uint64_t)hs.stat_ul_pairs;
     return COV_OK;
 }
 

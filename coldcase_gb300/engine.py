@@ -130,6 +130,18 @@ class Pool:
                 "cov_pool_get_rng")
         return out
 
+    PROF_NAMES = ("pick", "candidates", "entering", "select", "move", "finish", "compact", "other")
+
+    def prof(self, slot):
+        """Leader phase cycle counts and the list-pair counter."""
+        out = np.zeros(9, dtype=np.uint64)
+        L.check(self.lib.cov_pool_get_prof(self.h, int(slot),
+                                           out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
+                "cov_pool_get_prof")
+        d = {k: int(v) for k, v in zip(self.PROF_NAMES, out[:8])}
+        d["ul_pairs"] = int(out[8])
+        return d
+
     def trace(self, slot):
         n = ctypes.c_int64(0)
         L.check(self.lib.cov_pool_get_trace(self.h, int(slot), None, 0, ctypes.byref(n)), "cov_pool_get_trace")

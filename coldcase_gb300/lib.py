@@ -84,6 +84,7 @@ SIGNATURES = {
     "cov_pool_get_cnt": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint16)]),
     "cov_pool_get_private": (ctypes.c_int, [_P, _I32, _PI32]),
     "cov_pool_get_tabu": (ctypes.c_int, [_P, _I32, _PI32]),
+    "cov_pool_get_prof": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64)]),
     "cov_pool_get_rng": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64)]),
     "cov_pool_get_trace": (ctypes.c_int, [_P, _I32, ctypes.POINTER(CovMoveRec), _I64, _PI64]),
     "cov_pool_remove": (ctypes.c_int, [_P, _I32]),
