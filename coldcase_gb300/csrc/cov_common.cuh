@@ -124,7 +124,7 @@ struct CovSlotState {
     // cycle counts of the leader's phases, accumulated over launches:
     // 0 pick, 1 candidates + sample, 2 entering side, 3 select, 4 move op
     // (commit + sphere), 5 finish, 6 list compaction, 7 other ops
-    unsigned long long prof[8];
+    unsigned long long prof[16];   // 8..15: sub-phases (diagnostics)
 };
 
 // Generic enumeration unit of a sphere of radius r >= 1 around a word:

@@ -41,7 +41,10 @@ namespace cg = cooperative_groups;
 #define NWARP     (NT / 32)
 #define PERM_CAP  4096         // candidates kept in shared memory
 #define L_SM      256          // candidate codewords kept in shared memory
-#define RB        1024         // RNG outputs generated per batch
+#define RB        1024         // scratch draws (FY chunk)
+#define RS        2048         // RNG stream ring (draws generated ahead)
+#define RS_CKI    256          // a generator checkpoint every RS_CKI draws
+#define RS_NCK    16           // checkpoints kept (RS_NCK * RS_CKI > RS + RS_CKI)
 #define INV_N     1024         // moduli with a reciprocal in shared memory
 #define CODE_SM   4096         // codewords mirrored in the leader's shared memory
 #define NEG_CLUSTER_PAIRS 32768 // list x candidate pairs above which the whole cluster helps
@@ -78,7 +81,6 @@ struct Smem {
     int partT;
     int partH[COV_MAXN];
     // leader state
-    CovRng rng;
     long long it, unc, best_unc, since_improve, nkicks, moves_left, target, trace_n;
     long long chosen_delta;
     unsigned long long t_deadline;
@@ -88,7 +90,7 @@ struct Smem {
     uint64_t pu;
     long long uw;
     cov_move_rec rec;
-    unsigned long long prof[8];
+    unsigned long long prof[16];
     long long ul_pairs;
     // scratch
     int red_i[NWARP];
@@ -101,13 +103,18 @@ struct Smem {
     uint32_t perm[PERM_CAP];
     int32_t dval[PERM_CAP];
     uint8_t tflag[PERM_CAP];
-    uint64_t rbuf[RB];
     uint32_t L[L_SM];
     uint64_t Lpk[L_SM];
     int32_t neg[L_SM * COV_MAXN];
     uint32_t lbits[L_SM / 32];
     uint64_t Loh[L_SM][2];     // one-hot digit masks of the candidate codewords
     uint64_t inv[INV_N + 1];   // floor((2^64-1)/m), m = 1..INV_N
+    // RNG stream: draws generated ahead of use by an idle leader warp
+    uint64_t rs_buf[RS];
+    unsigned long long rs_gen, rs_use;
+    CovRng rs_state;           // generator after rs_gen draws
+    CovRng rs_ck[RS_NCK];      // generator at draw rs_ckpos[k]
+    unsigned long long rs_ckpos[RS_NCK];
     uint64_t code_sm[CODE_SM]; // leader's mirror of the packed code (M <= CODE_SM)
     uint8_t dist8[CODE_SM];    // distances to the sampled word
 };
@@ -223,6 +230,75 @@ __device__ __forceinline__ uint64_t fastmod(const Smem &S, uint64_t x, uint64_t 
     return x % m;
 }
 
+// ---- RNG stream.  The draws of the reference's single xoshiro256++ stream
+// are consumed strictly in order; only how many each step consumes depends
+// on the data.  So they are generated ahead into a ring (by the leader's
+// warp 0 while the cluster works on a move) and consumed at a cursor; the
+// generator state at the cursor is recovered from a checkpoint when the
+// launch ends.  All rs_* calls are made by one thread.
+__device__ __forceinline__ void rs_init(Smem &S, const uint64_t st[4])
+{
+    for (int k = 0; k < 4; k++) S.rs_state.s[k] = st[k];
+    S.rs_gen = S.rs_use = 0;
+    S.rs_ck[0] = S.rs_state;
+    S.rs_ckpos[0] = 0;
+    for (int k = 1; k < RS_NCK; k++) S.rs_ckpos[k] = ~0ull;
+}
+
+// generate until `limit` draws exist (never more than RS ahead of use)
+__device__ __forceinline__ void rs_fill(Smem &S, unsigned long long limit)
+{
+    const unsigned long long cap = S.rs_use + RS;
+    if (limit > cap) limit = cap;
+    unsigned long long g = S.rs_gen;
+    if (g >= limit) return;
+    CovRng st = S.rs_state;
+    for (; g < limit; g++) {
+        if ((g % RS_CKI) == 0) {
+            const int k = (int)((g / RS_CKI) % RS_NCK);
+            S.rs_ck[k] = st;
+            S.rs_ckpos[k] = g;
+        }
+        S.rs_buf[g % RS] = cov_rng_next(st);
+    }
+    S.rs_state = st;
+    S.rs_gen = g;
+}
+
+__device__ __forceinline__ void rs_ensure(Smem &S, int need)
+{
+    if (S.rs_gen < S.rs_use + (unsigned long long)need) rs_fill(S, S.rs_use + (unsigned long long)need);
+}
+
+// k-th draw after the cursor (k < what rs_ensure secured)
+__device__ __forceinline__ uint64_t rs_peek(const Smem &S, int k)
+{
+    return S.rs_buf[(S.rs_use + (unsigned long long)k) % RS];
+}
+
+__device__ __forceinline__ uint64_t rs_take(Smem &S)
+{
+    rs_ensure(S, 1);
+    uint64_t v = S.rs_buf[S.rs_use % RS];
+    S.rs_use++;
+    return v;
+}
+
+// generator state positioned at the cursor
+__device__ void rs_final(const Smem &S, uint64_t out[4])
+{
+    CovRng st;
+    if (S.rs_gen == S.rs_use) {
+        st = S.rs_state;
+    } else {
+        const unsigned long long blk = (S.rs_use / RS_CKI) * RS_CKI;
+        const int k = (int)((S.rs_use / RS_CKI) % RS_NCK);
+        st = S.rs_ck[k];
+        for (unsigned long long g = blk; g < S.rs_use; g++) cov_rng_next(st);
+    }
+    for (int k = 0; k < 4; k++) out[k] = st.s[k];
+}
+
 // one-hot digit masks: bit j*q + w_j set for every position (q*n <= 128);
 // d(a, b) = n - popc(oh_a & oh_b)
 __device__ __forceinline__ void onehot(uint64_t pk, int n, int q, uint64_t &lo, uint64_t &hi)
@@ -244,6 +320,32 @@ __device__ __forceinline__ void leader_set_code(const CovSlot &d, Smem &S, int i
 {
     cov_stcg(&d.code[i], pk);
     if (d.M <= CODE_SM) S.code_sm[i] = pk;
+}
+
+// exclusive scan of an int over the block with an associative op (applied
+// in thread order); the block total goes to `total`
+template <class Op>
+__device__ int block_scan_int(Smem &S, int v, int ident, Op op, int &total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = op(y, x);
+    }
+    int ex = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane == 0) ex = ident;
+    __syncthreads();
+    if (lane == 31) S.red_i[wid] = x;
+    __syncthreads();
+    int pre = ident, tot = ident;
+    for (int w = 0; w < NWARP; w++) {
+        if (w < wid) pre = op(pre, S.red_i[w]);
+        tot = op(tot, S.red_i[w]);
+    }
+    total = tot;
+    __syncthreads();
+    return op(pre, ex);
 }
 
 // ------------------------------------------------ private-count upkeep -----
@@ -369,10 +471,15 @@ __device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, 
     __syncthreads();
     long long dunc = 0;
     int T = 0;
-    const uint32_t wid = (uint32_t)rank * NWARP + (threadIdx.x >> 5);
-    const uint32_t wstride = (uint32_t)csize * NWARP * 32;
-    if (R == 0) {
-        if (rank == 0 && threadIdx.x == 0) {
+    // the leader's warp 0 generates RNG draws for the next iterations while
+    // every other warp of the cluster shares the move
+    const int gw = rank * NWARP + (int)(threadIdx.x >> 5) - 1;
+    const uint32_t wid = (uint32_t)max(gw, 0);
+    const uint32_t wstride = (uint32_t)(csize * NWARP - 1) * 32;
+    if (gw < 0) {
+        if (threadIdx.x == 0) rs_fill(S, S.rs_use + RS);
+    } else if (R == 0) {
+        if (rank == 0 && threadIdx.x == 32) {
             const uint32_t oa = cov_ldcg(&d.cw[P.base]);
             const uint32_t ob = cov_ldcg(&d.cw[P.base + P.dv]);
             T -= (oa & 0xffffu) == 1;
@@ -424,7 +531,7 @@ __device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, 
         }
         // X / Y pairs: (R-1)-subsets avoiding p
         if (R == 1) {
-            if (rank == 0 && threadIdx.x == 0) {
+            if (rank == 0 && threadIdx.x == 32) {
                 const int dy = (int)((cov_ldcg(&d.cw[P.base]) & 0xffffu) == 1) -
                                (int)((cov_ldcg(&d.cw[P.base + P.dv]) & 0xffffu) == 1);
                 T += dy;
@@ -669,7 +776,10 @@ __device__ void op_neg(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, i
         for (int x = threadIdx.x; x < nL * n; x += NT) S.neg[x] = 0;
         __syncthreads();
     }
-    ul_pass(d, P.pu, nL, S.Lpk, S.Loh, S.neg, (uint32_t)rank * NT + threadIdx.x, (uint32_t)csize * NT, true);
+    // the leader's warp 0 generates RNG draws; every other thread takes a slice
+    const int gt = rank * NT + (int)threadIdx.x - 32;
+    if (gt >= 0) ul_pass(d, P.pu, nL, S.Lpk, S.Loh, S.neg, (uint32_t)gt, (uint32_t)(csize * NT - 32), true);
+    else if (threadIdx.x == 0) rs_fill(S, S.rs_use + RS);
     if (rank != 0) {
         __syncthreads();
         for (int x = threadIdx.x; x < nL * n; x += NT)
@@ -685,13 +795,10 @@ __device__ void op_neg(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, i
 __device__ long long leader_pick(const CovSlot &d, Smem &S)
 {
     const int tid = threadIdx.x;
-    if (tid == 0) {
-        CovRng r = S.rng;
-        for (int t = 0; t < 65; t++) S.rbuf[t] = cov_rng_next(r);
-    }
+    if (tid == 0) rs_ensure(S, 65);
     __syncthreads();
     if (tid < 64) {
-        uint32_t w = (uint32_t)(S.rbuf[tid] % (uint64_t)d.N);
+        uint32_t w = (uint32_t)(rs_peek(S, tid) % (uint64_t)d.N);
         unsigned m = __ballot_sync(0xffffffffu, cnt_of(d, w) == 0);
         if ((tid & 31) == 0) S.hitmask[tid >> 5] = m;
     }
@@ -702,14 +809,10 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
     const int consumed = first >= 0 ? first + 1 : 65;
     long long result = -1;
     uint32_t start = 0;
-    if (first >= 0) result = (long long)(S.rbuf[first] % (uint64_t)d.N);
-    else start = (uint32_t)(S.rbuf[64] % (uint64_t)d.N);
+    if (first >= 0) result = (long long)(rs_peek(S, first) % (uint64_t)d.N);
+    else start = (uint32_t)(rs_peek(S, 64) % (uint64_t)d.N);
     __syncthreads();
-    if (tid == 0) {
-        CovRng r = S.rng;
-        for (int t = 0; t < consumed; t++) cov_rng_next(r);
-        S.rng = r;
-    }
+    if (tid == 0) S.rs_use += consumed;
     if (first >= 0 || S.unc <= 0) return result;     // no zero anywhere: -1
     if (S.ul_valid) {
         // every zero-count word is on the list: the first one after start is
@@ -845,6 +948,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         dm = min(dm, (unsigned)dd);
     }
     dm = block_min_u32(S, dm);
+    if (tid == 0) { long long t1 = clock64(); S.prof[10] += t1 - t0; }
     const int dtar = ((int)dm <= R + 1) ? R + 1 : (int)dm;
     // ordered list of codewords at distance dtar (covsearch2e.c:1359-1376):
     // always in global memory, the first L_SM also in shared memory with
@@ -878,6 +982,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
         return;
     }
+    if (tid == 0) { long long t1 = clock64(); S.prof[11] += t1 - t0; }
     const int take = min(ncand, d.cand);
     const int psm = ncand <= PERM_CAP;
     uint32_t *perm = psm ? S.perm : d.g_perm;
@@ -888,19 +993,19 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     for (int s0 = 0; s0 < take; s0 += RB) {
         const int cnt = min(RB, take - s0);
         __syncthreads();
-        if (tid == 0) {
-            CovRng r = S.rng;
-            for (int t = 0; t < cnt; t++) S.rbuf[t] = cov_rng_next(r);
-            S.rng = r;
-        }
+        if (tid == 0) rs_ensure(S, cnt);
         __syncthreads();
         for (int t = tid; t < cnt; t += NT) {
             int s = s0 + t;
-            dval[s] = s + (int32_t)fastmod(S, S.rbuf[t], (uint64_t)(ncand - s));
+            dval[s] = s + (int32_t)fastmod(S, rs_peek(S, t), (uint64_t)(ncand - s));
         }
+        __syncthreads();
+        if (tid == 0) S.rs_use += cnt;
     }
     __syncthreads();
     if (tid == 0) {
+        long long t1 = clock64();
+        S.prof[12] += t1 - t0;
         for (int s = 0; s < take; s++) {
             int j = dval[s];
             uint32_t tmp = perm[s]; perm[s] = perm[j]; perm[j] = tmp;
@@ -1020,34 +1125,109 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
         }
     }
     __syncthreads();
-    if (tid == 0) {
-        long long bestd = 1LL << 60;
-        int nties = 0, bs = -1;
-        CovRng r = S.rng;
-        for (int s = 0; s < take; s++) {
-            long long dd;
-            int tb;
-            if (psm) { dd = dval[s]; tb = S.tflag[s]; }
-            else {
-                uint32_t c = perm[s];
-                int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
-                int k = (int)Lp[l];
-                uint64_t pk = cov_ldcg(&d.code[k]);
-                int p = nth_set_pos(cov_spread(pk ^ pu), rr);
-                int v = cov_nib(pu, p);
-                const int32_t *Pk = d.P + (size_t)k * (n + 1);
-                dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
-                tb = (long long)cov_ldcg(&d.tabu[((size_t)k * n + p) * q + v]) > S.it;
-            }
-            if (tb && S.unc + dd >= S.best_unc) continue;
-            if (dd < bestd) { bestd = dd; bs = s; nties = 1; }
-            else if (dd == bestd) {
-                nties++;
-                if (fastmod(S, cov_rng_next(r), (uint64_t)nties) == 0) bs = s;
-            }
+    // Selection (covsearch2e.c:1503-1518) in parallel.  Scanning s in order
+    // with eligible keys d_s, a "reset" is an eligible s with d_s below the
+    // running minimum and an "event" one equal to it; each event draws once
+    // and, with nties = its rank in the current minimum's run (the reset
+    // counting 1), replaces the choice when draw % nties == 0.  Only events
+    // at the final minimum V can win: the last of them whose draw hits, else
+    // the first position holding V.  With nothing eligible one draw picks a
+    // random candidate.
+    int bs_par = -2, consumed = 0;
+    if (psm) {
+        const long long unc = S.unc, best = S.best_unc;
+        const int CH = (take + NT - 1) / NT;
+        const int s_lo = min(take, tid * CH), s_hi = min(take, s_lo + CH);
+        const int INF = 0x7fffffff;
+        auto keyof = [&](int s2) -> int {
+            const int dd = dval[s2];
+            return (S.tflag[s2] && unc + dd >= best) ? INF : dd;
+        };
+        int cmin = INF;
+        for (int s2 = s_lo; s2 < s_hi; s2++) cmin = min(cmin, keyof(s2));
+        int V;
+        const int pmin = block_scan_int(S, cmin, INF, [](int a2, int b2) { return min(a2, b2); }, V);
+        // events per chunk and the event count at the chunk's last reset
+        int m = pmin, nev = 0, ev_reset = -1;
+        for (int s2 = s_lo; s2 < s_hi; s2++) {
+            const int k2 = keyof(s2);
+            if (k2 == INF) continue;
+            if (k2 < m) { m = k2; ev_reset = nev; }
+            else if (k2 == m) nev++;
         }
-        if (bs < 0) bs = (int)fastmod(S, cov_rng_next(r), (uint64_t)take);
-        S.rng = r;
+        int E;
+        const int evbase = block_scan_int(S, nev, 0, [](int a2, int b2) { return a2 + b2; }, E);
+        int dummy;
+        const int in_reset = block_scan_int(S, ev_reset >= 0 ? evbase + ev_reset : -1, -1,
+                                            [](int a2, int b2) { return b2 != -1 ? b2 : a2; }, dummy);
+        if (V != INF && E <= RS / 2) {
+            if (tid == 0) rs_ensure(S, E);
+            __syncthreads();
+            // first occurrence of V and the last winning event at V
+            int firstV = INF, win = -1;
+            m = pmin;
+            int cur_reset = in_reset, g = evbase;
+            for (int s2 = s_lo; s2 < s_hi; s2++) {
+                const int k2 = keyof(s2);
+                if (k2 == INF) continue;
+                if (k2 < m) {
+                    m = k2;
+                    cur_reset = g;
+                    if (k2 == V) firstV = min(firstV, s2);
+                } else if (k2 == m) {
+                    const int nties = 1 + (g + 1) - cur_reset;
+                    if (k2 == V && fastmod(S, rs_peek(S, g), (uint64_t)nties) == 0) win = s2;
+                    g++;
+                }
+            }
+            int fv, wv;
+            block_scan_int(S, firstV, INF, [](int a2, int b2) { return min(a2, b2); }, fv);
+            block_scan_int(S, win, -1, [](int a2, int b2) { return max(a2, b2); }, wv);
+            bs_par = wv >= 0 ? wv : fv;
+            consumed = E;
+        } else if (V == INF) {
+            if (tid == 0) { rs_ensure(S, 1); }
+            __syncthreads();
+            bs_par = (int)fastmod(S, rs_peek(S, 0), (uint64_t)take);
+            consumed = 1;
+        }
+    }
+    if (tid == 0) {
+        long long ts1 = clock64();
+        S.prof[8] += ts1 - t0;
+        int bs = -1;
+        if (bs_par >= 0) {
+            bs = bs_par;
+            S.rs_use += consumed;
+        } else {
+            long long bestd = 1LL << 60;
+            int nties = 0;
+            for (int s = 0; s < take; s++) {
+                long long dd;
+                int tb;
+                if (psm) { dd = dval[s]; tb = S.tflag[s]; }
+                else {
+                    uint32_t c = perm[s];
+                    int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
+                    int k = (int)Lp[l];
+                    uint64_t pk = cov_ldcg(&d.code[k]);
+                    int p = nth_set_pos(cov_spread(pk ^ pu), rr);
+                    int v = cov_nib(pu, p);
+                    const int32_t *Pk = d.P + (size_t)k * (n + 1);
+                    dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
+                    tb = (long long)cov_ldcg(&d.tabu[((size_t)k * n + p) * q + v]) > S.it;
+                }
+                if (tb && S.unc + dd >= S.best_unc) continue;
+                if (dd < bestd) { bestd = dd; bs = s; nties = 1; }
+                else if (dd == bestd) {
+                    nties++;
+                    if (fastmod(S, rs_take(S), (uint64_t)nties) == 0) bs = s;
+                }
+            }
+            if (bs < 0) bs = (int)fastmod(S, rs_take(S), (uint64_t)take);
+        }
+        long long ts2 = clock64();
+        S.prof[9] += ts2 - ts1;
         uint32_t c = perm[bs];
         int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
         int k = (int)Lp[l];
@@ -1102,7 +1282,7 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
         cov_stcg(&Pk[0], cov_ldcg(&Pk[0]) + S.accT);
         for (int j = 0; j < n; j++) cov_stcg(&Pk[1 + j], cov_ldcg(&Pk[1 + j]) + S.accH[j]);
         const int oldv = S.ibc[3];
-        uint64_t r4 = cov_rng_next(S.rng) % 4ull;
+        uint64_t r4 = rs_take(S) % 4ull;
         cov_stcg(&d.tabu[((size_t)o.mi * n + o.mp) * q + oldv], (int32_t)(S.it + d.tenure + (long long)r4));
         S.rec.unc = S.unc;
         S.improved = S.unc < S.best_unc;
@@ -1159,7 +1339,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                     S.phase = PH_KICK_DONE;
                 } else {
                     if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
-                    int i = (int)fastmod(S, cov_rng_next(S.rng), (uint64_t)d.M);
+                    int i = (int)fastmod(S, rs_take(S), (uint64_t)d.M);
                     uint64_t pk = leader_code(d, S, i);
                     OpParams &o = S.opp;
                     o.op = OP_BALL; o.sgn = -1; o.mi = i; o.pc = pk; o.base = widx_pk(d, pk);
@@ -1185,14 +1365,14 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                     for (int t2 = 0; t2 < d.R; t2++) {
                         // the value's draw precedes the position's draw, as
                         // the reference binary evaluates covsearch2e.c:1567
-                        int val = (int)(cov_rng_next(S.rng) % (uint64_t)d.q);
-                        int pos = (int)(cov_rng_next(S.rng) % (uint64_t)d.n);
+                        int val = (int)(rs_take(S) % (uint64_t)d.q);
+                        int pos = (int)(rs_take(S) % (uint64_t)d.n);
                         pk = cov_setnib(pk, pos, val);
                     }
                 } else {
                     pk = 0;
                     for (int j = 0; j < d.n; j++)
-                        pk = cov_setnib(pk, j, (int)(cov_rng_next(S.rng) % (uint64_t)d.q));
+                        pk = cov_setnib(pk, j, (int)(rs_take(S) % (uint64_t)d.q));
                 }
                 OpParams &o = S.opp;
                 leader_set_code(d, S, o.mi, pk);
@@ -1248,7 +1428,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
             }
             long long w = leader_pick(d, S);
             if (tid == 0) {
-                if (w < 0) w = (long long)(cov_rng_next(S.rng) % (uint64_t)d.N);
+                if (w < 0) w = (long long)(rs_take(S) % (uint64_t)d.N);
                 uint64_t pk = pk_of_idx(d, (uint32_t)w);
                 int i = S.greedy_i;
                 leader_set_code(d, S, i, pk);
@@ -1301,7 +1481,7 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         for (int i = threadIdx.x; i < d.M; i += NT) S.code_sm[i] = cov_ldcg(&d.code[i]);
     if (leader && threadIdx.x == 0) {
         CovSlotState *st = d.st;
-        for (int k = 0; k < 4; k++) S.rng.s[k] = st->rng[k];
+        rs_init(S, st->rng);
         S.it = st->it; S.unc = st->unc; S.best_unc = st->best_unc;
         S.since_improve = st->since_improve; S.nkicks = st->nkicks;
         S.moves_left = st->moves_left; S.target = st->target; S.trace_n = st->trace_n;
@@ -1312,7 +1492,7 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         S.t_deadline = gtimer() + budget_ns;
         S.guard = 0;
         S.opp.op = -1;
-        for (int k = 0; k < 8; k++) S.prof[k] = st->prof[k];
+        for (int k = 0; k < 16; k++) S.prof[k] = st->prof[k];
         S.ul_pairs = st->stat_ul_pairs;
     }
     cl.sync();
@@ -1366,12 +1546,12 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
     cl.sync();
     if (leader && threadIdx.x == 0) {
         CovSlotState *st = d.st;
-        for (int k = 0; k < 4; k++) st->rng[k] = S.rng.s[k];
+        rs_final(S, st->rng);
         st->it = S.it; st->unc = S.unc; st->best_unc = S.best_unc;
         st->since_improve = S.since_improve; st->nkicks = S.nkicks;
         st->moves_left = S.moves_left; st->trace_n = S.trace_n;
         st->ul_valid = S.ul_valid;
-        for (int k = 0; k < 8; k++) st->prof[k] = S.prof[k];
+        for (int k = 0; k < 16; k++) st->prof[k] = S.prof[k];
         st->stat_ul_pairs = S.ul_pairs;
         int s0 = atomicAdd(&st->status, 0);
         st->status = S.status ? S.status : s0;
@@ -2206,15 +2386,15 @@ int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4)
     return COV_OK;
 }
 
-// leader phase cycle counts (8) followed by the list-pair counter
-int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out9)
+// leader phase cycle counts (16) followed by the list-pair counter
+int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out17)
 {
-    if (!pool || !out9 || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    if (!pool || !out17 || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
     CovSlotState hs;
     int rc = read_state(pool, slot, &hs);
     if (rc) return rc;
-    for (int k = 0; k < 8; k++) out9[k] = hs.prof[k];
-    out9[8] = (uint64_t)hs.stat_ul_pairs;
+    for (int k = 0; k < 16; k++) out17[k] = hs.prof[k];
+    out17[16] = (uint64_t)hs.stat_ul_pairs;
     return COV_OK;
 }
 

@@ -134,12 +134,14 @@ class Pool:
 
     def prof(self, slot):
         """Leader phase cycle counts and the list-pair counter."""
-        out = np.zeros(9, dtype=np.uint64)
+        out = np.zeros(17, dtype=np.uint64)
         L.check(self.lib.cov_pool_get_prof(self.h, int(slot),
                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
                 "cov_pool_get_prof")
         d = {k: int(v) for k, v in zip(self.PROF_NAMES, out[:8])}
-        d["ul_pairs"] = int(out[8])
+        for k in range(8, 16):
+            d["sub%d" % k] = int(out[k])
+        d["ul_pairs"] = int(out[16])
         return d
 
     def trace(self, slot):

@@ -132,8 +132,9 @@ int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4);
  * counterpart of the reference's -DPROF timers, covsearch2e.c:109-131):
  * [0] pick [1] candidates+sample [2] entering side [3] select
  * [4] commit+sphere [5] finish [6] list compaction [7] other ops,
- * then [8] uncovered-list x candidate-codeword pairs tested. */
-int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out9);
+ * [8..15] finer sub-phases, then [16] uncovered-list x candidate-codeword
+ * pairs tested. */
+int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out17);
 int cov_pool_get_trace(cov_pool *pool, int32_t slot, cov_move_rec *out,
                        int64_t cap, int64_t *n_out);
 int cov_pool_remove(cov_pool *pool, int32_t slot);
