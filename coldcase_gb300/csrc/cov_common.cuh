@@ -79,6 +79,7 @@ struct CovSlot {
     uint32_t ppow[COV_MAXN + 1]; // (q-1)^k
     int tenure, kick, cand;
     long long stall;
+    long long neg_cluster_pairs; // list x candidate pairs above which the cluster shares the list pass
     // device arrays
     uint32_t *cw;                // [N]  cnt (bits 0-15) | xor of covering ids (16-31)
     uint64_t *code;              // [M]  packed codewords
@@ -124,7 +125,7 @@ struct CovSlotState {
     // cycle counts of the leader's phases, accumulated over launches:
     // 0 pick, 1 candidates + sample, 2 entering side, 3 select, 4 move op
     // (commit + sphere), 5 finish, 6 list compaction, 7 other ops
-    unsigned long long prof[16];   // 8..15: sub-phases (diagnostics)
+    unsigned long long prof[24];   // 8..23: sub-phases (diagnostics)
 };
 
 // Generic enumeration unit of a sphere of radius r >= 1 around a word:

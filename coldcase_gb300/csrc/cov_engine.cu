@@ -39,15 +39,16 @@ namespace cg = cooperative_groups;
 
 #define NT        512          // threads per CTA
 #define NWARP     (NT / 32)
-#define PERM_CAP  4096         // candidates kept in shared memory
-#define L_SM      256          // candidate codewords kept in shared memory
+#define PERM_CAP  2048         // candidates kept in shared memory
+#define L_SM      128          // candidate codewords kept in shared memory
 #define RB        1024         // scratch draws (FY chunk)
-#define RS        2048         // RNG stream ring (draws generated ahead)
-#define RS_CKI    256          // a generator checkpoint every RS_CKI draws
+#define ULS       1024         // uncovered-list entries staged per chunk
+#define RS        1024         // RNG stream ring (draws generated ahead)
+#define RS_CKI    128          // a generator checkpoint every RS_CKI draws
 #define RS_NCK    16           // checkpoints kept (RS_NCK * RS_CKI > RS + RS_CKI)
 #define INV_N     1024         // moduli with a reciprocal in shared memory
-#define CODE_SM   4096         // codewords mirrored in the leader's shared memory
-#define NEG_CLUSTER_PAIRS 32768 // list x candidate pairs above which the whole cluster helps
+#define CODE_SM   2048         // codewords mirrored in every CTA's shared memory
+#define NEG_CLUSTER_PAIRS 4096  // list x candidate pairs above which the whole cluster helps
 #define UL_CAP_DEFAULT (1 << 20)
 
 enum { OP_STOP = 0, OP_MOVE, OP_NEGWALK, OP_BALL, OP_RECOMPUTE, OP_ZERO_TABU, OP_REBUILD_UL, OP_NEG };
@@ -67,6 +68,7 @@ struct OpParams {
     uint64_t pc, pcn, pu;      // packed codeword before / after, target word
     int nL, dtar;
     int L_sm, neg_sm;          // list / neg arrays live in the leader's smem
+    int uln;                   // uncovered-list length for OP_NEG
 };
 
 struct Smem {
@@ -86,12 +88,14 @@ struct Smem {
     unsigned long long t_deadline;
     long long guard;
     int ul_valid, status, phase, kick_t, finished, greedy_i, mode;
-    int nL, dtar, ncand, take, improved, dokick;
+    int nL, dtar, ncand, take, improved, dokick, swaps_pending;
     uint64_t pu;
     long long uw;
     cov_move_rec rec;
-    unsigned long long prof[16];
+    unsigned long long prof[24];
     long long ul_pairs;
+    unsigned long long diag_twmax, diag_hits, diag_atom;
+    int uln;                   // list length read once per iteration
     // scratch
     int red_i[NWARP];
     unsigned red_u[NWARP];
@@ -103,11 +107,17 @@ struct Smem {
     uint32_t perm[PERM_CAP];
     int32_t dval[PERM_CAP];
     uint8_t tflag[PERM_CAP];
+    int32_t fy_a[PERM_CAP];    // parallel Fisher-Yates scratch
+    int32_t fy_b[PERM_CAP];
+    int32_t fy_c[PERM_CAP];
     uint32_t L[L_SM];
     uint64_t Lpk[L_SM];
     int32_t neg[L_SM * COV_MAXN];
     uint32_t lbits[L_SM / 32];
-    uint64_t Loh[L_SM][2];     // one-hot digit masks of the candidate codewords
+    uint64_t cmask[COV_MAXN * COV_MAXQ]; // [j*q+v]: candidates (< 64) with digit v at position j
+    uint16_t Pmask[L_SM];      // positions where candidate l differs from the sampled word
+    uint64_t st_H[ULS];        // staged list chunk: candidates at distance R+1 from the entry
+    uint16_t st_E[ULS];        //                    positions where the entry equals the sampled word
     uint64_t inv[INV_N + 1];   // floor((2^64-1)/m), m = 1..INV_N
     // RNG stream: draws generated ahead of use by an idle leader warp
     uint64_t rs_buf[RS];
@@ -159,12 +169,39 @@ __device__ __forceinline__ void set_error(const CovSlot &d, int code)
     atomicCAS(&d.st->status, 0, code);
 }
 
-__device__ __forceinline__ unsigned long long gtimer()
+// Block / cluster barriers that first reconverge the warp.  A lane held back
+// on a divergent single-thread path (if (tid == 0) {...}) is otherwise
+// scheduled long after its warp-mates have parked at the barrier; a warp
+// barrier in front makes the scheduler run it at once.
+__device__ __forceinline__ void cov_bar()
 {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    __syncwarp();
+    __syncthreads();
+}
+__device__ __forceinline__ int cov_bar_or(int v)
+{
+    __syncwarp();
+    return __syncthreads_or(v);
+}
+__device__ __forceinline__ void cov_cbar(cg::cluster_group &cl)
+{
+    __syncwarp();
+    cl.sync();
+}
+
+// cycle counter read that stays in program order with the memory operations
+// around it (plain cov_clock() may be scheduled away from its position)
+__device__ __forceinline__ long long cov_clock()
+{
+    long long t;
+    asm volatile("mov.u64 %0, %%clock64;" : "=l"(t) :: "memory");
     return t;
 }
+
+// The launch deadline is kept in SM cycles (read through cov_clock): a
+// %globaltimer read can stall the reading warp for tens of microseconds,
+// which is too slow for a check made every iteration.
+#define COV_CYCLES_PER_NS 2ull
 
 template <class T>
 __device__ __forceinline__ T warp_sum(T v)
@@ -177,24 +214,24 @@ __device__ __forceinline__ T warp_sum(T v)
 __device__ int block_sum_int(Smem &S, int v)
 {
     v = warp_sum(v);
-    __syncthreads();
+    cov_bar();
     if ((threadIdx.x & 31) == 0) S.red_i[threadIdx.x >> 5] = v;
-    __syncthreads();
+    cov_bar();
     int t = 0;
     for (int w = 0; w < NWARP; w++) t += S.red_i[w];
-    __syncthreads();
+    cov_bar();
     return t;
 }
 
 __device__ unsigned block_min_u32(Smem &S, unsigned v)
 {
     for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
-    __syncthreads();
+    cov_bar();
     if ((threadIdx.x & 31) == 0) S.red_u[threadIdx.x >> 5] = v;
-    __syncthreads();
+    cov_bar();
     unsigned t = 0xffffffffu;
     for (int w = 0; w < NWARP; w++) t = min(t, S.red_u[w]);
-    __syncthreads();
+    cov_bar();
     return t;
 }
 
@@ -204,16 +241,16 @@ __device__ int block_excl_scan(Smem &S, int flag, int &pos)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned m = __ballot_sync(0xffffffffu, flag);
     int inwarp = __popc(m & ((1u << lane) - 1));
-    __syncthreads();
+    cov_bar();
     if (lane == 0) S.red_i[wid] = __popc(m);
-    __syncthreads();
+    cov_bar();
     int before = 0, tot = 0;
     for (int w = 0; w < NWARP; w++) {
         if (w < wid) before += S.red_i[w];
         tot += S.red_i[w];
     }
     pos = before + inwarp;
-    __syncthreads();
+    cov_bar();
     return tot;
 }
 
@@ -299,18 +336,6 @@ __device__ void rs_final(const Smem &S, uint64_t out[4])
     for (int k = 0; k < 4; k++) out[k] = st.s[k];
 }
 
-// one-hot digit masks: bit j*q + w_j set for every position (q*n <= 128);
-// d(a, b) = n - popc(oh_a & oh_b)
-__device__ __forceinline__ void onehot(uint64_t pk, int n, int q, uint64_t &lo, uint64_t &hi)
-{
-    lo = 0; hi = 0;
-    for (int j = 0; j < n; j++) {
-        int b = j * q + cov_nib(pk, j);
-        if (b < 64) lo |= 1ull << b;
-        else hi |= 1ull << (b - 64);
-    }
-}
-
 __device__ __forceinline__ uint64_t leader_code(const CovSlot &d, const Smem &S, int i)
 {
     return d.M <= CODE_SM ? S.code_sm[i] : cov_ldcg(&d.code[i]);
@@ -335,17 +360,44 @@ __device__ int block_scan_int(Smem &S, int v, int ident, Op op, int &total)
     }
     int ex = __shfl_up_sync(0xffffffffu, x, 1);
     if (lane == 0) ex = ident;
-    __syncthreads();
+    cov_bar();
     if (lane == 31) S.red_i[wid] = x;
-    __syncthreads();
+    cov_bar();
     int pre = ident, tot = ident;
     for (int w = 0; w < NWARP; w++) {
         if (w < wid) pre = op(pre, S.red_i[w]);
         tot = op(tot, S.red_i[w]);
     }
     total = tot;
-    __syncthreads();
+    cov_bar();
     return op(pre, ex);
+}
+
+// Fisher-Yates swaps of the sampled candidates (covsearch2e.c:1384-1389),
+// their draws already reduced into dval[s] = j_s; one thread, in order (the
+// oversized case; the shared-memory case is resolved by fy_parallel).
+// Also counts the distinct codewords among the sample for the trace.
+__device__ void apply_swaps(const CovSlot &d, Smem &S)
+{
+    if (!S.swaps_pending) return;
+    const int take = S.take, ncand = S.ncand, dtar = S.dtar;
+    const int psm = ncand <= PERM_CAP;
+    uint32_t *perm = psm ? S.perm : d.g_perm;
+    int32_t *dval = psm ? S.dval : d.g_dval;
+    for (int s = 0; s < take; s++) {
+        int j = dval[s];
+        uint32_t tmp = perm[s]; perm[s] = perm[j]; perm[j] = tmp;
+    }
+    if (take < ncand) {
+        int c = 0;
+        for (int s = 0; s < take; s++) {
+            int l = (int)(perm[s] / (uint32_t)dtar), dup = 0;
+            for (int t = 0; t < s; t++) if ((int)(perm[t] / (uint32_t)dtar) == l) { dup = 1; break; }
+            c += !dup;
+        }
+        S.rec.ncw = c;
+    }
+    S.swaps_pending = 0;
 }
 
 // ------------------------------------------------ private-count upkeep -----
@@ -432,10 +484,11 @@ __device__ __forceinline__ void cta_add_dunc(long long dunc, Smem *LS)
 {
     __shared__ long long cta_dunc;
     if (threadIdx.x == 0) cta_dunc = 0;
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
     dunc = warp_sum(dunc);
     if ((threadIdx.x & 31) == 0 && dunc != 0) atomicAdd((unsigned long long *)&cta_dunc, (unsigned long long)dunc);
-    __syncthreads();
+    cov_bar();
     if (threadIdx.x == 0 && cta_dunc != 0) atomicAdd(&LS->dunc, (unsigned long long)cta_dunc);
 }
 
@@ -467,8 +520,9 @@ __device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, 
 {
     const int R = d.R, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) S.partT = 0;
+    __syncwarp();
     if (threadIdx.x < COV_MAXN) S.partH[threadIdx.x] = 0;
-    __syncthreads();
+    cov_bar();
     long long dunc = 0;
     int T = 0;
     // the leader's warp 0 generates RNG draws for the next iterations while
@@ -478,6 +532,7 @@ __device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, 
     const uint32_t wstride = (uint32_t)(csize * NWARP - 1) * 32;
     if (gw < 0) {
         if (threadIdx.x == 0) rs_fill(S, S.rs_use + RS);
+        __syncwarp();
     } else if (R == 0) {
         if (rank == 0 && threadIdx.x == 32) {
             const uint32_t oa = cov_ldcg(&d.cw[P.base]);
@@ -573,7 +628,7 @@ __device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, 
     cta_add_dunc(dunc, LS);
     T = warp_sum(T);
     if (lane == 0 && T) atomicAdd(&S.partT, T);
-    __syncthreads();
+    cov_bar();
     if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
     if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
 }
@@ -589,8 +644,9 @@ __device__ void op_recompute(const CovSlot &d, uint32_t base, uint64_t pc, Smem 
     const int R = d.R;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x == 0) S.partT = 0;
+    __syncwarp();
     if (threadIdx.x < COV_MAXN) S.partH[threadIdx.x] = 0;
-    __syncthreads();
+    cov_bar();
     int T = 0;
     if (R == 0) {
         if (rank == 0 && threadIdx.x == 0) T = (cnt_of(d, base) == 1);
@@ -622,7 +678,7 @@ __device__ void op_recompute(const CovSlot &d, uint32_t base, uint64_t pc, Smem 
         }
     }
     if (lane == 0 && T) atomicAdd(&S.partT, T);
-    __syncthreads();
+    cov_bar();
     if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
     if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
 }
@@ -711,7 +767,7 @@ __device__ void op_rebuild_ul(const CovSlot &d, int rank, int csize, cg::cluster
     const uint32_t nb = (d.N + 31) / 32;
     for (uint32_t x = (uint32_t)rank * NT + threadIdx.x; x < nb; x += (uint32_t)csize * NT)
         cov_stcg(&d.ul_bit[x], 0u);
-    cl.sync();
+    cov_cbar(cl);
     for (uint32_t x = (uint32_t)rank * NT + threadIdx.x; x < d.N; x += (uint32_t)csize * NT) {
         if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) ul_insert(d, 1, x, pk_of_idx(d, x));
     }
@@ -721,29 +777,54 @@ __device__ void op_rebuild_ul(const CovSlot &d, int rank, int csize, cg::cluster
 // restricted to v = u_p, the only entries a non-wide candidate reads: for
 // every listed x that is still uncovered and every candidate codeword c with
 // d(x,c) = R+1, neg[c][j] += 1 for each j in D(x,c) with x_j = u_j.
-// Entries first, first+stride, ... of the list.
+// Entries first, first+stride, ... of the list.  With at most 64 candidates
+// the distance test is bit-sliced: cmask[j*q+v] holds the candidates whose
+// digit j is v, and a 5-bit counter kept across 64 lanes of bits adds up the
+// matching positions of all candidates at once; the candidates at distance
+// R+1 are those with exactly n-(R+1) matches.
 __device__ void ul_pass(const CovSlot &d, uint64_t pu, int nL, const uint64_t *Lpk,
-                        const uint64_t (*Loh)[2], int32_t *negp, uint32_t first, uint32_t stride,
-                        bool use_oh)
+                        const uint64_t *cmask, int32_t *negp, uint32_t first, uint32_t stride,
+                        uint32_t n0)
 {
     const int n = d.n, q = d.q, R = d.R;
-    const uint32_t n0 = (uint32_t)min(cov_ldcg(&d.st->ul_n), d.ul_cap);
     const uint64_t nm = nibmask(n);
-    const int match = n - (R + 1);          // positions shared at distance R+1
+    const int tgt = n - (R + 1);             // positions shared at distance R+1
+    const uint64_t lmask = nL >= 64 ? ~0ull : ((1ull << nL) - 1);
+    extern __shared__ __align__(16) unsigned char cov_smem[];
+    Smem &SS = *reinterpret_cast<Smem *>(cov_smem);
+    const bool probe = (first == 0);
+
+    const long long tw0 = cov_clock();
+    int nhit = 0, natom = 0;
     for (uint32_t e = first; e < n0; e += stride) {
+        long long ta = probe ? cov_clock() : 0;
         const uint32_t x = cov_ldcg(&d.ul_idx[e]);
         const uint64_t px = cov_ldcg(&d.ul_pk[e]);
-        if ((cov_ldcg(&d.cw[x]) & 0xffffu) != 0) continue;     // stale entry
+        const uint32_t cxv = cov_ldcg(&d.cw[x]);
+
+        if ((cxv & 0xffffu) != 0) continue;     // stale entry
         const uint64_t eq = ~cov_spread(px ^ pu) & nm;
-        if (use_oh) {
-            uint64_t lo, hi;
-            onehot(px, n, q, lo, hi);
-            for (int l = 0; l < nL; l++) {
-                if (__popcll(lo & Loh[l][0]) + __popcll(hi & Loh[l][1]) != match) continue;
+        uint64_t hit;
+        if (nL <= 64) {
+            uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0;
+            for (int j = 0; j < n; j++) {
+                const uint64_t m = cmask[j * q + cov_nib(px, j)];
+                uint64_t c0 = b0 & m; b0 ^= m;
+                uint64_t c1 = b1 & c0; b1 ^= c0;
+                uint64_t c2 = b2 & c1; b2 ^= c1;
+                uint64_t c3 = b3 & c2; b3 ^= c2;
+                b4 ^= c3;
+            }
+            hit = ((tgt & 1) ? b0 : ~b0) & ((tgt & 2) ? b1 : ~b1) & ((tgt & 4) ? b2 : ~b2) &
+                  ((tgt & 8) ? b3 : ~b3) & ((tgt & 16) ? b4 : ~b4) & lmask;
+            while (hit) {
+                const int l = __ffsll((long long)hit) - 1;
+                hit &= hit - 1;
+                nhit++;
                 uint64_t m = cov_spread(px ^ Lpk[l]) & eq;
                 while (m) {
-                    int j = (__ffsll((long long)m) - 1) >> 2;
-                    atomicAdd(&negp[l * n + j], 1);
+                    atomicAdd(&negp[l * n + ((__ffsll((long long)m) - 1) >> 2)], 1);
+                    natom++;
                     m &= m - 1;
                 }
             }
@@ -753,12 +834,106 @@ __device__ void ul_pass(const CovSlot &d, uint64_t pu, int nL, const uint64_t *L
                 if (__popcll(D) != R + 1) continue;
                 uint64_t m = D & eq;
                 while (m) {
-                    int j = (__ffsll((long long)m) - 1) >> 2;
-                    atomicAdd(&negp[l * n + j], 1);
+                    atomicAdd(&negp[l * n + ((__ffsll((long long)m) - 1) >> 2)], 1);
                     m &= m - 1;
                 }
             }
         }
+
+    }
+    // diagnostics: slowest warp's pass time, hits and counter atomics
+    const long long tw = cov_clock() - tw0;
+    long long twmax = tw;
+    for (int o = 16; o > 0; o >>= 1) twmax = max(twmax, __shfl_xor_sync(__activemask(), twmax, o));
+    nhit = warp_sum(nhit);
+    natom = warp_sum(natom);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&SS.diag_twmax, (unsigned long long)twmax);
+        atomicAdd(&SS.diag_hits, (unsigned long long)nhit);
+        atomicAdd(&SS.diag_atom, (unsigned long long)natom);
+    }
+}
+
+// The entering side for at most 64 candidates, without atomics.  The list
+// entries [e0, e1) are taken in chunks: every thread stages, for its
+// entries, the bit-sliced mask of candidates at distance R+1 (H) and the
+// positions where the entry equals the sampled word u (E).  Then each warp
+// owns whole candidates: for candidate l, neg[l][j] counts the staged
+// entries with l in H and j in E, for j among the positions where c_l
+// differs from u (exactly the j in D(x,c_l) with x_j = u_j).  Lane-private
+// byte counters are reduced over the warp; each counter has one writer.
+__device__ void neg_chunks(const CovSlot &d, Smem &S, uint64_t pu, int nL, uint32_t e0, uint32_t e1,
+                           int32_t *negp)
+{
+    const int n = d.n, q = d.q, R = d.R;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t nm = nibmask(n);
+    const int tgt = n - (R + 1);
+    const uint64_t lmask = nL >= 64 ? ~0ull : ((1ull << nL) - 1);
+    for (uint32_t c0 = e0; c0 < e1; c0 += ULS) {
+        const int cnt = (int)min((uint32_t)ULS, e1 - c0);
+        for (int k = threadIdx.x; k < cnt; k += NT) {
+            const uint32_t e = c0 + (uint32_t)k;
+            const uint32_t x = cov_ldcg(&d.ul_idx[e]);
+            const uint64_t px = cov_ldcg(&d.ul_pk[e]);
+            uint64_t hit = 0;
+            if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) {          // not a stale entry
+                uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0;
+                for (int j = 0; j < n; j++) {
+                    const uint64_t m = S.cmask[j * q + cov_nib(px, j)];
+                    uint64_t c1 = b0 & m; b0 ^= m;
+                    uint64_t c2 = b1 & c1; b1 ^= c1;
+                    uint64_t c3 = b2 & c2; b2 ^= c2;
+                    uint64_t c4 = b3 & c3; b3 ^= c3;
+                    b4 ^= c4;
+                }
+                hit = ((tgt & 1) ? b0 : ~b0) & ((tgt & 2) ? b1 : ~b1) & ((tgt & 4) ? b2 : ~b2) &
+                      ((tgt & 8) ? b3 : ~b3) & ((tgt & 16) ? b4 : ~b4) & lmask;
+            }
+            const uint64_t eq = ~cov_spread(px ^ pu) & nm;
+            uint32_t E = 0;
+            for (uint64_t m = eq; m; m &= m - 1) E |= 1u << ((__ffsll((long long)m) - 1) >> 2);
+            S.st_H[k] = hit;
+            S.st_E[k] = (uint16_t)E;
+        }
+        cov_bar();
+        for (int l = warp; l < nL; l += NWARP) {
+            const uint32_t Pl = S.Pmask[l];
+            uint64_t lo = 0, hi = 0;
+            for (int k = lane; k < cnt; k += 32) {
+                if (!((S.st_H[k] >> l) & 1)) continue;
+                for (uint32_t m = S.st_E[k] & Pl; m; m &= m - 1) {
+                    const int j = __ffs(m) - 1;
+                    if (j < 8) lo += 1ull << (8 * j);
+                    else hi += 1ull << (8 * (j - 8));
+                }
+            }
+            for (uint32_t m = Pl; m; m &= m - 1) {
+                const int j = __ffs(m) - 1;
+                int v = (int)(((j < 8) ? (lo >> (8 * j)) : (hi >> (8 * (j - 8)))) & 255u);
+                v = warp_sum(v);
+                if (lane == 0 && v) atomicAdd(&negp[l * n + j], v);
+            }
+        }
+        cov_bar();
+    }
+}
+
+// candidate mask table for the bit-sliced list pass (nL <= 64)
+__device__ void build_cmask(const CovSlot &d, Smem &S, int nL, uint64_t pu)
+{
+    for (int l = threadIdx.x; l < nL && l < L_SM; l += NT) {
+        uint32_t P = 0;
+        for (uint64_t m = cov_spread(S.Lpk[l] ^ pu); m; m &= m - 1) P |= 1u << ((__ffsll((long long)m) - 1) >> 2);
+        S.Pmask[l] = (uint16_t)P;
+    }
+    const int nq = d.n * d.q;
+    for (int t = threadIdx.x; t < nq; t += NT) {
+        const int j = t / d.q, v = t - j * d.q;
+        uint64_t m = 0;
+        for (int l = 0; l < nL && l < 64; l++)
+            if (cov_nib(S.Lpk[l], j) == v) m |= 1ull << l;
+        S.cmask[t] = m;
     }
 }
 
@@ -767,21 +942,29 @@ __device__ void ul_pass(const CovSlot &d, uint64_t pu, int nL, const uint64_t *L
 __device__ void op_neg(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank, int csize)
 {
     const int nL = P.nL, n = d.n;
-    if (rank != 0) {
-        for (int l = threadIdx.x; l < nL; l += NT) {
-            S.Lpk[l] = LS->Lpk[l];
-            S.Loh[l][0] = LS->Loh[l][0];
-            S.Loh[l][1] = LS->Loh[l][1];
+    const uint32_t n0 = (uint32_t)P.uln;
+    if (nL <= 64) {
+        // contiguous slice of the list per CTA; counts go straight into the
+        // leader's neg (one atomic per candidate and position per chunk)
+        if (rank != 0) {
+            for (int l = threadIdx.x; l < nL; l += NT) { S.Lpk[l] = LS->Lpk[l]; S.Pmask[l] = LS->Pmask[l]; }
+            for (int t = threadIdx.x; t < d.n * d.q; t += NT) S.cmask[t] = LS->cmask[t];
+            cov_bar();
         }
-        for (int x = threadIdx.x; x < nL * n; x += NT) S.neg[x] = 0;
-        __syncthreads();
+        const uint32_t per = (n0 + (uint32_t)csize - 1) / (uint32_t)csize;
+        const uint32_t e0 = min(n0, (uint32_t)rank * per), e1 = min(n0, e0 + per);
+        neg_chunks(d, S, P.pu, nL, e0, e1, LS->neg);
+        return;
     }
-    // the leader's warp 0 generates RNG draws; every other thread takes a slice
-    const int gt = rank * NT + (int)threadIdx.x - 32;
-    if (gt >= 0) ul_pass(d, P.pu, nL, S.Lpk, S.Loh, S.neg, (uint32_t)gt, (uint32_t)(csize * NT - 32), true);
-    else if (threadIdx.x == 0) rs_fill(S, S.rs_use + RS);
     if (rank != 0) {
-        __syncthreads();
+        for (int l = threadIdx.x; l < nL; l += NT) S.Lpk[l] = LS->Lpk[l];
+        for (int t = threadIdx.x; t < d.n * d.q; t += NT) S.cmask[t] = LS->cmask[t];
+        for (int x = threadIdx.x; x < nL * n; x += NT) S.neg[x] = 0;
+        cov_bar();
+    }
+    ul_pass(d, P.pu, nL, S.Lpk, S.cmask, S.neg, (uint32_t)rank * NT + threadIdx.x, (uint32_t)(csize * NT), n0);
+    if (rank != 0) {
+        cov_bar();
         for (int x = threadIdx.x; x < nL * n; x += NT)
             if (S.neg[x]) atomicAdd(&LS->neg[x], S.neg[x]);
     }
@@ -796,13 +979,14 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
 {
     const int tid = threadIdx.x;
     if (tid == 0) rs_ensure(S, 65);
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
     if (tid < 64) {
         uint32_t w = (uint32_t)(rs_peek(S, tid) % (uint64_t)d.N);
         unsigned m = __ballot_sync(0xffffffffu, cnt_of(d, w) == 0);
         if ((tid & 31) == 0) S.hitmask[tid >> 5] = m;
     }
-    __syncthreads();
+    cov_bar();
     int first = -1;
     if (S.hitmask[0]) first = __ffs(S.hitmask[0]) - 1;
     else if (S.hitmask[1]) first = 32 + __ffs(S.hitmask[1]) - 1;
@@ -811,13 +995,14 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
     uint32_t start = 0;
     if (first >= 0) result = (long long)(rs_peek(S, first) % (uint64_t)d.N);
     else start = (uint32_t)(rs_peek(S, 64) % (uint64_t)d.N);
-    __syncthreads();
+    cov_bar();
     if (tid == 0) S.rs_use += consumed;
+    __syncwarp();
     if (first >= 0 || S.unc <= 0) return result;     // no zero anywhere: -1
     if (S.ul_valid) {
         // every zero-count word is on the list: the first one after start is
         // the entry minimising (x - start) mod N
-        const int n0 = min(cov_ldcg(&d.st->ul_n), d.ul_cap);
+        const int n0 = S.uln;
         unsigned best = 0xffffffffu;
         for (int e = tid; e < n0; e += NT) {
             uint32_t x = cov_ldcg(&d.ul_idx[e]);
@@ -832,6 +1017,7 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
             return (long long)x;
         }
         if (tid == 0) set_error(d, COV_EDRIFT);
+        __syncwarp();
         return -1;
     }
     // chunked linear scan from start
@@ -852,13 +1038,14 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
         }
     }
     if (tid == 0) set_error(d, COV_EDRIFT);
+    __syncwarp();
     return -1;
 }
 
 // drop list entries that are covered again (covsearch2e.c:305-320)
 __device__ void leader_compact(const CovSlot &d, Smem &S)
 {
-    const int n0 = min(cov_ldcg(&d.st->ul_n), d.ul_cap);
+    const int n0 = S.uln;
     int m = 0;
     for (int c0 = 0; c0 < n0; c0 += NT) {
         int e = c0 + threadIdx.x;
@@ -874,15 +1061,107 @@ __device__ void leader_compact(const CovSlot &d, Smem &S)
         int tot = block_excl_scan(S, keep, pos);
         if (keep) { cov_stcg(&d.ul_idx[m + pos], x); cov_stcg(&d.ul_pk[m + pos], pk); }
         m += tot;
-        __syncthreads();
+        cov_bar();
     }
-    if (threadIdx.x == 0) d.st->ul_n = m;
-    __syncthreads();
+    if (threadIdx.x == 0) { d.st->ul_n = m; S.uln = m; }
+    __syncwarp();
+    cov_bar();
+}
+
+// Fisher-Yates resolved in parallel (shared-memory case, take <= PERM_CAP).
+// Step s swaps positions s and j_s >= s.  Position x changes before step s
+// only through earlier steps that target it, so with
+//   prevT(t) = last step t' < t with j_t' = t          (position t's feeder)
+//   W(t)     = value at position t when step t begins = W(prevT(t)) or t
+// the value sampled at step s is W(prevS(s)) when some earlier step
+// targeted j_s (prevS(s) = the last one), else j_s itself.  Steps are
+// bucketed by target (counting sort), each bucket sorted by step, and W
+// follows prevT chains by pointer jumping.  j_s arrives in dval[s]; the
+// result is written to perm[0..take).  ncand entries of fy_a/fy_b are used.
+__device__ void fy_parallel(Smem &S, int take, int ncand)
+{
+    const int tid = threadIdx.x;
+    int32_t *cnt = S.fy_a;        // per position: number of steps targeting it, then bucket start
+    int32_t *bkt = S.fy_b;        // bucketed step ids
+    uint32_t *perm = S.perm;
+    const int32_t *jv = S.dval;
+    for (int x = tid; x < ncand; x += NT) cnt[x] = 0;
+    cov_bar();
+    for (int s = tid; s < take; s += NT) atomicAdd(&cnt[jv[s]], 1);
+    cov_bar();
+    // exclusive prefix over positions, NT-chunked
+    {
+        const int CH = (ncand + NT - 1) / NT;
+        const int lo = min(ncand, tid * CH), hi = min(ncand, lo + CH);
+        int loc = 0;
+        for (int x = lo; x < hi; x++) loc += cnt[x];
+        int tot;
+        int pre = block_scan_int(S, loc, 0, [](int a, int b) { return a + b; }, tot);
+        for (int x = lo; x < hi; x++) { int c = cnt[x]; cnt[x] = pre; pre += c; }
+    }
+    cov_bar();
+    // place steps; cnt[x] becomes the end of bucket x
+    for (int s = tid; s < take; s += NT) {
+        const int slot = atomicAdd(&cnt[jv[s]], 1);
+        bkt[slot] = s;
+    }
+    cov_bar();
+    // sort each bucket by step (buckets are tiny); bucket x = [start, end)
+    for (int x = tid; x < ncand; x += NT) {
+        const int end = cnt[x];
+        int start = end;
+        // start of bucket x = end of bucket x-1 (cnt is an end pointer now)
+        start = x ? cnt[x - 1] : 0;
+        for (int a = start + 1; a < end; a++) {
+            int v = bkt[a], b = a - 1;
+            while (b >= start && bkt[b] > v) { bkt[b + 1] = bkt[b]; b--; }
+            bkt[b + 1] = v;
+        }
+    }
+    cov_bar();
+    // one thread per bucket (= position x): prevS for its steps and, for
+    // x < take, prevT(x) = the last step < x targeting x
+    int32_t *prevS = reinterpret_cast<int32_t *>(perm);   // perm[0..take) reused
+    for (int x = tid; x < ncand; x += NT) {
+        const int start = x ? cnt[x - 1] : 0, end = cnt[x];
+        int pt = -1;
+        for (int a = start; a < end; a++) {
+            const int st = bkt[a];
+            prevS[st] = a > start ? bkt[a - 1] : -1;
+            if (st < x) pt = st;
+        }
+        if (x < take) S.fy_c[x] = pt;
+    }
+    cov_bar();
+    // W by pointer jumping: w[t] is a step index until its chain is resolved,
+    // then -(value + 1).  Chains strictly decrease, so they end.
+    int32_t *w = S.fy_a;
+    for (int t = tid; t < take; t += NT) {
+        const int pt = S.fy_c[t];
+        w[t] = pt < 0 ? -(t + 1) : pt;
+    }
+    cov_bar();
+    for (int round = 0; round < 16; round++) {
+        int changed = 0;
+        for (int t = tid; t < take; t += NT) {
+            const int a = w[t];
+            if (a >= 0) { w[t] = w[a]; changed = 1; }
+        }
+        changed = cov_bar_or(changed);
+        if (!changed) break;
+    }
+    // perm[s] = W(prevS(s)) or j_s
+    for (int s = tid; s < take; s += NT) {
+        const int ps = prevS[s];
+        perm[s] = (uint32_t)(ps >= 0 ? -(w[ps] + 1) : jv[s]);
+    }
+    cov_bar();
 }
 
 __device__ void zero_acc(Smem &S)
 {
     if (threadIdx.x == 0) { S.dunc = 0; S.accT = 0; }
+    __syncwarp();
     if (threadIdx.x < COV_MAXN) S.accH[threadIdx.x] = 0;
 }
 
@@ -893,16 +1172,22 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     const int tid = threadIdx.x;
     const int n = d.n, R = d.R, M = d.M;
     if (tid == 0) {
-        if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
+        const int u = cov_ldcg(&d.st->ul_n);
+        if (S.ul_valid && u > d.ul_cap) S.ul_valid = 0;
+        S.uln = min(u, d.ul_cap);
         int stop = S.status != 0 || S.unc <= 0 || S.moves_left <= 0 ||
-                   (S.target >= 0 && S.best_unc <= S.target) || gtimer() > S.t_deadline;
-        if (!stop && gtimer() > S.t_deadline) S.status = COV_ETIMEOUT;
+                   (S.target >= 0 && S.best_unc <= S.target);
+        const bool late = (unsigned long long)cov_clock() > S.t_deadline;
+        if (!stop && late) S.status = COV_ETIMEOUT;
+        stop = stop || late;
         S.ibc[0] = stop;
         S.ibc[1] = !stop && !S.ul_valid && S.unc <= d.ul_cap / 2;
     }
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
     if (S.ibc[0]) {
         if (tid == 0) { S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
+        __syncwarp();
         return;
     }
     if (S.ibc[1]) {
@@ -911,12 +1196,13 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
             S.opp.op = OP_REBUILD_UL;
             S.phase = PH_REBUILD_DONE;
         }
+        __syncwarp();
         return;
     }
-    long long t0 = clock64();
-    if (S.ul_valid && (long long)cov_ldcg(&d.st->ul_n) > 2 * S.unc + 64) leader_compact(d, S);
+    long long t0 = cov_clock();
+    if (S.ul_valid && (long long)S.uln > 2 * S.unc + 64) leader_compact(d, S);
     if (tid == 0) {
-        long long t1 = clock64();
+        long long t1 = cov_clock();
         S.prof[6] += t1 - t0;
         t0 = t1;
         S.it++;
@@ -924,10 +1210,11 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         memset(&S.rec, 0, sizeof(S.rec));
         S.rec.it = S.it;
     }
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
     long long uw = leader_pick(d, S);
     if (tid == 0) {
-        long long t1 = clock64();
+        long long t1 = cov_clock();
         S.prof[0] += t1 - t0;
         t0 = t1;
         S.uw = uw;
@@ -935,7 +1222,8 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         S.pu = uw >= 0 ? pk_of_idx(d, (uint32_t)uw) : 0;
         S.rec.u = uw;
     }
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
     if (S.status) { if (tid == 0) { S.opp.op = OP_STOP; S.phase = PH_STOPPED; } return; }
     const uint64_t pu = S.pu;
 
@@ -948,7 +1236,8 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         dm = min(dm, (unsigned)dd);
     }
     dm = block_min_u32(S, dm);
-    if (tid == 0) { long long t1 = clock64(); S.prof[10] += t1 - t0; }
+    if (tid == 0) { long long t1 = cov_clock(); S.prof[10] += t1 - t0; }
+    __syncwarp();
     const int dtar = ((int)dm <= R + 1) ? R + 1 : (int)dm;
     // ordered list of codewords at distance dtar (covsearch2e.c:1359-1376):
     // always in global memory, the first L_SM also in shared memory with
@@ -970,7 +1259,6 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
             if (at < L_SM) {
                 S.L[at] = (uint32_t)i;
                 S.Lpk[at] = pk;
-                onehot(pk, n, d.q, S.Loh[at][0], S.Loh[at][1]);
             }
         }
         nL += tot;
@@ -980,9 +1268,9 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     const int ncand = nL * dtar;
     if (ncand == 0) {     // impossible for an uncovered target word
         if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
+        __syncwarp();
         return;
     }
-    if (tid == 0) { long long t1 = clock64(); S.prof[11] += t1 - t0; }
     const int take = min(ncand, d.cand);
     const int psm = ncand <= PERM_CAP;
     uint32_t *perm = psm ? S.perm : d.g_perm;
@@ -992,81 +1280,95 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     // generated in order by one thread, reduced in parallel, applied in order.
     for (int s0 = 0; s0 < take; s0 += RB) {
         const int cnt = min(RB, take - s0);
-        __syncthreads();
+        cov_bar();
         if (tid == 0) rs_ensure(S, cnt);
-        __syncthreads();
+        __syncwarp();
+        cov_bar();
         for (int t = tid; t < cnt; t += NT) {
             int s = s0 + t;
             dval[s] = s + (int32_t)fastmod(S, rs_peek(S, t), (uint64_t)(ncand - s));
         }
-        __syncthreads();
+        cov_bar();
         if (tid == 0) S.rs_use += cnt;
+        __syncwarp();
     }
-    __syncthreads();
-    if (tid == 0) {
-        long long t1 = clock64();
-        S.prof[12] += t1 - t0;
-        for (int s = 0; s < take; s++) {
-            int j = dval[s];
-            uint32_t tmp = perm[s]; perm[s] = perm[j]; perm[j] = tmp;
-        }
-    }
-    __syncthreads();
-    // distinct codewords among the sampled candidates (for the trace)
-    int ncw = nL;
-    if (take < ncand) {
-        int c = 0;
-        if (tid == 0) {
-            for (int s = 0; s < take; s++) {
-                int l = (int)(perm[s] / (uint32_t)dtar), dup = 0;
-                for (int t = 0; t < s; t++) if ((int)(perm[t] / (uint32_t)dtar) == l) { dup = 1; break; }
+    cov_bar();
+    // the sample's permutation: in parallel in shared memory; the oversized
+    // case is swapped in order by one thread while the others work on the
+    // entering side (apply_swaps), which does not need it
+    int pending = 1;
+    if (psm) {
+        // perm[c] = c was set above for c < ncand; fy_parallel rewrites
+        // perm[0..take) directly from the draws
+        fy_parallel(S, take, ncand);
+        pending = 0;
+        if (take < ncand && tid == 0) {
+            int c = 0;
+            for (int s2 = 0; s2 < take; s2++) {
+                int l = (int)(perm[s2] / (uint32_t)dtar), dup = 0;
+                for (int t2 = 0; t2 < s2; t2++) if ((int)(perm[t2] / (uint32_t)dtar) == l) { dup = 1; break; }
                 c += !dup;
             }
             S.ibc[2] = c;
         }
-        __syncthreads();
-        ncw = S.ibc[2];
+        cov_bar();
     }
     if (tid == 0) {
+        S.swaps_pending = pending;
         S.nL = nL; S.dtar = dtar; S.ncand = ncand; S.take = take;
-        S.rec.ncand = ncand; S.rec.ncw = ncw;
-        long long t1 = clock64();
+        S.rec.ncand = ncand; S.rec.ncw = (!pending && take < ncand) ? S.ibc[2] : nL;
+        long long t1 = cov_clock();
         S.prof[1] += t1 - t0;
         t0 = t1;
     }
+    __syncwarp();
     // entering side
     const int nsm = nL <= L_SM;
     int32_t *negp = nsm ? S.neg : d.g_neg;
     for (int x = tid; x < nL * n; x += NT) negp[x] = 0;
     zero_acc(S);
-    __syncthreads();
+    cov_bar();
     if (!S.ul_valid) {
         if (tid == 0) {
+            apply_swaps(d, S);
             OpParams &o = S.opp;
             o.op = OP_NEGWALK; o.nL = nL; o.dtar = dtar; o.pu = pu;
             o.L_sm = Lsm; o.neg_sm = nsm; o.ul_valid = 0;
             S.phase = PH_SELECT;
         }
+        __syncwarp();
         return;
     }
-    const bool use_oh = d.q * n <= 128;
-    const long long pairs = (long long)min(cov_ldcg(&d.st->ul_n), d.ul_cap) * nL;
-    if (csize > 1 && Lsm && use_oh && pairs >= NEG_CLUSTER_PAIRS) {
+    if (Lsm) build_cmask(d, S, nL, pu);
+    cov_bar();
+    const long long pairs = (long long)S.uln * nL;
+    long long tp0 = 0;
+    if (tid == 0) tp0 = cov_clock();
+    __syncwarp();
+    if (csize > 1 && Lsm && pairs >= d.neg_cluster_pairs) {
         if (tid == 0) {
             OpParams &o = S.opp;
-            o.op = OP_NEG; o.nL = nL; o.dtar = dtar; o.pu = pu;
+            o.op = OP_NEG; o.nL = nL; o.dtar = dtar; o.pu = pu; o.uln = S.uln;
             o.L_sm = 1; o.neg_sm = 1; o.ul_valid = 1;
             S.phase = PH_SELECT;
-            S.prof[2] += clock64() - t0;
+            S.prof[2] += cov_clock() - t0;
             S.ul_pairs += pairs;
         }
+        __syncwarp();
         return;
     }
-    if (Lsm) {
-        ul_pass(d, pu, nL, S.Lpk, S.Loh, negp, tid, NT, use_oh);
+    if (Lsm && nL <= 64) {
+        neg_chunks(d, S, pu, nL, 0, (uint32_t)S.uln, negp);
+        if (tid == 0) S.prof[13] += cov_clock() - tp0;
+        __syncwarp();
+    } else if (Lsm) {
+        ul_pass(d, pu, nL, S.Lpk, S.cmask, negp, tid, NT, (uint32_t)S.uln);
+        cov_bar();
     } else {
+        if (tid == 0) apply_swaps(d, S);
+        __syncwarp();
         // oversized candidate list: codes from global memory, nibble test
-        const int n0 = min(cov_ldcg(&d.st->ul_n), d.ul_cap);
+        const int n0 = S.uln;
         const uint64_t nm = nibmask(n);
         for (int e = tid; e < n0; e += NT) {
             uint32_t x = cov_ldcg(&d.ul_idx[e]);
@@ -1086,12 +1388,13 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
             }
         }
     }
-    __syncthreads();
+    cov_bar();
     if (tid == 0) {
         S.phase = PH_SELECT;
-        S.prof[2] += clock64() - t0;
-        S.ul_pairs += (long long)min(cov_ldcg(&d.st->ul_n), d.ul_cap) * nL;
+        S.prof[2] += cov_clock() - t0;
+        S.ul_pairs += (long long)S.uln * nL;
     }
+    __syncwarp();
     S.opp.op = -1;   // no op yet: select follows
 }
 
@@ -1108,7 +1411,10 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
     int32_t *dval = psm ? S.dval : d.g_dval;
     uint32_t *Lp = Lsm ? S.L : d.g_list;
     int32_t *negp = Lsm ? S.neg : d.g_neg;
-    const long long t0 = clock64();
+    const long long t0 = cov_clock();
+    if (tid == 0) apply_swaps(d, S);
+    __syncwarp();
+    cov_bar();
     // deltas and tabu flags in parallel (shared-memory case); the rare
     // oversized case recomputes them inside the serial scan below
     if (psm) {
@@ -1124,7 +1430,7 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
             S.tflag[s] = (uint8_t)((long long)cov_ldcg(&d.tabu[((size_t)k * n + p) * q + v]) > S.it);
         }
     }
-    __syncthreads();
+    cov_bar();
     // Selection (covsearch2e.c:1503-1518) in parallel.  Scanning s in order
     // with eligible keys d_s, a "reset" is an eligible s with d_s below the
     // running minimum and an "event" one equal to it; each event draws once
@@ -1162,7 +1468,8 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
                                             [](int a2, int b2) { return b2 != -1 ? b2 : a2; }, dummy);
         if (V != INF && E <= RS / 2) {
             if (tid == 0) rs_ensure(S, E);
-            __syncthreads();
+            __syncwarp();
+            cov_bar();
             // first occurrence of V and the last winning event at V
             int firstV = INF, win = -1;
             m = pmin;
@@ -1187,13 +1494,14 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
             consumed = E;
         } else if (V == INF) {
             if (tid == 0) { rs_ensure(S, 1); }
-            __syncthreads();
+            __syncwarp();
+            cov_bar();
             bs_par = (int)fastmod(S, rs_peek(S, 0), (uint64_t)take);
             consumed = 1;
         }
     }
     if (tid == 0) {
-        long long ts1 = clock64();
+        long long ts1 = cov_clock();
         S.prof[8] += ts1 - t0;
         int bs = -1;
         if (bs_par >= 0) {
@@ -1226,7 +1534,7 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
             }
             if (bs < 0) bs = (int)fastmod(S, rs_take(S), (uint64_t)take);
         }
-        long long ts2 = clock64();
+        long long ts2 = cov_clock();
         S.prof[9] += ts2 - ts1;
         uint32_t c = perm[bs];
         int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
@@ -1250,8 +1558,9 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
         S.ibc[3] = oldv;
         S.rec.i = k; S.rec.p = p; S.rec.v = v; S.rec.delta = dd;
         S.phase = PH_FINISH_MOVE;
-        S.prof[3] += clock64() - t0;
+        S.prof[3] += cov_clock() - t0;
     }
+    __syncwarp();
 }
 
 __device__ void write_trace(const CovSlot &d, Smem &S)
@@ -1271,7 +1580,7 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
 {
     const int tid = threadIdx.x;
     const int n = d.n, q = d.q;
-    const long long t0 = clock64();
+    const long long t0 = cov_clock();
     if (tid == 0) {
         long long dunc = (long long)S.dunc;
         S.unc += dunc;
@@ -1290,9 +1599,10 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
         if (S.improved) { S.best_unc = S.unc; S.since_improve = 0; }
         else if (++S.since_improve > d.stall) S.dokick = 1;
     }
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
     if (S.improved) copy_best(d);
-    __syncthreads();
+    cov_bar();
     if (tid == 0) {
         if (S.dokick) { S.kick_t = 0; S.phase = PH_KICK_START; }
         else {
@@ -1300,9 +1610,10 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
             write_trace(d, S);
             S.phase = PH_PLAN;
         }
-        S.prof[5] += clock64() - t0;
+        S.prof[5] += cov_clock() - t0;
     }
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
 }
 
 // one leader step: consume the result of the previous op, do the serial
@@ -1311,25 +1622,27 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
 {
     const int tid = threadIdx.x;
     for (int guard = 0; guard < 64; guard++) {
-        __syncthreads();
+        cov_bar();
         const int ph = S.phase;
-        __syncthreads();
+        cov_bar();
         if (ph == PH_STOPPED) { if (tid == 0) S.opp.op = OP_STOP; return; }
         if (ph == PH_PLAN) {
             if (S.mode == MODE_GREEDY) { if (tid == 0) S.phase = PH_GREEDY; continue; }
             leader_plan(d, S, csize);
-            __syncthreads();
-            if (S.phase == PH_SELECT && S.opp.op == -1) { leader_select(d, S); __syncthreads(); return; }
+            cov_bar();
+            if (S.phase == PH_SELECT && S.opp.op == -1) { leader_select(d, S); cov_bar(); return; }
             return;
         }
-        if (ph == PH_SELECT) { leader_select(d, S); __syncthreads(); return; }
+        if (ph == PH_SELECT) { leader_select(d, S); cov_bar(); return; }
         if (ph == PH_FINISH_MOVE) { leader_finish_move(d, S); continue; }
         if (ph == PH_REBUILD_DONE) {
             if (tid == 0) {
                 int cnt = cov_ldcg(&d.st->ul_n);
                 S.ul_valid = cnt <= d.ul_cap;
+                S.uln = min(cnt, d.ul_cap);
                 S.phase = PH_PLAN;
             }
+            __syncwarp();
             continue;
         }
         if (ph == PH_KICK_START) {
@@ -1338,7 +1651,9 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                     S.opp.op = OP_ZERO_TABU;
                     S.phase = PH_KICK_DONE;
                 } else {
-                    if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
+                    const int cnt = cov_ldcg(&d.st->ul_n);
+                    if (S.ul_valid && cnt > d.ul_cap) S.ul_valid = 0;
+                    S.uln = min(cnt, d.ul_cap);
                     int i = (int)fastmod(S, rs_take(S), (uint64_t)d.M);
                     uint64_t pk = leader_code(d, S, i);
                     OpParams &o = S.opp;
@@ -1348,15 +1663,20 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                     S.phase = PH_KICK_PICK;
                 }
             }
-            __syncthreads();
+            __syncwarp();
+            cov_bar();
             return;
         }
         if (ph == PH_KICK_PICK) {
             if (tid == 0) {
                 S.unc += (long long)S.dunc;
-                if (S.ul_valid && cov_ldcg(&d.st->ul_n) > d.ul_cap) S.ul_valid = 0;
+                // the -1 ball appended newly uncovered words to the list
+                const int cnt = cov_ldcg(&d.st->ul_n);
+                if (S.ul_valid && cnt > d.ul_cap) S.ul_valid = 0;
+                S.uln = min(cnt, d.ul_cap);
             }
-            __syncthreads();
+            __syncwarp();
+            cov_bar();
             long long w = leader_pick(d, S);
             if (tid == 0) {
                 uint64_t pk;
@@ -1381,7 +1701,8 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 S.dunc = 0;
                 S.phase = PH_KICK_RECOMP;
             }
-            __syncthreads();
+            __syncwarp();
+            cov_bar();
             return;
         }
         if (ph == PH_KICK_RECOMP) {
@@ -1392,8 +1713,9 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 o.basen = o.base; o.pcn = o.pc;
                 S.phase = PH_KICK_END;
             }
+            __syncwarp();
             zero_acc(S);
-            __syncthreads();
+            cov_bar();
             return;
         }
         if (ph == PH_KICK_END) {
@@ -1405,6 +1727,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 S.kick_t++;
                 S.phase = PH_KICK_START;
             }
+            __syncwarp();
             continue;
         }
         if (ph == PH_KICK_DONE) {
@@ -1417,13 +1740,15 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 write_trace(d, S);
                 S.phase = PH_PLAN;
             }
+            __syncwarp();
             continue;
         }
         if (ph == PH_GREEDY) {
             // greedy placement on uncovered words: covsearch2e.c:1210-1234
             if (S.greedy_i >= d.M) {
                 if (tid == 0) { S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
-                __syncthreads();
+                __syncwarp();
+                cov_bar();
                 return;
             }
             long long w = leader_pick(d, S);
@@ -1438,7 +1763,8 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 S.dunc = 0;
                 S.phase = PH_GREEDY_NEXT;
             }
-            __syncthreads();
+            __syncwarp();
+            cov_bar();
             return;
         }
         if (ph == PH_GREEDY_NEXT) {
@@ -1447,14 +1773,17 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 S.greedy_i++;
                 S.phase = PH_GREEDY;
             }
+            __syncwarp();
             continue;
         }
         if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
-        __syncthreads();
+        __syncwarp();
+        cov_bar();
         return;
     }
     if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
 }
 
 // ------------------------------------------------------------- kernel -----
@@ -1469,7 +1798,8 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
     const int csize = (int)cl.num_blocks();
     const int cid = blockIdx.x / csize;
     if (threadIdx.x == 0) S.slot = slots[cluster_slot[cid]];
-    __syncthreads();
+    __syncwarp();
+    cov_bar();
     const CovSlot &d = S.slot;
     const bool leader = rank == 0;
     Smem *LS = cl.map_shared_rank(&S, 0);
@@ -1489,32 +1819,34 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         S.mode = mode;
         S.greedy_i = (int)st->moves_left;   // greedy: first codeword to place
         S.phase = PH_PLAN;
-        S.t_deadline = gtimer() + budget_ns;
+        S.t_deadline = (unsigned long long)cov_clock() + budget_ns * COV_CYCLES_PER_NS;
         S.guard = 0;
         S.opp.op = -1;
-        for (int k = 0; k < 16; k++) S.prof[k] = st->prof[k];
+        for (int k = 0; k < 24; k++) S.prof[k] = st->prof[k];
         S.ul_pairs = st->stat_ul_pairs;
     }
-    cl.sync();
+    cov_cbar(cl);
     for (;;) {
         if (leader) {
             leader_step(d, S, csize);
             // safety net: an op budget and the launch deadline bound every
             // launch even if the phase machine never reaches a move boundary
             if (threadIdx.x == 0 && S.opp.op != OP_STOP &&
-                (++S.guard > op_guard || gtimer() > S.t_deadline + 1000000000ull)) {
+                (++S.guard > op_guard ||
+                 (unsigned long long)cov_clock() > S.t_deadline + 1000000000ull * COV_CYCLES_PER_NS)) {
                 S.status = COV_ETIMEOUT;
                 S.opp.op = OP_STOP;
                 S.phase = PH_STOPPED;
             }
         }
-        cl.sync();
+        cov_cbar(cl);
         if (threadIdx.x == 0) S.opl = LS->opp;
-        __syncthreads();
+        __syncwarp();
+        cov_bar();
         const OpParams &P = S.opl;
         const int op = P.op;
         if (op == OP_STOP) break;
-        const long long top = clock64();
+        const long long top = cov_clock();
         if (op == OP_MOVE) {
             op_move(d, P, S, LS, rank, csize);
             if (d.M <= CODE_SM && threadIdx.x == 0) S.code_sm[P.mi] = P.pcn;
@@ -1525,7 +1857,7 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         } else if (op == OP_BALL) {
             // a +1 ball places the slot's new codeword: mirror it first
             if (P.sgn > 0 && d.M <= CODE_SM && threadIdx.x == 0) S.code_sm[P.mi] = P.pc;
-            __syncthreads();
+            cov_bar();
             op_ball(d, P, LS, rank, csize);
         } else if (op == OP_RECOMPUTE) {
             op_recompute(d, P.basen, P.pcn, S, LS, rank, csize);
@@ -1534,16 +1866,16 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         } else if (op == OP_REBUILD_UL) {
             op_rebuild_ul(d, rank, csize, cl);
         }
-        cl.sync();
+        cov_cbar(cl);
         if (leader && threadIdx.x == 0) {
-            const long long dt = clock64() - top;
+            const long long dt = cov_clock() - top;
             if (op == OP_MOVE) S.prof[4] += dt;
-            else if (op == OP_NEGWALK || op == OP_NEG) S.prof[2] += dt;
+            else if (op == OP_NEGWALK || op == OP_NEG) { S.prof[2] += dt; S.prof[14] += dt; }
             else S.prof[7] += dt;
         }
     }
     // no CTA may leave while another can still read the leader's shared memory
-    cl.sync();
+    cov_cbar(cl);
     if (leader && threadIdx.x == 0) {
         CovSlotState *st = d.st;
         rs_final(S, st->rng);
@@ -1551,7 +1883,7 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         st->since_improve = S.since_improve; st->nkicks = S.nkicks;
         st->moves_left = S.moves_left; st->trace_n = S.trace_n;
         st->ul_valid = S.ul_valid;
-        for (int k = 0; k < 16; k++) st->prof[k] = S.prof[k];
+        for (int k = 0; k < 24; k++) st->prof[k] = S.prof[k];
         st->stat_ul_pairs = S.ul_pairs;
         int s0 = atomicAdd(&st->status, 0);
         st->status = S.status ? S.status : s0;
@@ -1672,12 +2004,13 @@ __global__ void k_unique_cover(CovSlot d, int count, int *out)
     __shared__ int red[32];
     u = warp_sum(u);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = u;
-    __syncthreads();
+    cov_bar();
     if (threadIdx.x == 0) {
         int s = 0;
         for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) s += red[w];
         out[i] = s;
     }
+    __syncwarp();
 }
 
 // per-launch budget of every listed slot, set on the device so that a run
@@ -1760,6 +2093,7 @@ struct cov_pool {
     bool use_ext = false;
     double budget_s = 30.0;
     long long launch_moves = 0;      // move budget of the current launch
+    long long neg_cluster_pairs = NEG_CLUSTER_PAIRS;
     cudaGraphExec_t gexec = nullptr; // captured multi-step run
     long long g_moves = -1, g_target = -2;
     int g_steps = 0;
@@ -1976,6 +2310,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     for (int k = 0; k <= COV_MAXN; k++) d.ppow[k] = (uint32_t)std::min<long long>(ipow_h(q - 1, k), 0xffffffffLL);
     d.tenure = prm->tabu; d.kick = prm->kick; d.cand = prm->cand; d.stall = prm->stall;
     d.ul_cap = UL_CAP_DEFAULT;
+    d.neg_cluster_pairs = pool->neg_cluster_pairs;
     std::vector<uint8_t> subs((size_t)n * std::max(d.nsub, 1) * d.rs, 0);
     for (int p = 0; p < n; p++) {
         int pool_[32], np = 0;
@@ -2268,6 +2603,28 @@ int cov_pool_graph_run(cov_pool *pool, int64_t moves, int64_t target, int32_t st
     return COV_OK;
 }
 
+// Tuning knobs (applied to every slot, present and future):
+//   "neg_cluster_pairs"  list x candidate pairs from which the whole cluster
+//                        shares the uncovered-list pass (default 32768)
+int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value)
+{
+    if (!pool || !name) return COV_EINVAL;
+    if (!strcmp(name, "neg_cluster_pairs")) {
+        if (value < 0) return COV_EINVAL;
+        pool->neg_cluster_pairs = value;
+        for (int s = 0; s < pool->max_slots; s++) {
+            if (!pool->slots[s].used) continue;
+            pool->slots[s].d.neg_cluster_pairs = value;
+            int rc = push_slot(pool, s);
+            if (rc) return rc;
+        }
+        CK(cudaStreamSynchronize(pool->cur_stream()));
+        if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        return COV_OK;
+    }
+    return COV_EINVAL;
+}
+
 // Run on the caller's stream (a cudaStream_t passed as void*); NULL returns
 // to the pool's own stream.
 int cov_pool_set_stream(cov_pool *pool, void *stream)
@@ -2386,15 +2743,15 @@ int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4)
     return COV_OK;
 }
 
-// leader phase cycle counts (16) followed by the list-pair counter
-int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out17)
+// leader phase cycle counts (24) followed by the list-pair counter
+int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out25)
 {
-    if (!pool || !out17 || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    if (!pool || !out25 || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
     CovSlotState hs;
     int rc = read_state(pool, slot, &hs);
     if (rc) return rc;
-    for (int k = 0; k < 16; k++) out17[k] = hs.prof[k];
-    out17[16] = (uint64_t)hs.stat_ul_pairs;
+    for (int k = 0; k < 24; k++) out25[k] = hs.prof[k];
+    out25[24] = (uint64_t)hs.stat_ul_pairs;
     return COV_OK;
 }
 

@@ -38,6 +38,9 @@ class Pool:
         self.meta = {}
         L.check(self.lib.cov_pool_set_budget(self.h, float(budget_s)), "cov_pool_set_budget")
 
+    def set_param(self, name, value):
+        L.check(self.lib.cov_pool_set_param(self.h, name.encode(), int(value)), "cov_pool_set_param")
+
     def add(self, q, n, R, M, code=None, random_init=False, seed=12345, tabu=0, kick=2,
             stall=5000, cand=100000, trace=0, trace_cap=0):
         """Create an instance from `code` (m x n digits; m may be <, = or > M)."""
@@ -134,14 +137,14 @@ class Pool:
 
     def prof(self, slot):
         """Leader phase cycle counts and the list-pair counter."""
-        out = np.zeros(17, dtype=np.uint64)
+        out = np.zeros(25, dtype=np.uint64)
         L.check(self.lib.cov_pool_get_prof(self.h, int(slot),
                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
                 "cov_pool_get_prof")
         d = {k: int(v) for k, v in zip(self.PROF_NAMES, out[:8])}
-        for k in range(8, 16):
+        for k in range(8, 24):
             d["sub%d" % k] = int(out[k])
-        d["ul_pairs"] = int(out[16])
+        d["ul_pairs"] = int(out[24])
         return d
 
     def trace(self, slot):

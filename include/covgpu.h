@@ -95,6 +95,9 @@ typedef struct {
  * GPU entry; cov_pool_* generalises it to uneven instances. */
 int cov_pool_create(int32_t max_slots, int32_t cluster, cov_pool **out);
 int cov_pool_set_budget(cov_pool *pool, double seconds);   /* per-launch wall limit */
+/* Tuning knob by name ("neg_cluster_pairs": list x candidate pairs from
+ * which the whole cluster shares the uncovered-list pass). */
+int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value);
 /* Device bytes one slot with these parameters occupies (0 = invalid). */
 size_t cov_slot_bytes(const cov_params *prm);
 /* Add an instance and build its initial state from `m` codewords
@@ -132,9 +135,9 @@ int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4);
  * counterpart of the reference's -DPROF timers, covsearch2e.c:109-131):
  * [0] pick [1] candidates+sample [2] entering side [3] select
  * [4] commit+sphere [5] finish [6] list compaction [7] other ops,
- * [8..15] finer sub-phases, then [16] uncovered-list x candidate-codeword
+ * [8..23] finer sub-phases, then [24] uncovered-list x candidate-codeword
  * pairs tested. */
-int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out17);
+int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out25);
 int cov_pool_get_trace(cov_pool *pool, int32_t slot, cov_move_rec *out,
                        int64_t cap, int64_t *n_out);
 int cov_pool_remove(cov_pool *pool, int32_t slot);
