@@ -303,6 +303,55 @@ int cov_mindist_dev(int32_t q, int32_t n, const uint8_t *d_code, int32_t M, uint
     return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free distance transform.
+//
+// For callers that must not allocate device memory themselves: a host runtime
+// whose device memory is entirely owned by another allocator (for example a
+// framework's caching allocator that has reserved the whole GPU), or code
+// that runs where an allocation would break the surrounding contract (inside
+// an out-of-memory handler, or while another component is capturing the
+// stream).  The one scratch buffer the transform needs -- the bitmap of
+// codeword positions -- lives in a file-scope device array instead of being
+// allocated per call.
+//
+//  * Limit: q^n <= COV_DT_STATIC_MAX_WORDS (2^26 words, an 8 MiB bitmap that
+//    every GPU which loads the library keeps until the process exits).
+//  * The first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress, with that device current) and caches it; make
+//    that first call before any stream capture.
+//  * Every call uses the same array and clears it before use: two calls
+//    whose work overlaps on the GPU (different streams, no ordering) race.
+#define COV_DT_STATIC_MAX_WORDS (1u << 26)
+#define COV_DT_STATIC_MAX_DEVICES 64
+
+static __device__ __align__(256) uint32_t g_dt_static_bitmap[COV_DT_STATIC_MAX_WORDS / 32];
+static uint32_t *g_dt_static_addr[COV_DT_STATIC_MAX_DEVICES];   // per device, host side
+
+int cov_mindist_dev_static(int32_t q, int32_t n, const uint8_t *d_code, int32_t M, uint8_t *d_dist, void *stream)
+{
+    DtGeom g;
+    int rc = geom(q, n, g);
+    if (rc) return rc;
+    if (g.N > COV_DT_STATIC_MAX_WORDS) {
+        fprintf(stderr, "cov_mindist_dev_static: q^n = %u words exceeds the %u-word limit of the static scratch\n",
+                g.N, COV_DT_STATIC_MAX_WORDS);
+        return COV_ERANGE;
+    }
+    if (M < 0 || (M > 0 && !d_code) || !d_dist) return COV_EINVAL;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= COV_DT_STATIC_MAX_DEVICES) return COV_ENODEV;
+    if (!g_dt_static_addr[dev]) {
+        // the array's name is only a host-side stand-in: ask the runtime for
+        // its address on the current device
+        void *ptr = nullptr;
+        CK(cudaGetSymbolAddress(&ptr, g_dt_static_bitmap));
+        g_dt_static_addr[dev] = (uint32_t *)ptr;
+    }
+    return dt_run(g, d_code, M, d_dist, nullptr, g_dt_static_addr[dev], (cudaStream_t)stream);
+}
+
 int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist, int32_t R, void *stream)
 {
     DtGeom g;

@@ -169,6 +169,15 @@ int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code,
                   int32_t M, uint16_t *d_cnt, void *stream);
 int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist,
                             int32_t R, void *stream);
+/* cov_mindist_dev without any device allocation, for callers that cannot
+ * allocate (their device memory belongs to another allocator, or they run
+ * where an allocation is not allowed).  No counterpart in the reference.
+ * Its one scratch buffer is a file-scope device array: q^n must be at most
+ * 2^26 (else COV_ERANGE); the first call on a device looks the array up and
+ * should come before any stream capture; calls that overlap on the GPU
+ * share the array and race. */
+int cov_mindist_dev_static(int32_t q, int32_t n, const uint8_t *d_code,
+                           int32_t M, uint8_t *d_dist, void *stream);
 
 #ifdef __cplusplus
 }
