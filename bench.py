@@ -17,8 +17,10 @@ Printed (rank 0, one JSON line):
                step re-seeds every restart from a pinned host code (H2D),
                builds its state, runs --moves moves and reads every best code
                back (D2H)
-  roofline     the batched kernel's algorithmic bytes / its time vs the
-               measured HBM copy bandwidth
+  roofline     the batched kernel's algorithmic bytes (the reference
+               algorithm's per-move bytes with the measured candidate and
+               list counts) / its time vs the measured HBM copy bandwidth;
+               `design` gives the same for the bytes this engine touches
   cpu_baseline the oracle restatement of the reference engine timed on this
                host's cores (independent restarts, one per core)
 --impl reference times that CPU path alone (the reference arm).
@@ -156,14 +158,32 @@ def profiled_traffic():
     return d.get("dram_bytes_per_move")
 
 
-def algo_bytes_per_move(q, n, R, M):
-    """Bytes one move of this engine must touch (word granularity):
-    commit  2 S' counter words read + written (4 B each, S' = C(n-1,R)(q-1)^R)
-    sphere  S_R counter words read for the moved codeword (S_R = C(n,R)(q-1)^R)
-    scan    M packed codewords (8 B) for the candidate distances."""
+def algo_bytes_per_move(q, n, R, M, ncw, ul_n, b_r=1, b_c=2):
+    """Algorithmic bytes of one tabu move of the reference algorithm (p5b,
+    uncovered list on):
+        ncw * S_R * b_r      every candidate codeword's radius-R sphere read
+                             once (covsearch2e.c:592-654)
+      + U_n * (n + b_c)      the uncovered list: digits and count of each entry
+                             (covsearch2e.c:720-734)
+      + 2 * S' * 2 * b_c     commit: the leaving and the entering word read
+                             and written (covsearch2e.c:450-493)
+      + M * n                the distance scan over the code
+    S_R = C(n,R)(q-1)^R, S' = C(n-1,R)(q-1)^R; ncw and U_n are the measured
+    means per move; b_r = 1 (the 1-byte shadow the reference reads), b_c = 2
+    (its uint16 counts)."""
     Sp = math.comb(n - 1, R) * (q - 1) ** R
     SR = math.comb(n, R) * (q - 1) ** R
-    return 2 * Sp * 8 + SR * 4 + M * 8
+    return ncw * SR * b_r + ul_n * (n + b_c) + 2 * Sp * 2 * b_c + M * n
+
+
+def design_bytes_per_move(q, n, R, M, ul_n):
+    """Bytes one move of this engine touches at word granularity: the commit
+    reads and writes 2 S' 4-byte counters, the moved codeword's sphere
+    change reads 2 C(n-1,R-1)(q-1)^(R-1) counters, the list pass reads U_n
+    entries of 12 bytes and the distance scan M packed codewords."""
+    Sp = math.comb(n - 1, R) * (q - 1) ** R
+    X = math.comb(n - 1, R - 1) * (q - 1) ** (R - 1) if R >= 1 else 0
+    return 2 * Sp * 8 + 2 * X * 4 + ul_n * 12 + M * 8
 
 
 # ------------------------------------------------------------------ GPU ----
@@ -188,6 +208,7 @@ def gpu_bench(args, rank, world, dist):
     for _ in range(args.warmup):
         pool.run(S)
     it0 = sum(s["it"] for s in pool.status_all(args.restarts))
+    prof0 = [pool.prof(sl) for sl in slots]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -227,6 +248,10 @@ def gpu_bench(args, rank, world, dist):
     value = moves_all / (ms_max / 1e3)
     finished = sum(1 for s in st if s["finished"])
     best_unc = [s["best"] for s in st]
+    prof1 = [pool.prof(sl) for sl in slots]
+    pm = sum(b["planned_moves"] - a["planned_moves"] for a, b in zip(prof0, prof1))
+    work = dict(ncw=sum(b["sum_ncw"] - a["sum_ncw"] for a, b in zip(prof0, prof1)) / max(1, pm),
+                ul_n=sum(b["sum_ul_n"] - a["sum_ul_n"] for a, b in zip(prof0, prof1)) / max(1, pm))
 
     # ---------------- e2e: host buffers through the public API
     e2e = None
@@ -309,7 +334,7 @@ def gpu_bench(args, rank, world, dist):
         cov = dict(dt_words_s=Nw / (dt_ms / 1e3), dt_ms=dt_ms, count_words_s=Nw / (ct_ms / 1e3), count_ms=ct_ms,
                    dt_traffic_bytes=int(Nw * 3.25), uncovered=unc_dt)
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
-                plain=plain, cov=cov, finished=finished, best_unc=best_unc)
+                plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work)
 
 
 def main():
@@ -368,10 +393,13 @@ def main():
     r = gpu_bench(args, rank, world, dist)
     if rank == 0:
         peak, peak_kind = measured_peaks()
-        bpm = algo_bytes_per_move(Q, N_, R_, M_)
+        w = r["work"]
+        bpm = algo_bytes_per_move(Q, N_, R_, M_, w["ncw"], w["ul_n"])
+        dpm = design_bytes_per_move(Q, N_, R_, M_, w["ul_n"])
         launch_ms = statistics.mean(r["step_ms"])
         moves_per_launch = r["moves"] / max(1, args.steps) / max(1, world)
         achieved = bpm * moves_per_launch / (launch_ms / 1e3) / 1e9
+        d_achieved = dpm * moves_per_launch / (launch_ms / 1e3) / 1e9
         tpm = profiled_traffic()
         line = dict(
             metric=METRIC, value=r["value"], unit="moves/s", n_gpus=world, steps=args.steps, warmup=args.warmup,
@@ -384,7 +412,11 @@ def main():
             roofline=dict(bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
                           traffic=(tpm * moves_per_launch) if tpm else None,
                           peak_source=peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                          algorithmic_bytes_per_move=bpm, kernel="cov_run_kernel"),
+                          algorithmic_bytes_per_move=bpm, mean_candidate_codewords=w["ncw"],
+                          mean_list_length=w["ul_n"], moves_per_launch=moves_per_launch,
+                          launch_ms=launch_ms, kernel="cov_run_kernel",
+                          design=dict(bytes_per_move=dpm, achieved=d_achieved, frac=d_achieved / peak,
+                                      note="bytes this engine's own algorithm touches per move")),
             clocks=r["clocks"],
             e2e=r["e2e"],
             gpu_launches=2 * args.steps,

@@ -66,6 +66,17 @@ __device__ __forceinline__ int cov_dist(uint64_t a, uint64_t b)
     return __popcll(cov_spread(a ^ b));
 }
 
+// Counter word of the coverage array: the multiplicity in bits 0-15 and the
+// sum (mod 2^16) of the ids of the covering codewords in bits 16-31.  When
+// the multiplicity is 1 the sum is the id of the only covering codeword.
+// Adding or removing coverer i is one 32-bit add of cov_cw_unit(i): the
+// multiplicity never exceeds M <= 65535, so it never carries into the sum,
+// and it is >= 1 before a removal, so nothing borrows from the sum.
+__host__ __device__ __forceinline__ uint32_t cov_cw_unit(int i)
+{
+    return 1u + ((uint32_t)i << 16);
+}
+
 // ------------------------------------------------------------ slots ------
 // One search instance.  Immutable after creation except through the
 // pointed-to device arrays.
@@ -81,7 +92,7 @@ struct CovSlot {
     long long stall;
     long long neg_cluster_pairs; // list x candidate pairs above which the cluster shares the list pass
     // device arrays
-    uint32_t *cw;                // [N]  cnt (bits 0-15) | xor of covering ids (16-31)
+    uint32_t *cw;                // [N]  cnt (bits 0-15) | sum of covering ids mod 2^16 (16-31)
     uint64_t *code;              // [M]  packed codewords
     uint64_t *best;              // [M]  best code so far
     int32_t *tabu;               // [M*n*q]
@@ -95,6 +106,14 @@ struct CovSlot {
     int nsub1;                   // C(n-1,R-1)
     const uint8_t *ball_sub;     // concatenated r-subset tables, r = 0..R
     int ball_off[COV_MAXN + 2];  // start (in subsets) of radius r in ball_sub
+    // state build by tiles: a tile is the q^bt_nl words that share their
+    // first bt_nh digits; bt_items lists the ball of radius <= min(R, bt_nl)
+    // on the low digits (nibble j = value index + 1 at position j, 0 = the
+    // centre's digit), by radius: bt_v[r] items have radius <= r
+    const uint64_t *bt_items;
+    int bt_nh, bt_nl;
+    uint32_t bt_tw;              // q^bt_nl
+    uint32_t bt_v[COV_MAXN + 2];
     // per-slot global scratch for the rare large cases
     uint32_t *g_perm;            // [M*n]
     int32_t *g_dval;             // [M*n]
@@ -125,7 +144,8 @@ struct CovSlotState {
     // cycle counts of the leader's phases, accumulated over launches:
     // 0 pick, 1 candidates + sample, 2 entering side, 3 select, 4 move op
     // (commit + sphere), 5 finish, 6 list compaction, 7 other ops
-    unsigned long long prof[24];   // 8..23: sub-phases (diagnostics)
+    unsigned long long prof[24];   // 8..19: sub-phases (diagnostics); 20: sum of candidate
+                                   // codewords, 21: sum of list lengths, 22: planned moves
 };
 
 // Generic enumeration unit of a sphere of radius r >= 1 around a word:

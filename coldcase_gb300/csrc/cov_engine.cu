@@ -12,7 +12,7 @@
 //   * here those counts are kept per codeword in P[k] = (T_k, H_k[0..n-1])
 //     and updated incrementally: a word's count crosses 1 only inside a
 //     commit or a kick, and when cnt[w] == 1 the covering codeword is named
-//     by the xor of covering ids stored beside cnt.  Only the moved
+//     by the sum of covering ids stored beside cnt.  Only the moved
 //     codeword's sphere is walked again.  pos_p = T_k - H_k[p] exactly as in
 //     covsearch2e.c:755-758.
 //   * the entering side (neg) is read off the uncovered-word list as in
@@ -25,7 +25,7 @@
 // reductions travel through distributed shared memory; the CTAs meet at
 // hardware cluster barriers, so there is no software spin-wait anywhere in
 // the engine.  Each launch is bounded by a move budget, an op-count guard and
-// a wall-clock deadline read from %globaltimer.
+// a deadline counted in SM clock cycles.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -443,7 +443,7 @@ __device__ __forceinline__ long long word_dec_v(const CovSlot &d, int ul_valid, 
 {
     uint32_t c = o & 0xffffu;
     if (c == 0) { set_error(d, COV_EDRIFT); return 0; }
-    uint32_t nw = (o - 1u) ^ ((uint32_t)i << 16);
+    uint32_t nw = o - cov_cw_unit(i);
     cov_stcg(&d.cw[w], nw);
     if (c == 1) { ul_insert(d, ul_valid, w, pk); return 1; }
     if (c == 2) private_adjust(d, (int)(nw >> 16), pk, +1);
@@ -456,7 +456,7 @@ __device__ __forceinline__ long long word_inc_v(const CovSlot &d, int i, uint32_
 {
     uint32_t c = o & 0xffffu;
     if (c == 0xffffu) { set_error(d, COV_EDRIFT); return 0; }
-    uint32_t nw = (o + 1u) ^ ((uint32_t)i << 16);
+    uint32_t nw = o + cov_cw_unit(i);
     cov_stcg(&d.cw[w], nw);
     if (c == 0) return -1;
     if (c == 1) private_adjust(d, (int)(o >> 16), pk, -1);
@@ -1328,6 +1328,12 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     for (int x = tid; x < nL * n; x += NT) negp[x] = 0;
     zero_acc(S);
     cov_bar();
+    if (tid == 0) {
+        // per-move workload counters: candidate codewords, list length, moves
+        S.prof[20] += (unsigned long long)nL;
+        S.prof[21] += S.ul_valid ? (unsigned long long)S.uln : 0ull;
+        S.prof[22] += 1;
+    }
     if (!S.ul_valid) {
         if (tid == 0) {
             apply_swaps(d, S);
@@ -1892,7 +1898,8 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
 }
 
 // ------------------------------------------------------ init kernels -------
-// cnt|xid marking of every codeword's ball (ids first..first+count-1)
+// cnt|id-sum marking of the balls of codewords first..first+count-1 (the
+// incremental form, used by greedy placement and remove-and-repair)
 __global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
 {
     const int R = d.R;
@@ -1908,9 +1915,8 @@ __global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
         const uint32_t t = (uint32_t)(g - (unsigned long long)(i - first) * per);
         const uint64_t pc = d.code[i];
         const uint32_t base = widx_pk(d, pc);
-        const uint32_t add = (sgn > 0 ? 1u : 0xffffffffu);
-        const uint32_t x = (uint32_t)i << 16;
-        if (t == 0) { atomicAdd(&d.cw[base], add); atomicXor(&d.cw[base], x); continue; }
+        const uint32_t add = sgn > 0 ? cov_cw_unit(i) : 0u - cov_cw_unit(i);
+        if (t == 0) { atomicAdd(&d.cw[base], add); continue; }
         int r = 1;
         while (t >= cum[r]) r++;
         const uint8_t *subs = d.ball_sub + (size_t)d.ball_off[r] * d.rs;
@@ -1919,9 +1925,140 @@ __global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
             uint32_t w; uint64_t pk;
             cov_item_word(d, it, kk, w, pk);
             atomicAdd(&d.cw[w], add);
-            atomicXor(&d.cw[w], x);
         }
     }
+}
+
+// Whole-state build, one CTA per tile of q^bt_nl consecutive words (the
+// words sharing their first bt_nh digits).  The tile's counters live in
+// shared memory while every codeword within distance R of the tile's prefix
+// marks its ball there -- a ball of radius R - d(prefix) on the low digits --
+// so the M*V increments of covsearch2e.c:958-967 (rebuild = M x ball_apply)
+// are shared-memory atomics, and the coverage array is written to HBM once.
+// Before leaving, the CTA counts the tile's uncovered words and adds each
+// singly covered word at distance exactly R from its coverer k to
+// P[k] = (T_k, H_k) -- the counts the reference's shared-sphere walk
+// (covsearch2e.c:592-654) produces for k.
+#define BT_MAX 24576           // words of a tile (96 KB of shared memory)
+#define BT_LCH 1024            // codewords staged per chunk
+#define BT_NT  512
+
+static inline size_t bt_smem_bytes(uint32_t tw)
+{
+    return (size_t)BT_LCH * (8 + 4 + 4) + (size_t)tw * 4;
+}
+
+__global__ void __launch_bounds__(BT_NT) k_build_state(CovSlot d, unsigned long long *zeros)
+{
+    extern __shared__ __align__(16) unsigned char bt_raw[];
+    uint64_t *lpc = (uint64_t *)bt_raw;            // [BT_LCH] packed codewords of this chunk
+    uint32_t *lid = (uint32_t *)(lpc + BT_LCH);    // [BT_LCH] their ids
+    uint32_t *lbase = lid + BT_LCH;                // [BT_LCH] their low-digit index
+    uint32_t *tile = lbase + BT_LCH;               // [bt_tw]
+    __shared__ int gcnt[COV_MAXN + 2], gpos[COV_MAXN + 2], gfill[COV_MAXN + 2];
+    constexpr int PER = BT_LCH / BT_NT;
+
+    const int q = d.q, n = d.n, R = d.R, nh = d.bt_nh, nl = d.bt_nl;
+    const uint32_t T = d.bt_tw;
+    const int rmax = min(R, nl);
+    uint64_t hp = 0;
+    {
+        uint32_t t = blockIdx.x;
+        for (int j = nh - 1; j >= 0; --j) { hp |= (uint64_t)(t % (uint32_t)q) << (4 * j); t /= (uint32_t)q; }
+    }
+    const uint64_t hmask = (1ull << (4 * nh)) - 1;   // nh <= 15
+    for (uint32_t x = threadIdx.x; x < T; x += BT_NT) tile[x] = 0;
+
+    for (int m0 = 0; m0 < d.M; m0 += BT_LCH) {
+        if (threadIdx.x < COV_MAXN + 2) gcnt[threadIdx.x] = 0;
+        __syncthreads();
+        int g[PER];
+        uint64_t pcv[PER];
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            const int k = m0 + threadIdx.x + u * BT_NT;
+            g[u] = -1;
+            pcv[u] = 0;
+            if (k < d.M) {
+                const uint64_t pc = d.code[k];
+                pcv[u] = pc;
+                const int dh = __popcll(cov_spread((pc ^ hp) & hmask));
+                if (dh <= R) {
+                    g[u] = min(R - dh, nl);
+                    atomicAdd(&gcnt[g[u]], 1);
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int r = 0; r <= rmax; r++) { gpos[r] = acc; gfill[r] = acc; acc += gcnt[r]; }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+            if (g[u] < 0) continue;
+            const int at = atomicAdd(&gfill[g[u]], 1);
+            uint32_t lb = 0;
+            for (int j = nh; j < n; j++) lb += (uint32_t)cov_nib(pcv[u], j) * d.pw[j];
+            lpc[at] = pcv[u];
+            lid[at] = (uint32_t)(m0 + threadIdx.x + u * BT_NT);
+            lbase[at] = lb;
+        }
+        __syncthreads();
+        for (int r = 0; r <= rmax; r++) {
+            const uint32_t cnt = (uint32_t)gcnt[r];
+            if (!cnt) continue;
+            const uint32_t V = d.bt_v[r];
+            const uint64_t minv = (0x100000000ull + V - 1) / V;     // ceil(2^32 / V)
+            const uint32_t total = cnt * V;
+            const int p0 = gpos[r];
+            for (uint32_t t = threadIdx.x; t < total; t += BT_NT) {
+                uint32_t kk = (uint32_t)(((uint64_t)t * minv) >> 32);   // t / V or one more
+                if (kk * V > t) kk--;
+                const uint32_t it = t - kk * V;
+                const uint64_t pc = lpc[p0 + kk];
+                uint64_t sp = d.bt_items[it];
+                int off = (int)lbase[p0 + kk];
+                while (sp) {
+                    const int j = (__ffsll((long long)sp) - 1) >> 2;
+                    const int dig = (int)((sp >> (4 * j)) & 15u) - 1;
+                    sp &= ~(15ull << (4 * j));
+                    const int cj = cov_nib(pc, j);
+                    off += (dig + (dig >= cj) - cj) * (int)d.pw[j];
+                }
+                atomicAdd(&tile[off], cov_cw_unit((int)lid[p0 + kk]));
+            }
+        }
+        __syncthreads();
+    }
+
+    uint32_t *gout = d.cw + (size_t)blockIdx.x * T;
+    unsigned long long z = 0;
+    for (uint32_t x = threadIdx.x; x < T; x += BT_NT) {
+        const uint32_t v = tile[x];
+        gout[x] = v;
+        const uint32_t c = v & 0xffffu;
+        z += c == 0;
+        if (c == 1) {
+            const int k = (int)(v >> 16);
+            uint64_t pk = hp;
+            uint32_t y = x;
+            for (int j = n - 1; j >= nh; --j) { pk |= (uint64_t)(y % (uint32_t)q) << (4 * j); y /= (uint32_t)q; }
+            uint64_t D = cov_spread(pk ^ d.code[k]);
+            if (__popcll(D) == R) {
+                int32_t *Pk = d.P + (size_t)k * (n + 1);
+                atomicAdd(&Pk[0], 1);
+                while (D) {
+                    const int j = (__ffsll((long long)D) - 1) >> 2;
+                    D &= D - 1;
+                    atomicAdd(&Pk[1 + j], 1);
+                }
+            }
+        }
+    }
+    z = warp_sum(z);
+    if ((threadIdx.x & 31) == 0 && z) atomicAdd(zeros, z);
 }
 
 __global__ void k_count_zero(const uint32_t *cw, uint32_t N, unsigned long long *out)
@@ -1931,49 +2068,6 @@ __global__ void k_count_zero(const uint32_t *cw, uint32_t N, unsigned long long 
         c += (cw[x] & 0xffffu) == 0;
     c = warp_sum(c);
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
-}
-
-// P[k] = (T_k, H_k) for every codeword from scratch; one warp per
-// (codeword, R-subset, block of 32 prefix assignments)
-__global__ void k_private_all(CovSlot d)
-{
-    const int R = d.R, n = d.n;
-    const int lane = threadIdx.x & 31;
-    const uint8_t *fs = d.ball_sub + (size_t)d.ball_off[R] * d.rs;
-    const uint32_t pp = R ? d.ppow[R - 1] : 1;
-    const uint32_t nblk = (pp + 31) / 32;
-    const unsigned long long per = (unsigned long long)(R ? d.nfsub : 1) * nblk;
-    const unsigned long long units = per * d.M;
-    const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long wstride = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long u = gw; u < units; u += wstride) {
-        const int k = (int)(u / per);
-        const uint32_t rest = (uint32_t)(u - (unsigned long long)k * per);
-        const uint64_t pc = d.code[k];
-        const uint32_t base = widx_pk(d, pc);
-        int32_t *Pk = d.P + (size_t)k * (n + 1);
-        if (R == 0) {
-            if (lane == 0 && (d.cw[base] & 0xffffu) == 1) atomicAdd(&Pk[0], 1);
-            continue;
-        }
-        const uint32_t sub = rest / nblk;
-        const uint32_t r = (rest - sub * nblk) * 32 + lane;
-        int t1 = 0;
-        if (r < pp) {
-            CovItem it = cov_item(d, fs, R, sub * pp + r, base, pc);
-            for (int kk = 0; kk < d.q - 1; kk++) {
-                uint32_t w; uint64_t pk;
-                cov_item_word(d, it, kk, w, pk);
-                t1 += (d.cw[w] & 0xffffu) == 1;
-            }
-        }
-        t1 = warp_sum(t1);
-        if (lane == 0 && t1) {
-            atomicAdd(&Pk[0], t1);
-            const uint8_t *ps = fs + (size_t)sub * d.rs;
-            for (int s2 = 0; s2 < R; s2++) atomicAdd(&Pk[1 + ps[s2]], t1);
-        }
-    }
 }
 
 // words of codeword i's ball that nothing else covers (covsearch2e.c:927-946)
@@ -2048,6 +2142,46 @@ long long binom_h(int a, int b)
     for (int i = 0; i < b; i++) r = r * (a - i) / (i + 1);
     return r;
 }
+
+// tile geometry of the state build: the most low digits whose q^nl words fit
+// a tile
+static void bt_geom(int q, int n, int *nh, int *nl)
+{
+    int l = 1;
+    while (l < n && ipow_h(q, l + 1) <= BT_MAX) l++;
+    *nl = l;
+    *nh = n - l;
+}
+
+// the ball of radius <= min(R, nl) on the low digits nh..n-1, by radius
+static std::vector<uint64_t> bt_items_h(int q, int n, int R, int nh, uint32_t *vcum)
+{
+    const int nl = n - nh, rmax = std::min(R, nl);
+    std::vector<uint64_t> out;
+    for (int r = 0; r <= rmax; r++) {
+        std::vector<int> sub(r);
+        for (int k = 0; k < r; k++) sub[k] = k;
+        while (true) {
+            std::vector<int> dig(r, 0);
+            while (true) {
+                uint64_t sp = 0;
+                for (int k = 0; k < r; k++) sp |= (uint64_t)(dig[k] + 1) << (4 * (nh + sub[k]));
+                out.push_back(sp);
+                int k = r - 1;
+                while (k >= 0 && dig[k] == q - 2) dig[k--] = 0;
+                if (k < 0) break;
+                dig[k]++;
+            }
+            int k = r - 1;
+            while (k >= 0 && sub[k] == nl - r + k) k--;
+            if (k < 0) break;
+            sub[k]++;
+            for (int m = k + 1; m < r; m++) sub[m] = sub[m - 1] + 1;
+        }
+        vcum[r] = (uint32_t)out.size();
+    }
+    return out;
+}
 int fill_subsets_h(const int *pool, int np, int R, int rs, uint8_t *out)
 {
     if (binom_h(np, R) <= 0) return 0;
@@ -2107,6 +2241,7 @@ static int ensure_attrs()
     if (g_attr_done) return 0;
     CK(cudaFuncSetAttribute(cov_run_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
     CK(cudaFuncSetAttribute(cov_run_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    CK(cudaFuncSetAttribute(k_build_state, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem_bytes(BT_MAX)));
     g_attr_done = 1;
     return 0;
 }
@@ -2274,6 +2409,12 @@ size_t cov_slot_bytes(const cov_params *prm)
     add((size_t)((N + 31) / 32) * 4);                // ul_bit
     add((size_t)M * n * 4 * 3 + (size_t)M * 4);      // g_perm, g_dval, g_neg, g_list
     add(65536);                                      // subset tables
+    {
+        int nh, nl;
+        bt_geom(q, n, &nh, &nl);
+        uint32_t vc[COV_MAXN + 2];
+        add(bt_items_h(q, n, std::min(R, n), nh, vc).size() * 8);   // state-build ball table
+    }
     add(sizeof(CovSlotState));
     if (prm->trace) add((size_t)prm->trace_cap * sizeof(cov_move_rec));
     return b;
@@ -2342,7 +2483,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     }
     cov_params p2 = *prm;
     p2.M = Mw;
-    size_t need = cov_slot_bytes(&p2) + subs.size() + subs1.size() + balls.size() + 1536;
+    size_t need = cov_slot_bytes(&p2) + subs.size() + subs1.size() + balls.size() + 2048;
     void *arena = nullptr;
     if (cudaMalloc(&arena, need) != cudaSuccess) { cudaGetLastError(); return COV_ENOMEM; }
     size_t off = 0;
@@ -2363,6 +2504,11 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     uint8_t *dball = (uint8_t *)take_(balls.size());
     uint8_t *dsub1 = (uint8_t *)take_(subs1.size());
     d.sub = dsub; d.ball_sub = dball; d.sub1 = dsub1;
+    bt_geom(q, n, &d.bt_nh, &d.bt_nl);
+    d.bt_tw = (uint32_t)ipow_h(q, d.bt_nl);
+    std::vector<uint64_t> bti = bt_items_h(q, n, R, d.bt_nh, d.bt_v);
+    uint64_t *dbt = (uint64_t *)take_(bti.size() * 8);
+    d.bt_items = dbt;
     d.st = pool->d_states + s;
     d.trace = prm->trace ? take_((size_t)prm->trace_cap * sizeof(cov_move_rec)) : nullptr;
     d.trace_cap = prm->trace ? prm->trace_cap : 0;
@@ -2374,6 +2520,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     cudaError_t e = cudaMemcpyAsync(dsub, subs.data(), subs.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dball, balls.data(), balls.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dsub1, subs1.data(), subs1.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dbt, bti.data(), bti.size() * 8, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { cudaFree(arena); return -(100 + (int)e); }
     pool->slots[s] = h;
@@ -2395,7 +2542,12 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
     for (long long i = 0; i < (long long)m * n; i++) if (code[i] >= q) return COV_EINVAL;
     cudaStream_t st = pool->cur_stream();
     if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
-    CK(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
+    {
+        int rc = ensure_attrs();
+        if (rc) return rc;
+    }
+    const bool incremental = m > M || (m < M && !random_init);   // repair or greedy
+    if (incremental) CK(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
     CK(cudaMemsetAsync(d.tabu, 0, (size_t)M * n * q * 4, st));
     CK(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
     CK(cudaMemsetAsync(d.ul_bit, 0, (size_t)((N + 31) / 32) * 4, st));
@@ -2441,7 +2593,6 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
         }
         for (int i = 0; i < M; i++) pk[i] = cur[i];
         have = M;
-        CK(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
     }
     unsigned long long *d_z = (unsigned long long *)d.g_dval;
     if (have < M && !random_init) {
@@ -2475,10 +2626,6 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
         CK(cudaStreamSynchronize(st));
         if (hs.status) return hs.status;
         for (int k = 0; k < 4; k++) rng.s[k] = hs.rng[k];
-        // cnt|xid again from the final code so the xor ids are those of M words
-        CK(cudaMemsetAsync(d.cw, 0, (size_t)N * 4, st));
-        k_mark_balls<<<grid, 256, 0, st>>>(d, 0, M, +1);
-        CK(cudaGetLastError());
     } else {
         for (int i = have; i < M; i++) {
             uint64_t v = 0;
@@ -2486,15 +2633,12 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
             pk[i] = v;
         }
         CK(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
-        k_mark_balls<<<grid, 256, 0, st>>>(d, 0, M, +1);
-        CK(cudaGetLastError());
     }
-    // uncovered count, private counts, best code
+    // coverage array, uncovered count and private counts of the final M
+    // codewords, built tile by tile; then the best code
     CK(cudaMemsetAsync(d_z, 0, 8, st));
-    k_count_zero<<<grid, 256, 0, st>>>(d.cw, d.N, d_z);
-    CK(cudaGetLastError());
     CK(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
-    k_private_all<<<grid, 256, 0, st>>>(d);
+    k_build_state<<<(unsigned)ipow_h(q, d.bt_nh), BT_NT, bt_smem_bytes(d.bt_tw), st>>>(d, d_z);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(d.best, d.code, (size_t)M * 8, cudaMemcpyDeviceToDevice, st));
     unsigned long long z = 0;

@@ -142,8 +142,9 @@ class Pool:
                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
                 "cov_pool_get_prof")
         d = {k: int(v) for k, v in zip(self.PROF_NAMES, out[:8])}
-        for k in range(8, 24):
+        for k in range(8, 20):
             d["sub%d" % k] = int(out[k])
+        d["sum_ncw"], d["sum_ul_n"], d["planned_moves"] = int(out[20]), int(out[21]), int(out[22])
         d["ul_pairs"] = int(out[24])
         return d
 
