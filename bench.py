@@ -13,6 +13,10 @@ Printed (rank 0, one JSON line):
   plain        the same search as one instance on one wide cluster, same GPU
   coverage     words/s of the uint8 distance transform and of the coverage
                count over the 7^9 words
+  hetero       256 uneven (q,n,R,M) cells, 2e4 moves each, as one graph
+               launch with autotuned cluster sizes per size class
+  served       a Poisson stream of solve requests through the continuous-
+               batching server: aggregate moves/s and p50/p99 latency
   e2e          moves/s through the public Python API with host buffers: each
                step re-seeds every restart from a pinned host code (H2D),
                builds its state, runs --moves moves and reads every best code
@@ -55,7 +59,8 @@ def _cpu_worker(args):
     idx, steps, moves, barrier = args
     sys.path.insert(0, HERE)
     from oracle.pyoracle import Oracle
-    from coldcase_gb300.workloads import uniform_code, instance_seed
+    from coldcase_gb300 import replicas
+    from coldcase_gb300.workloads import uniform_code
     seed = instance_seed(BASE_SEED, idx)
     o = Oracle(Q, N_, R_, M_, seed=seed, tabu=TENURE, threads=1)
     o.init(uniform_code(Q, N_, M_, seed))
@@ -192,12 +197,13 @@ def gpu_bench(args, rank, world, dist):
     import torch
     from coldcase_gb300 import lib as L
     from coldcase_gb300.engine import Pool, Search
-    from coldcase_gb300.workloads import uniform_code, instance_seed
+    from coldcase_gb300 import replicas
+    from coldcase_gb300.workloads import uniform_code
 
     L.load(build_if_missing=True)
     dev = torch.device("cuda", torch.cuda.current_device())
     S = args.moves
-    seeds = [instance_seed(BASE_SEED + 7919 * rank, i) for i in range(args.restarts)]
+    seeds = replicas.rank_seeds(BASE_SEED, rank, args.restarts)
     codes = [uniform_code(Q, N_, M_, sd) for sd in seeds]
 
     # ---------------- batched: device-resident state, events on its stream
@@ -237,14 +243,7 @@ def gpu_bench(args, rank, world, dist):
         raise RuntimeError("engine status %s" % errs[:4])
     ms = e_all0.elapsed_time(e_all1)
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    t = torch.tensor([ms, float(moves)], dtype=torch.float64, device=dev)
-    if dist:
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms_max, moves_all = float(tmax[0]), float(t[1])
-    else:
-        ms_max, moves_all = ms, float(moves)
+    ms_max, moves_all = replicas.combine(dist, ms, moves, device=dev)
     value = moves_all / (ms_max / 1e3)
     finished = sum(1 for s in st if s["finished"])
     best_unc = [s["best"] for s in st]
@@ -333,8 +332,53 @@ def gpu_bench(args, rank, world, dist):
             raise RuntimeError("distance transform and count disagree: %d vs %d" % (unc_dt, unc_ct))
         cov = dict(dt_words_s=Nw / (dt_ms / 1e3), dt_ms=dt_ms, count_words_s=Nw / (ct_ms / 1e3), count_ms=ct_ms,
                    dt_traffic_bytes=int(Nw * 3.25), uncovered=unc_dt)
+    # ---------------- heterogeneous cells: one tuned graph launch
+    hetero = None
+    if not args.no_hetero:
+        from coldcase_gb300 import workloads
+        from coldcase_gb300.batch import Batch, tune_batch
+        cells = replicas.shard(workloads.hetero_cells(count=args.cells * world), rank, world)
+        for c in cells:
+            c["moves"] = args.cell_moves
+        t0 = time.monotonic()
+        plan, est, classes = tune_batch(cells)
+        t_tune = time.monotonic() - t0
+        with Batch(cells, clusters=plan) as b:
+            hs = torch.cuda.Stream(device=dev)
+            b.pool.set_stream(hs.cuda_stream)
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if dist:
+                dist.barrier()
+            a0.record(hs)
+            b.run_async(graph=True)
+            a1.record(hs)
+            hs.synchronize()
+            hms = a0.elapsed_time(a1)
+            res = b.results()
+            if any(x["status"] != 0 for x in res):
+                raise RuntimeError("hetero batch: engine status")
+            hmoves = sum(x["iters"] for x in res)
+        hms_max, hmoves_all = replicas.combine(dist, hms, hmoves, device=dev)
+        hetero = dict(value=hmoves_all / (hms_max / 1e3), unit="moves/s", cells=len(cells) * world,
+                      moves_per_cell=args.cell_moves, ms=hms_max, clusters=plan, plan_estimate_s=est,
+                      tune_s=t_tune, launches="one graph: one persistent kernel per cluster size")
+
+    # ---------------- serving: Poisson arrivals, continuous batching
+    served = None
+    if not args.no_serve:
+        from coldcase_gb300 import workloads
+        from coldcase_gb300.serve import Server
+        reqs = replicas.shard(workloads.serve_requests(args.requests * world, lam=args.lam * world,
+                                                       seed=2027), rank, world)
+        with Server(max_slots=256, chunk=args.serve_chunk) as srv:
+            if dist:
+                dist.barrier()
+            rep = srv.serve(reqs)
+        served = dict(rep, lam_per_s=args.lam, unit="moves/s", value=rep["moves_per_s"])
+
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
-                plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work)
+                plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work, hetero=hetero,
+                served=served)
 
 
 def main():
@@ -356,6 +400,13 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cov", action="store_true")
+    ap.add_argument("--no-hetero", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--cells", type=int, default=256, help="heterogeneous cells per GPU")
+    ap.add_argument("--cell-moves", type=int, default=20000)
+    ap.add_argument("--requests", type=int, default=100, help="served requests per GPU")
+    ap.add_argument("--lam", type=float, default=100.0, help="request arrival rate per GPU (1/s)")
+    ap.add_argument("--serve-chunk", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -422,6 +473,10 @@ def main():
             gpu_launches=2 * args.steps,
             plain=r["plain"],
             batched_over_plain=(r["value"] / world / r["plain"]["value"]) if r["plain"] else None,
+            hetero=r["hetero"],
+            served=r["served"],
+            served_over_plain=(r["served"]["value"] / r["plain"]["value"])
+            if r["served"] and r["plain"] else None,
             coverage=r["cov"],
             finished_restarts=r["finished"],
         )

@@ -91,6 +91,9 @@ struct CovSlot {
     int tenure, kick, cand;
     long long stall;
     long long neg_cluster_pairs; // list x candidate pairs above which the cluster shares the list pass
+    int padj_warp;               // private-count events of a commit aggregated per warp
+    int list_cost;               // cost of one list entry in walked words: the entering side
+                                 // reads the list while U_n * list_cost < ncw (R+1) S
     // device arrays
     uint32_t *cw;                // [N]  cnt (bits 0-15) | sum of covering ids mod 2^16 (16-31)
     uint64_t *code;              // [M]  packed codewords
@@ -144,6 +147,7 @@ struct CovSlotState {
     // cycle counts of the leader's phases, accumulated over launches:
     // 0 pick, 1 candidates + sample, 2 entering side, 3 select, 4 move op
     // (commit + sphere), 5 finish, 6 list compaction, 7 other ops
+    long long it_limit;          // iteration count at which the slot stops (-1: none)
     unsigned long long prof[24];   // 8..19: sub-phases (diagnostics); 20: sum of candidate
                                    // codewords, 21: sum of list lengths, 22: planned moves
 };

@@ -27,6 +27,7 @@
 // the engine.  Each launch is bounded by a move budget, an op-count guard and
 // a deadline counted in SM clock cycles.
 #include <cstdio>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -49,6 +50,7 @@ namespace cg = cooperative_groups;
 #define INV_N     1024         // moduli with a reciprocal in shared memory
 #define CODE_SM   2048         // codewords mirrored in every CTA's shared memory
 #define NEG_CLUSTER_PAIRS 4096  // list x candidate pairs above which the whole cluster helps
+#define LIST_COST 5             // one uncovered-list entry costs about five walked words
 #define UL_CAP_DEFAULT (1 << 20)
 
 enum { OP_STOP = 0, OP_MOVE, OP_NEGWALK, OP_BALL, OP_RECOMPUTE, OP_ZERO_TABU, OP_REBUILD_UL, OP_NEG };
@@ -128,6 +130,9 @@ struct Smem {
     uint64_t code_sm[CODE_SM]; // leader's mirror of the packed code (M <= CODE_SM)
     uint8_t dist8[CODE_SM];    // distances to the sampled word
 };
+
+static_assert(offsetof(Smem, fy_c) == offsetof(Smem, fy_a) + 2 * PERM_CAP * sizeof(int32_t),
+              "the Fisher-Yates scratch doubles as one table during a move");
 
 // ------------------------------------------------------------ helpers -----
 __device__ __forceinline__ uint32_t widx_pk(const CovSlot &d, uint64_t pk)
@@ -404,7 +409,25 @@ __device__ void apply_swaps(const CovSlot &d, Smem &S)
 // Word w (packed pkw) just became (s=+1) or stopped being (s=-1) privately
 // covered by codeword k.  If w sits on k's distance-R sphere, T_k and H_k[j]
 // (j in D(w,c_k)) move with it.
-__device__ __forceinline__ void private_adjust(const CovSlot &d, int k, uint64_t pkw, int s)
+// During a move the adjustments collect in a per-CTA shared-memory table and
+// reach P once per touched counter at the end of the move: early in a search
+// about half of the 2 S' words of a commit cross multiplicity 1 <-> 2, and
+// their coverers are few (those within 2R of the moved codeword), so
+// adding each one to P in global memory serialises on a handful of rows.
+// The table is indexed by codeword when M (n+1) counters fit, else a small
+// open-addressing hash of rows; a row that finds no place goes to P directly.
+#define PADJ_CAP (3 * PERM_CAP)    // int32 entries: the Fisher-Yates scratch, idle during a move
+#define PADJ_PROBES 8
+struct PAdjTab {
+    int32_t *cnt;                  // rows of n+1 deltas
+    int32_t *keys;                 // hashed form: codeword of each row (-1: free)
+    int hs;                        // rows
+    int w;                         // n + 1
+    int direct;
+};
+
+__device__ __forceinline__ void private_adjust(const CovSlot &d, int k, uint64_t pkw, int s,
+                                               const PAdjTab *t = nullptr)
 {
     if (k < 0 || k >= d.M) { set_error(d, COV_EDRIFT); return; }
     extern __shared__ __align__(16) unsigned char cov_smem[];
@@ -412,13 +435,114 @@ __device__ __forceinline__ void private_adjust(const CovSlot &d, int k, uint64_t
                                        : cov_ldcg(&d.code[k]);
     uint64_t D = cov_spread(pkw ^ ck);
     if (__popcll(D) != d.R) return;
-    int32_t *Pk = d.P + (size_t)k * (d.n + 1);
+    int32_t *Pk = nullptr;
+    if (t) {
+        if (t->direct) {
+            Pk = t->cnt + k * t->w;
+        } else {
+            uint32_t h = ((uint32_t)k * 2654435761u) % (uint32_t)t->hs;
+            for (int pr = 0; pr < PADJ_PROBES; pr++) {
+                const int old = atomicCAS(&t->keys[h], -1, k);
+                if (old == -1 || old == k) { Pk = t->cnt + h * t->w; break; }
+                h = h + 1 == (uint32_t)t->hs ? 0 : h + 1;
+            }
+        }
+    }
+    if (!Pk) Pk = d.P + (size_t)k * (d.n + 1);
     atomicAdd(&Pk[0], s);
     while (D) {
         int j = (__ffsll((long long)D) - 1) >> 2;
         atomicAdd(&Pk[1 + j], s);
         D &= D - 1;
     }
+}
+
+// Warp-wide form for the commit: every lane of the warp calls it together;
+// lane events (on) whose word lies on the distance-R sphere of codeword k
+// (D = its difference set) are grouped by k, and one lane per group adds the
+// group's counts -- neighbouring words of a commit mostly share their
+// coverer, so per-lane atomics would queue on the same counters.
+__device__ __forceinline__ void warp_private_adjust_slow(const CovSlot &d, const PAdjTab &t, bool ev, int k,
+                                                      uint64_t pkw, int s)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    extern __shared__ __align__(16) unsigned char cov_smem[];
+    uint64_t D = 0;
+    bool on = false;
+    if (ev) {
+        if (k < 0 || k >= d.M) {
+            set_error(d, COV_EDRIFT);
+        } else {
+            const uint64_t ck = d.M <= CODE_SM ? reinterpret_cast<const Smem *>(cov_smem)->code_sm[k]
+                                               : cov_ldcg(&d.code[k]);
+            D = cov_spread(pkw ^ ck);
+            on = __popcll(D) == d.R;
+        }
+    }
+    const unsigned act = __ballot_sync(FULL, on);
+    if (!act) return;
+    const unsigned grp = __match_any_sync(FULL, on ? k : -1) & act;
+    if (!__any_sync(FULL, on && grp != (1u << lane))) {
+        // no two lanes share a coverer: each adds its own counts
+        if (on) {
+            int32_t *Pk = nullptr;
+            if (t.direct) {
+                Pk = t.cnt + k * t.w;
+            } else {
+                uint32_t h = ((uint32_t)k * 2654435761u) % (uint32_t)t.hs;
+                for (int pr = 0; pr < PADJ_PROBES; pr++) {
+                    const int old = atomicCAS(&t.keys[h], -1, k);
+                    if (old == -1 || old == k) { Pk = t.cnt + h * t.w; break; }
+                    h = h + 1 == (uint32_t)t.hs ? 0 : h + 1;
+                }
+                if (!Pk) Pk = d.P + (size_t)k * t.w;
+            }
+            atomicAdd(&Pk[0], s);
+            uint64_t m = D;
+            while (m) {
+                const int j = (__ffsll((long long)m) - 1) >> 2;
+                atomicAdd(&Pk[1 + j], s);
+                m &= m - 1;
+            }
+        }
+        return;
+    }
+    const bool lead = on && lane == __ffs(grp) - 1;
+    int32_t *Pk = nullptr;
+    if (lead) {
+        if (t.direct) {
+            Pk = t.cnt + k * t.w;
+        } else {
+            uint32_t h = ((uint32_t)k * 2654435761u) % (uint32_t)t.hs;
+            for (int pr = 0; pr < PADJ_PROBES; pr++) {
+                const int old = atomicCAS(&t.keys[h], -1, k);
+                if (old == -1 || old == k) { Pk = t.cnt + h * t.w; break; }
+                h = h + 1 == (uint32_t)t.hs ? 0 : h + 1;
+            }
+            if (!Pk) Pk = d.P + (size_t)k * t.w;
+        }
+        atomicAdd(&Pk[0], s * __popc(grp));
+    }
+    // positions present in any lane's difference set
+    const unsigned ulo = __reduce_or_sync(FULL, (unsigned)D);
+    const unsigned uhi = __reduce_or_sync(FULL, (unsigned)(D >> 32));
+    uint64_t U = ((uint64_t)uhi << 32) | ulo;
+    while (U) {
+        const int j = (__ffsll((long long)U) - 1) >> 2;
+        U &= U - 1;
+        const unsigned b = __ballot_sync(FULL, on && ((D >> (4 * j)) & 1ull));
+        if (lead) {
+            const int c = __popc(b & grp);
+            if (c) atomicAdd(&Pk[1 + j], s * c);
+        }
+    }
+}
+
+__device__ __forceinline__ void warp_private_adjust(const CovSlot &d, const PAdjTab &t, bool ev, int k,
+                                                    uint64_t pkw, int s)
+{
+    if (__any_sync(0xffffffffu, ev)) warp_private_adjust_slow(d, t, ev, k, pkw, s);
 }
 
 __device__ __forceinline__ void ul_insert(const CovSlot &d, int ul_valid, uint32_t x, uint64_t pk)
@@ -439,27 +563,27 @@ __device__ __forceinline__ void ul_insert(const CovSlot &d, int ul_valid, uint32
 // word w loses coverage by codeword i (leaving side of a commit / -1 ball);
 // o is the word's counter as loaded
 __device__ __forceinline__ long long word_dec_v(const CovSlot &d, int ul_valid, int i, uint32_t w,
-                                                uint64_t pk, uint32_t o)
+                                                uint64_t pk, uint32_t o, const PAdjTab *t = nullptr)
 {
     uint32_t c = o & 0xffffu;
     if (c == 0) { set_error(d, COV_EDRIFT); return 0; }
     uint32_t nw = o - cov_cw_unit(i);
     cov_stcg(&d.cw[w], nw);
     if (c == 1) { ul_insert(d, ul_valid, w, pk); return 1; }
-    if (c == 2) private_adjust(d, (int)(nw >> 16), pk, +1);
+    if (c == 2) private_adjust(d, (int)(nw >> 16), pk, +1, t);
     return 0;
 }
 
 // word w gains coverage by codeword i (entering side / +1 ball)
 __device__ __forceinline__ long long word_inc_v(const CovSlot &d, int i, uint32_t w, uint64_t pk,
-                                                uint32_t o)
+                                                uint32_t o, const PAdjTab *t = nullptr)
 {
     uint32_t c = o & 0xffffu;
     if (c == 0xffffu) { set_error(d, COV_EDRIFT); return 0; }
     uint32_t nw = o + cov_cw_unit(i);
     cov_stcg(&d.cw[w], nw);
     if (c == 0) return -1;
-    if (c == 1) private_adjust(d, (int)(o >> 16), pk, -1);
+    if (c == 1) private_adjust(d, (int)(o >> 16), pk, -1, t);
     return 0;
 }
 
@@ -516,12 +640,154 @@ __device__ __forceinline__ void group_add_h(int *partH, int key, int v, const ui
 //    Y = {w_p = c_p, d(w,c) = R-1} (in); X = Y + dv.  The counts of X and Y
 //    are not changed by the move, so they are read in the same pass.
 // The change of T_i / H_i goes to the leader's accT / accH.
-__device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank, int csize)
+// Leaving / entering pairs of a commit (covsearch2e.c:450-493): the S'
+// patterns of R positions avoiding p, q-1 values of the last one per item.
+// Per-lane form: each private-count event goes to P on its own.
+__device__ __forceinline__ void commit_pairs_lane(const CovSlot &d, const OpParams &P, Smem &S, uint32_t wid,
+                                               uint32_t wstride, int &T, long long &dunc)
+{
+    const int R = d.R, lane = threadIdx.x & 31;
+    const uint8_t *subp = d.sub + (size_t)P.mp * d.nsub * d.rs;
+    const uint32_t nit = (uint32_t)d.nsub * d.ppow[R - 1];
+    const uint32_t nstep = (nit + 31) / 32 * 32;
+    const int qm1 = d.q - 1;
+
+        // few private-count events per move: each lane adds its own to P
+    for (uint32_t t0 = wid * 32; t0 < nstep; t0 += wstride) {
+        const uint32_t t = t0 + lane;
+        int dt = 0;
+        int key = -1;
+        const uint8_t *ps = subp;
+        if (t < nit) {
+            // every word of the item is distinct: all 2(q-1) counters are
+            // loaded before any is written, so the loads are in flight together
+            CovItem it = cov_item(d, subp, R, t, P.base, P.pc);
+            key = (int)(t / d.ppow[R - 1]);
+            ps = it.ps;
+            uint32_t oa[COV_MAXQ - 1], ob[COV_MAXQ - 1];
+#pragma unroll
+            for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
+                if (kk < qm1) {
+                    uint32_t a; uint64_t pka;
+                    cov_item_word(d, it, kk, a, pka);
+                    oa[kk] = cov_ldcg(&d.cw[a]);
+                    ob[kk] = cov_ldcg(&d.cw[a + P.dv]);
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
+                if (kk < qm1) {
+                    uint32_t a; uint64_t pka;
+                    cov_item_word(d, it, kk, a, pka);
+                    dt -= (oa[kk] & 0xffffu) == 1;
+                    dt += (ob[kk] & 0xffffu) == 0;
+                    dunc += word_dec_v(d, P.ul_valid, P.mi, a, pka, oa[kk]);
+                    dunc += word_inc_v(d, P.mi, a + P.dv, cov_setnib(pka, P.mp, P.mv), ob[kk]);
+                }
+            }
+        }
+        T += dt;
+        if (t0 < nit) group_add_h(S.partH, key, dt, ps, R, -1);
+    }
+}
+
+// Warp-aggregated form: events collected into the shared table.
+__device__ __forceinline__ void commit_pairs_warp(const CovSlot &d, const OpParams &P, Smem &S, const PAdjTab &tab,
+                                               uint32_t wid, uint32_t wstride, int &T, long long &dunc)
+{
+    const int R = d.R, lane = threadIdx.x & 31;
+    const uint8_t *subp = d.sub + (size_t)P.mp * d.nsub * d.rs;
+    const uint32_t nit = (uint32_t)d.nsub * d.ppow[R - 1];
+    const uint32_t nstep = (nit + 31) / 32 * 32;
+    const int qm1 = d.q - 1;
+
+        // many events: collected per warp into the shared table
+    const uint32_t unit = cov_cw_unit(P.mi);
+    constexpr int CH = 8;
+    for (uint32_t t0 = wid * 32; t0 < nstep; t0 += wstride) {
+        const uint32_t t = t0 + lane;
+        const bool live = t < nit;
+        int dt = 0;
+        int key = -1;
+        const uint8_t *ps = subp;
+        // every word of the item is distinct: all 2(q-1) counters are
+        // loaded before any is written, so the loads are in flight together
+        CovItem it = cov_item(d, subp, R, live ? t : 0, P.base, P.pc);
+        if (live) {
+            key = (int)(t / d.ppow[R - 1]);
+            ps = it.ps;
+        }
+        // values of the last position in chunks of CH (one chunk for q <= 9)
+        for (int kb = 0; kb < qm1; kb += CH) {
+        uint32_t oa[CH], ob[CH];
+        if (live) {
+#pragma unroll
+            for (int kc = 0; kc < CH; kc++) {
+                if (kb + kc < qm1) {
+                    uint32_t a; uint64_t pka;
+                    cov_item_word(d, it, kb + kc, a, pka);
+                    oa[kc] = cov_ldcg(&d.cw[a]);
+                    ob[kc] = cov_ldcg(&d.cw[a + P.dv]);
+                }
+            }
+        }
+        // leaving word a loses codeword i, entering word a + dv gains it
+        // (the steps of word_dec_v / word_inc_v, with the private-count
+        // events handed to the warp-wide adjust)
+#pragma unroll
+        for (int kc = 0; kc < CH; kc++) {
+            if (kb + kc < qm1) {
+                bool evd = false, evi = false;
+                int kd = 0, ki = 0;
+                uint64_t pka = 0;
+                if (live) {
+                    uint32_t a;
+                    cov_item_word(d, it, kb + kc, a, pka);
+                    const uint32_t o1 = oa[kc], o2 = ob[kc];
+                    const uint32_t c1 = o1 & 0xffffu, c2 = o2 & 0xffffu;
+                    dt -= c1 == 1;
+                    dt += c2 == 0;
+                    if (c1 == 0 || c2 == 0xffffu) {
+                        set_error(d, COV_EDRIFT);
+                    } else {
+                        const uint32_t n1 = o1 - unit;
+                        cov_stcg(&d.cw[a], n1);
+                        cov_stcg(&d.cw[a + P.dv], o2 + unit);
+                        if (c1 == 1) { ul_insert(d, P.ul_valid, a, pka); dunc += 1; }
+                        else if (c1 == 2) { evd = true; kd = (int)(n1 >> 16); }
+                        if (c2 == 0) dunc -= 1;
+                        else if (c2 == 1) { evi = true; ki = (int)(o2 >> 16); }
+                    }
+                }
+                warp_private_adjust(d, tab, evd, kd, pka, +1);
+                warp_private_adjust(d, tab, evi, ki, cov_setnib(pka, P.mp, P.mv), -1);
+            }
+        }
+        }
+        T += dt;
+        if (t0 < nit) group_add_h(S.partH, key, dt, ps, R, -1);
+    }
+}
+
+template <bool WARP>
+__device__ __forceinline__ void op_move_t(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank,
+                                          int csize)
 {
     const int R = d.R, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) S.partT = 0;
     __syncwarp();
     if (threadIdx.x < COV_MAXN) S.partH[threadIdx.x] = 0;
+    PAdjTab tab;
+    tab.w = d.n + 1;
+    tab.direct = d.M * tab.w <= PADJ_CAP;
+    tab.hs = !WARP || R == 0 ? 0 : tab.direct ? d.M : PADJ_CAP / (tab.w + 1);
+    tab.keys = S.fy_a;
+    tab.cnt = tab.direct ? S.fy_a : S.fy_a + tab.hs;
+    if (WARP) {
+        const int nk = tab.direct ? 0 : tab.hs;
+        const int ne = nk + tab.hs * tab.w;
+        for (int e = threadIdx.x; e < ne; e += NT) S.fy_a[e] = e < nk ? -1 : 0;
+    }
     cov_bar();
     long long dunc = 0;
     int T = 0;
@@ -544,46 +810,9 @@ __device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, 
         }
     } else {
         // leaving / entering pairs
-        const uint8_t *subp = d.sub + (size_t)P.mp * d.nsub * d.rs;
-        const uint32_t nit = (uint32_t)d.nsub * d.ppow[R - 1];
-        const uint32_t nstep = (nit + 31) / 32 * 32;
+        if (WARP) commit_pairs_warp(d, P, S, tab, wid, wstride, T, dunc);
+        else commit_pairs_lane(d, P, S, wid, wstride, T, dunc);
         const int qm1 = d.q - 1;
-        for (uint32_t t0 = wid * 32; t0 < nstep; t0 += wstride) {
-            const uint32_t t = t0 + lane;
-            int dt = 0;
-            int key = -1;
-            const uint8_t *ps = subp;
-            if (t < nit) {
-                // every word of the item is distinct: all 2(q-1) counters are
-                // loaded before any is written, so the loads are in flight together
-                CovItem it = cov_item(d, subp, R, t, P.base, P.pc);
-                key = (int)(t / d.ppow[R - 1]);
-                ps = it.ps;
-                uint32_t oa[COV_MAXQ - 1], ob[COV_MAXQ - 1];
-#pragma unroll
-                for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
-                    if (kk < qm1) {
-                        uint32_t a; uint64_t pka;
-                        cov_item_word(d, it, kk, a, pka);
-                        oa[kk] = cov_ldcg(&d.cw[a]);
-                        ob[kk] = cov_ldcg(&d.cw[a + P.dv]);
-                    }
-                }
-#pragma unroll
-                for (int kk = 0; kk < COV_MAXQ - 1; kk++) {
-                    if (kk < qm1) {
-                        uint32_t a; uint64_t pka;
-                        cov_item_word(d, it, kk, a, pka);
-                        dt -= (oa[kk] & 0xffffu) == 1;
-                        dt += (ob[kk] & 0xffffu) == 0;
-                        dunc += word_dec_v(d, P.ul_valid, P.mi, a, pka, oa[kk]);
-                        dunc += word_inc_v(d, P.mi, a + P.dv, cov_setnib(pka, P.mp, P.mv), ob[kk]);
-                    }
-                }
-            }
-            T += dt;
-            if (t0 < nit) group_add_h(S.partH, key, dt, ps, R, -1);
-        }
         // X / Y pairs: (R-1)-subsets avoiding p
         if (R == 1) {
             if (rank == 0 && threadIdx.x == 32) {
@@ -631,6 +860,14 @@ __device__ void op_move(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, 
     cov_bar();
     if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
     if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
+    // private-count deltas of this CTA to P
+    if (WARP) for (int e = threadIdx.x; e < tab.hs * tab.w; e += NT) {
+        const int v = tab.cnt[e];
+        if (!v) continue;
+        const int row = e / tab.w;
+        const int k = tab.direct ? row : tab.keys[row];
+        atomicAdd(&d.P[(size_t)k * tab.w + (e - row * tab.w)], v);
+    }
 }
 
 // T and H of the codeword with packed digits pc at word index base: one
@@ -716,9 +953,14 @@ __device__ void op_ball(const CovSlot &d, const OpParams &P, Smem *LS, int rank,
 
 // Entering-side counts by walking, used while the uncovered list is not
 // valid: covsearch2e.c:656-683, 735-753.
+// CHUNK: the values of an item loaded together in chunks of 8 (faster; used
+// by the engine instantiation for dense-coverage slots, whose register
+// budget has room for it).
+template <bool CHUNK>
 __device__ void op_negwalk(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank,
                            int csize, cg::cluster_group &cl)
 {
+    constexpr int WCH = 8;
     const int R = d.R;
     const uint32_t *Lp = P.L_sm ? cl.map_shared_rank(S.L, 0) : d.g_list;
     int32_t *negp = P.neg_sm ? cl.map_shared_rank(S.neg, 0) : d.g_neg;
@@ -743,13 +985,36 @@ __device__ void op_negwalk(const CovSlot &d, const OpParams &P, Smem &S, Smem *L
         } else {
             const uint8_t *subp = d.sub + (size_t)p * d.nsub * d.rs;
             CovItem it = cov_item(d, subp, R, tt, b0, pc2);
-            for (int kk = 0; kk < d.q - 1; kk++) {
-                uint32_t w; uint64_t pk;
-                cov_item_word(d, it, kk, w, pk);
-                nz += (cnt_of(d, w) == 0);
+            // loads of a chunk of values in flight together
+            const int qm1 = d.q - 1;
+            if (!CHUNK) {
+                for (int kk = 0; kk < qm1; kk++) {
+                    uint32_t w; uint64_t pk;
+                    cov_item_word(d, it, kk, w, pk);
+                    nz += (cnt_of(d, w) == 0);
+                }
+            } else for (int kb = 0; kb < qm1; kb += WCH) {
+                uint32_t cv[WCH];
+#pragma unroll
+                for (int kc = 0; kc < WCH; kc++) {
+                    if (kb + kc < qm1) {
+                        uint32_t w; uint64_t pk;
+                        cov_item_word(d, it, kb + kc, w, pk);
+                        cv[kc] = cov_ldcg(&d.cw[w]);
+                    }
+                }
+#pragma unroll
+                for (int kc = 0; kc < WCH; kc++)
+                    if (kb + kc < qm1) nz += (cv[kc] & 0xffffu) == 0;
             }
         }
-        if (nz) atomicAdd(&negp[l * d.n + p], nz);
+        // lanes of a warp mostly walk the same (codeword, position): one
+        // atomic per group
+        const unsigned am = __activemask();
+        const int key = l * d.n + p;
+        const unsigned grp = __match_any_sync(am, key);
+        const int sum = __reduce_add_sync(grp, nz);
+        if ((threadIdx.x & 31) == __ffs(grp) - 1 && sum) atomicAdd(&negp[key], sum);
     }
 }
 
@@ -1334,7 +1599,14 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         S.prof[21] += S.ul_valid ? (unsigned long long)S.uln : 0ull;
         S.prof[22] += 1;
     }
-    if (!S.ul_valid) {
+    // The list and the walk give the same counts (covsearch2e.c:720-753);
+    // the reference picks the list while U_n n < (R+1) S' (:1466-1467).  Here
+    // the list costs per entry whatever the number of candidates (one mask
+    // test for up to 64), the walk per candidate: list while
+    // U_n * list_cost < ncw (R+1) S'.
+    const bool use_list = S.ul_valid &&
+        (long long)S.uln * d.list_cost < (long long)nL * (R + 1) * (long long)d.nsub * (long long)d.ppow[R];
+    if (!use_list) {
         if (tid == 0) {
             apply_swaps(d, S);
             OpParams &o = S.opp;
@@ -1793,6 +2065,10 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
 }
 
 // ------------------------------------------------------------- kernel -----
+// One instantiation per private-count upkeep form (per-lane or warp-
+// aggregated commit), so that each is register-allocated on its own; a slot
+// runs in the one its adjust mode names.
+template <bool WARP>
 __global__ void __launch_bounds__(NT, 1)
 cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluster_slot, int mode,
                unsigned long long budget_ns, long long op_guard)
@@ -1854,10 +2130,10 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         if (op == OP_STOP) break;
         const long long top = cov_clock();
         if (op == OP_MOVE) {
-            op_move(d, P, S, LS, rank, csize);
+            op_move_t<WARP>(d, P, S, LS, rank, csize);
             if (d.M <= CODE_SM && threadIdx.x == 0) S.code_sm[P.mi] = P.pcn;
         } else if (op == OP_NEGWALK) {
-            op_negwalk(d, P, S, LS, rank, csize, cl);
+            op_negwalk<WARP>(d, P, S, LS, rank, csize, cl);
         } else if (op == OP_NEG) {
             op_neg(d, P, S, LS, rank, csize);
         } else if (op == OP_BALL) {
@@ -2115,7 +2391,9 @@ __global__ void k_set_budget(CovSlotState *states, const int *map, int nslots, l
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < nslots) {
         CovSlotState &s = states[map[k]];
-        s.moves_left = moves;
+        long long m = moves;
+        if (s.it_limit >= 0) m = min(m, max(0ll, s.it_limit - s.it));
+        s.moves_left = m;
         s.target = target;
     }
 }
@@ -2141,6 +2419,20 @@ long long binom_h(int a, int b)
     long long r = 1;
     for (int i = 0; i < b; i++) r = r * (a - i) / (i + 1);
     return r;
+}
+
+// Private-count events of a commit (words crossing multiplicity 1 <-> 2):
+// with mean coverage lambda = M |B| / q^n -- fixed for an instance, the sum
+// of all counts being M |B| -- about 2 S' lambda e^-lambda (1 + lambda/2)
+// per move.  From ~8k per move the warp-aggregated form is the faster one.
+static int padj_auto(int q, int n, int R, int M)
+{
+    if (R < 1 || R >= n) return 0;
+    double V = 0;
+    for (int r = 0; r <= R; r++) V += (double)binom_h(n, r) * (double)ipow_h(q - 1, r);
+    const double lam = (double)M * V / (double)ipow_h(q, n);
+    const double Sp = (double)binom_h(n - 1, R) * (double)ipow_h(q - 1, R);
+    return 2.0 * Sp * lam * std::exp(-lam) * (1.0 + lam / 2.0) >= 8192.0;
 }
 
 // tile geometry of the state build: the most low digits whose q^nl words fit
@@ -2228,9 +2520,17 @@ struct cov_pool {
     double budget_s = 30.0;
     long long launch_moves = 0;      // move budget of the current launch
     long long neg_cluster_pairs = NEG_CLUSTER_PAIRS;
+    int list_cost = LIST_COST;
     cudaGraphExec_t gexec = nullptr; // captured multi-step run
     long long g_moves = -1, g_target = -2;
     int g_steps = 0;
+    // slots grouped by cluster size: d_all holds the groups one after the
+    // other; every group after the first runs on its own stream, forked from
+    // and joined back to the current stream
+    struct Group { int csize, warp, off, count; };
+    std::vector<Group> groups;
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> ev;      // ev[0] fork, ev[1 + g] join of group g
     cudaStream_t cur_stream() const { return use_ext ? ext : stream; }
 };
 
@@ -2239,23 +2539,25 @@ static int g_attr_done = 0;
 static int ensure_attrs()
 {
     if (g_attr_done) return 0;
-    CK(cudaFuncSetAttribute(cov_run_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
-    CK(cudaFuncSetAttribute(cov_run_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    CK(cudaFuncSetAttribute(cov_run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
+    CK(cudaFuncSetAttribute(cov_run_kernel<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    CK(cudaFuncSetAttribute(cov_run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
+    CK(cudaFuncSetAttribute(cov_run_kernel<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     CK(cudaFuncSetAttribute(k_build_state, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem_bytes(BT_MAX)));
     g_attr_done = 1;
     return 0;
 }
 
 // one cluster per listed slot; d_list holds `count` slot indices on the device
-static int launch_kernel(cov_pool *pool, const int *d_list, int count, int csize, int mode,
-                         long long moves)
+static int launch_kernel(cov_pool *pool, const int *d_list, int count, int csize, int warp, int mode,
+                         long long moves, cudaStream_t stream)
 {
     if (count <= 0) return 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(count * csize));
     cfg.blockDim = dim3(NT);
     cfg.dynamicSmemBytes = sizeof(Smem);
-    cfg.stream = pool->cur_stream();
+    cfg.stream = stream;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = (unsigned)csize;
@@ -2273,7 +2575,8 @@ static int launch_kernel(cov_pool *pool, const int *d_list, int count, int csize
         mmax = std::max<long long>(mmax, pool->slots[s].d.M);
     }
     long long guard = mode == MODE_GREEDY ? 4 * mmax + 4096 : moves * (6 + 3LL * kmax) + 4096;
-    CK(cudaLaunchKernelEx(&cfg, cov_run_kernel, (const CovSlot *)pool->d_slots, d_list, mode, budget_ns,
+    CK(cudaLaunchKernelEx(&cfg, warp ? cov_run_kernel<true> : cov_run_kernel<false>,
+                          (const CovSlot *)pool->d_slots, d_list, mode, budget_ns,
                           guard));
     CK(cudaGetLastError());
     return 0;
@@ -2286,7 +2589,10 @@ static int launch_run(cov_pool *pool, const std::vector<int> &active, int csize,
     CK(cudaMemcpyAsync(pool->d_map, active.data(), sizeof(int) * active.size(), cudaMemcpyHostToDevice,
                        pool->cur_stream()));
     CK(cudaStreamSynchronize(pool->cur_stream()));
-    return launch_kernel(pool, pool->d_map, (int)active.size(), csize, mode, pool->launch_moves);
+    int warp = 0;
+    for (int s : active) warp |= pool->slots[s].d.padj_warp;
+    return launch_kernel(pool, pool->d_map, (int)active.size(), csize, warp, mode, pool->launch_moves,
+                         pool->cur_stream());
 }
 
 // device list of every used slot, refreshed after add/remove
@@ -2294,23 +2600,58 @@ static int refresh_all(cov_pool *pool)
 {
     if (!pool->all_dirty) return 0;
     std::vector<int> all;
-    for (int s = 0; s < pool->max_slots; s++) if (pool->slots[s].used) all.push_back(s);
+    pool->groups.clear();
+    for (int c = 1; c <= 16; c++) {
+        for (int w = 0; w < 2; w++) {
+            const int off = (int)all.size();
+            for (int s = 0; s < pool->max_slots; s++)
+                if (pool->slots[s].used && pool->slots[s].cluster == c && pool->slots[s].d.padj_warp == w)
+                    all.push_back(s);
+            if ((int)all.size() > off) pool->groups.push_back({c, w, off, (int)all.size() - off});
+        }
+    }
     if (!all.empty())
         CK(cudaMemcpy(pool->d_all, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice));
+    while (pool->aux.size() + 1 < pool->groups.size()) {
+        cudaStream_t a;
+        CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+        pool->aux.push_back(a);
+    }
+    while (pool->ev.size() < pool->groups.size() + 1) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        pool->ev.push_back(e);
+    }
     pool->n_all = (int)all.size();
     pool->all_dirty = false;
     if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
     return 0;
 }
 
-// budget + run for every used slot, enqueued on the current stream
+// budget + run for every used slot, enqueued on the current stream (groups
+// of other cluster sizes on forked streams that join back into it)
 static int enqueue_step(cov_pool *pool, long long moves, long long target)
 {
     if (pool->n_all == 0) return 0;
-    k_set_budget<<<(pool->n_all + 127) / 128, 128, 0, pool->cur_stream()>>>(pool->d_states, pool->d_all,
-                                                                          pool->n_all, moves, target);
+    cudaStream_t st = pool->cur_stream();
+    k_set_budget<<<(pool->n_all + 127) / 128, 128, 0, st>>>(pool->d_states, pool->d_all, pool->n_all, moves,
+                                                            target);
     CK(cudaGetLastError());
-    return launch_kernel(pool, pool->d_all, pool->n_all, pool->cluster, MODE_SEARCH, moves);
+    const int ng = (int)pool->groups.size();
+    if (ng > 1) CK(cudaEventRecord(pool->ev[0], st));
+    for (int g = 1; g < ng; g++) {
+        const cov_pool::Group &G = pool->groups[g];
+        cudaStream_t a = pool->aux[g - 1];
+        CK(cudaStreamWaitEvent(a, pool->ev[0], 0));
+        int rc = launch_kernel(pool, pool->d_all + G.off, G.count, G.csize, G.warp, MODE_SEARCH, moves, a);
+        if (rc) return rc;
+        CK(cudaEventRecord(pool->ev[1 + g], a));
+    }
+    const cov_pool::Group &G0 = pool->groups[0];
+    int rc = launch_kernel(pool, pool->d_all + G0.off, G0.count, G0.csize, G0.warp, MODE_SEARCH, moves, st);
+    if (rc) return rc;
+    for (int g = 1; g < ng; g++) CK(cudaStreamWaitEvent(st, pool->ev[1 + g], 0));
+    return 0;
 }
 
 static int push_slot(cov_pool *pool, int s)
@@ -2387,6 +2728,8 @@ int cov_pool_destroy(cov_pool *pool)
         if (pool->slots[s].used) cudaFree(pool->slots[s].arena);
     if (pool->gexec) cudaGraphExecDestroy(pool->gexec);
     cudaFree(pool->d_slots); cudaFree(pool->d_map); cudaFree(pool->d_all); cudaFree(pool->d_states);
+    for (cudaStream_t a : pool->aux) cudaStreamDestroy(a);
+    for (cudaEvent_t e : pool->ev) cudaEventDestroy(e);
     cudaStreamDestroy(pool->stream);
     delete pool;
     return COV_OK;
@@ -2452,6 +2795,8 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.tenure = prm->tabu; d.kick = prm->kick; d.cand = prm->cand; d.stall = prm->stall;
     d.ul_cap = UL_CAP_DEFAULT;
     d.neg_cluster_pairs = pool->neg_cluster_pairs;
+    d.list_cost = pool->list_cost;
+    d.padj_warp = padj_auto(q, n, R, M);
     std::vector<uint8_t> subs((size_t)n * std::max(d.nsub, 1) * d.rs, 0);
     for (int p = 0; p < n; p++) {
         int pool_[32], np = 0;
@@ -2649,6 +2994,7 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
     hs.unc = (long long)z;
     hs.best_unc = hs.unc;
     hs.target = -1;
+    hs.it_limit = -1;
     hs.ul_valid = 0;
     hs.finished = hs.unc == 0;
     CK(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
@@ -2749,7 +3095,10 @@ int cov_pool_graph_run(cov_pool *pool, int64_t moves, int64_t target, int32_t st
 
 // Tuning knobs (applied to every slot, present and future):
 //   "neg_cluster_pairs"  list x candidate pairs from which the whole cluster
-//                        shares the uncovered-list pass (default 32768)
+//                        shares the uncovered-list pass (default 4096)
+//   "list_cost"          cost of one uncovered-list entry in walked words
+//                        (default 5): the entering side reads the list while
+//                        U_n * list_cost < ncw (R+1) S', else walks
 int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value)
 {
     if (!pool || !name) return COV_EINVAL;
@@ -2764,6 +3113,84 @@ int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value)
         }
         CK(cudaStreamSynchronize(pool->cur_stream()));
         if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        return COV_OK;
+    }
+    if (!strcmp(name, "list_cost")) {
+        if (value < 0 || value > 1000000) return COV_EINVAL;
+        pool->list_cost = (int)value;
+        for (int s = 0; s < pool->max_slots; s++) {
+            if (!pool->slots[s].used) continue;
+            pool->slots[s].d.list_cost = (int)value;
+            int rc = push_slot(pool, s);
+            if (rc) return rc;
+        }
+        CK(cudaStreamSynchronize(pool->cur_stream()));
+        if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        return COV_OK;
+    }
+    return COV_EINVAL;
+}
+
+// Free and total device memory of the current device (cudaMemGetInfo): what
+// admission of new instances is measured against.
+int cov_device_memory(int64_t *free_bytes, int64_t *total_bytes)
+{
+    if (!free_bytes || !total_bytes) return COV_EINVAL;
+    size_t f = 0, t = 0;
+    CK(cudaMemGetInfo(&f, &t));
+    *free_bytes = (int64_t)f;
+    *total_bytes = (int64_t)t;
+    return COV_OK;
+}
+
+// Per-slot settings:
+//   "cluster"            CTAs that advance this slot (1..16); slots of each
+//                        cluster size run as one launch, the launches of a
+//                        step side by side
+//   "neg_cluster_pairs", "list_cost"  as for cov_pool_set_param, this slot only
+//   "adjust_mode"        private-count upkeep during a commit: 0 per lane,
+//                        1 aggregated per warp, -1 chosen from the expected
+//                        number of events (the default)
+//   "it_limit"           iteration count at which the slot stops (-1: none);
+//                        each run advances it by at most the remainder
+int cov_pool_set_slot_param(cov_pool *pool, int32_t slot, const char *name, int64_t value)
+{
+    if (!pool || !name || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    HostSlot &h = pool->slots[slot];
+    if (!strcmp(name, "cluster")) {
+        if (value < 1 || value > 16) return COV_EINVAL;
+        if (h.cluster != (int)value) {
+            h.cluster = (int)value;
+            pool->all_dirty = true;
+        }
+        return COV_OK;
+    }
+    if (!strcmp(name, "neg_cluster_pairs") || !strcmp(name, "list_cost")) {
+        if (value < 0 || (name[0] == 'l' && value > 1000000)) return COV_EINVAL;
+        if (name[0] == 'n') h.d.neg_cluster_pairs = value;
+        else h.d.list_cost = (int)value;
+        int rc = push_slot(pool, slot);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(pool->cur_stream()));
+        if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        return COV_OK;
+    }
+    if (!strcmp(name, "adjust_mode")) {
+        // 0: per-lane private-count updates, 1: warp-aggregated, -1: by estimate
+        if (value < -1 || value > 1) return COV_EINVAL;
+        h.d.padj_warp = value < 0 ? padj_auto(h.d.q, h.d.n, h.d.R, h.d.M) : (int)value;
+        pool->all_dirty = true;
+        int rc = push_slot(pool, slot);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(pool->cur_stream()));
+        if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        return COV_OK;
+    }
+    if (!strcmp(name, "it_limit")) {
+        if (value < -1) return COV_EINVAL;
+        long long v = value;
+        CK(cudaMemcpyAsync(&h.st->it_limit, &v, sizeof v, cudaMemcpyHostToDevice, pool->cur_stream()));
+        CK(cudaStreamSynchronize(pool->cur_stream()));
         return COV_OK;
     }
     return COV_EINVAL;

@@ -25,6 +25,14 @@ def slot_bytes(q, n, R, M, **kw):
     return int(lib.cov_slot_bytes(ctypes.byref(p)))
 
 
+def device_memory():
+    """(free, total) bytes of the current device."""
+    lib = L.load()
+    f, t = ctypes.c_int64(), ctypes.c_int64()
+    L.check(lib.cov_device_memory(ctypes.byref(f), ctypes.byref(t)), "cov_device_memory")
+    return f.value, t.value
+
+
 class Pool:
     """Up to `max_slots` independent searches, one thread-block cluster of
     `cluster` CTAs each, advanced together by run()."""
@@ -40,6 +48,11 @@ class Pool:
 
     def set_param(self, name, value):
         L.check(self.lib.cov_pool_set_param(self.h, name.encode(), int(value)), "cov_pool_set_param")
+
+    def set_slot_param(self, slot, name, value):
+        """Per-slot setting: "cluster", "neg_cluster_pairs" or "it_limit"."""
+        L.check(self.lib.cov_pool_set_slot_param(self.h, int(slot), name.encode(), int(value)),
+                "cov_pool_set_slot_param")
 
     def add(self, q, n, R, M, code=None, random_init=False, seed=12345, tabu=0, kick=2,
             stall=5000, cand=100000, trace=0, trace_cap=0):

@@ -70,7 +70,9 @@ SIGNATURES = {
     "cov_pool_create": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_P)]),
     "cov_pool_set_budget": (ctypes.c_int, [_P, ctypes.c_double]),
     "cov_pool_set_param": (ctypes.c_int, [_P, ctypes.c_char_p, _I64]),
+    "cov_pool_set_slot_param": (ctypes.c_int, [_P, _I32, ctypes.c_char_p, _I64]),
     "cov_slot_bytes": (ctypes.c_size_t, [ctypes.POINTER(CovParams)]),
+    "cov_device_memory": (ctypes.c_int, [_PI64, _PI64]),
     "cov_pool_add": (ctypes.c_int, [_P, ctypes.POINTER(CovParams), _PU8, _I32, _I32, _PI32]),
     "cov_pool_load": (ctypes.c_int, [_P, _I32, ctypes.c_uint64, _PU8, _I32, _I32]),
     "cov_pool_run": (ctypes.c_int, [_P, _I64, _I64]),

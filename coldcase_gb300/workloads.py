@@ -45,3 +45,27 @@ def hetero_cells(count=256, seed=2026, max_words=43_000_000, max_m=65535):
             continue
         out.append(dict(q=q, n=n, R=R, M=M, seed=instance_seed(seed, len(out))))
     return out
+
+
+def serve_requests(count=200, lam=100.0, seed=2027, max_words=60_500_000, max_m=65535):
+    """Open-loop Poisson stream of solve requests: q in {5,6,7}, n in
+    {6..10} with q^n <= 6.05e7, R in {1..4}, M = ceil(1.3 q^n / |B(n,R)|)
+    (redrawn above 65535), move budget log-uniform in [1e3, 1e5], arrivals
+    with exponential gaps of mean 1/lam seconds."""
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    while len(out) < count:
+        q = int(rng.integers(5, 8))
+        n = int(rng.integers(6, 11))
+        R = int(rng.integers(1, 5))
+        if q ** n > max_words:
+            continue
+        M = math.ceil(1.3 * q ** n / ball_volume(q, n, R))
+        if M > max_m:
+            continue
+        moves = int(round(10 ** rng.uniform(3, 5)))
+        t += float(rng.exponential(1.0 / lam))
+        out.append(dict(id=len(out), q=q, n=n, R=R, M=M, seed=instance_seed(seed, len(out)), moves=moves,
+                        arrival=t))
+    return out

@@ -95,9 +95,25 @@ typedef struct {
  * GPU entry; cov_pool_* generalises it to uneven instances. */
 int cov_pool_create(int32_t max_slots, int32_t cluster, cov_pool **out);
 int cov_pool_set_budget(cov_pool *pool, double seconds);   /* per-launch wall limit */
-/* Tuning knob by name ("neg_cluster_pairs": list x candidate pairs from
- * which the whole cluster shares the uncovered-list pass). */
+/* Tuning knob by name: "neg_cluster_pairs" (list x candidate pairs from
+ * which the whole cluster shares the uncovered-list pass), "list_cost"
+ * (weight of one uncovered-list entry against one walked word when the
+ * entering side chooses between them, covsearch2e.c:1466-1467).  Neither
+ * changes a trajectory. */
 int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value);
+/* Per-slot setting by name: "cluster" (CTAs per instance, 1..16; slots of
+ * each cluster size run as one launch, the launches of a step side by side),
+ * "neg_cluster_pairs" and "list_cost" (this slot only), "adjust_mode"
+ * (private-count upkeep of a commit: 0 per thread, 1 aggregated per warp,
+ * -1 chosen from the expected event count), "it_limit" (iteration count at which
+ * the slot stops; -1 none).  chain_run (cov/gemm2/chainsolve.cu:370-375)
+ * takes one iteration budget for all chains; covengine gives each chain its
+ * own time budget (cov/engine/covengine:624-643). */
+int cov_pool_set_slot_param(cov_pool *pool, int32_t slot, const char *name, int64_t value);
+/* Free and total bytes of the current device (cudaMemGetInfo), for
+ * admitting instances by free HBM.  No counterpart in the reference, whose
+ * solvers run as CPU processes. */
+int cov_device_memory(int64_t *free_bytes, int64_t *total_bytes);
 /* Device bytes one slot with these parameters occupies (0 = invalid). */
 size_t cov_slot_bytes(const cov_params *prm);
 /* Add an instance and build its initial state from `m` codewords

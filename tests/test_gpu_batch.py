@@ -1,0 +1,128 @@
+"""Batched uneven instances and serving, against the oracle.
+
+Every instance of a batch (one pool, slots of several cluster sizes, each
+slot stopped by its own move budget) must follow exactly the trajectory the
+oracle follows for that instance alone: same move records, best code and
+counts.  A served request must give the same answer alone and in a mix.
+"""
+import numpy as np
+import pytest
+
+from coldcase_gb300.batch import Batch, size_class
+from coldcase_gb300.engine import Pool
+from coldcase_gb300.serve import Server
+from coldcase_gb300.workloads import uniform_code
+
+pytestmark = pytest.mark.gpu
+
+CELLS = [  # q, n, R, M, moves, tabu
+    (4, 6, 1, 420, 300, 10),
+    (5, 6, 2, 90, 700, 0),
+    (6, 6, 3, 18, 900, 0),
+    (3, 8, 2, 60, 500, 3),
+    (5, 7, 3, 40, 1200, 0),
+    (7, 6, 2, 300, 450, 5),
+    (4, 8, 3, 30, 800, 0),
+    (6, 7, 1, 7000, 250, 0),
+]
+
+
+def oracle_of(q, n, R, M, moves, tabu, seed):
+    from oracle.pyoracle import Oracle
+    o = Oracle(q, n, R, M, seed=seed, tabu=tabu)
+    o.init(uniform_code(q, n, M, seed))
+    tr = o.run(moves, trace=True)
+    return o, tr
+
+
+def specs():
+    return [dict(q=q, n=n, R=R, M=M, moves=mv, tabu=tb, seed=1000 + i)
+            for i, (q, n, R, M, mv, tb) in enumerate(CELLS)]
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_mixed_clusters_bit_exact(covlib, graph):
+    sp = specs()
+    keys = sorted({size_class(s["q"], s["n"], s["R"], s["M"]) for s in sp})
+    clusters = {k: [1, 2, 4, 8][i % 4] for i, k in enumerate(keys)}
+    with Batch(sp, clusters=clusters) as b:
+        assert len(set(b.cluster_of)) > 1
+        b.run(graph=graph)
+        res = b.results()
+        for i, s in enumerate(sp):
+            o, tr = oracle_of(s["q"], s["n"], s["R"], s["M"], s["moves"], s["tabu"], s["seed"])
+            assert res[i]["status"] == 0
+            assert res[i]["iters"] == o.iters(), (s, res[i])
+            assert res[i]["uncovered"] == o.best_uncovered(), (s, res[i])
+            assert res[i]["kicks"] == o.kicks()
+            assert (b.best(i) == o.best()).all(), s
+
+
+def test_iteration_limit_across_chunks(covlib):
+    """it_limit stops a slot at exactly its budget however the runs are cut."""
+    q, n, R, M, moves, tabu = 5, 7, 3, 40, 1000, 0
+    seed = 77
+    o, otr = oracle_of(q, n, R, M, moves, tabu, seed)
+    pool = Pool(2, cluster=2)
+    a = pool.add(q, n, R, M, code=uniform_code(q, n, M, seed), seed=seed, tabu=tabu, trace=1, trace_cap=2000)
+    b = pool.add(q, n, R, M, code=uniform_code(q, n, M, seed), seed=seed, tabu=tabu, trace=1, trace_cap=2000)
+    pool.set_slot_param(a, "it_limit", moves)
+    pool.set_slot_param(b, "cluster", 1)
+    pool.set_slot_param(b, "it_limit", moves)
+    for k in (37, 400, 1, 999, 5000):
+        pool.run(k)
+    for s in (a, b):
+        assert pool.status(s)["it"] == min(moves, o.iters())
+        assert pool.trace(s).tobytes() == otr.tobytes()
+    pool.set_slot_param(a, "it_limit", -1)
+    pool.run(10)
+    assert pool.status(a)["it"] == pool.status(b)["it"] + 10 or pool.status(a)["finished"]
+    pool.close()
+
+
+def _requests():
+    out = []
+    for i, (q, n, R, M, mv, tb) in enumerate(CELLS):
+        out.append(dict(id=i, q=q, n=n, R=R, M=M, moves=mv, tabu=tb, seed=500 + i, arrival=0.002 * i))
+    return out
+
+
+def test_served_result_same_alone_and_in_mix(covlib):
+    """Bit-identical answers alone and under continuous batching (tolerance:
+    none -- the codes, counts and iteration numbers are equal)."""
+    reqs = _requests()
+    mix = {}
+    with Server(max_slots=4, chunk=97) as srv:
+        rep = srv.serve(reqs)
+        assert rep["requests"] == len(reqs)
+        for r in srv.done:
+            mix[r["id"]] = (r["result"], r["best"])
+    for r in reqs[::3]:
+        with Server(max_slots=1, chunk=1000) as alone:
+            alone.serve([dict(r, arrival=0.0)])
+            a = alone.done[0]
+        res, best = mix[r["id"]]
+        assert a["result"] == res, (r, a["result"], res)
+        assert (a["best"] == best).all()
+        o, _ = oracle_of(r["q"], r["n"], r["R"], r["M"], r["moves"], r["tabu"], r["seed"])
+        assert res["uncovered"] == o.best_uncovered() and res["iters"] == o.iters()
+
+
+def test_admission_by_device_bytes(covlib):
+    """With a byte budget for two requests, at most two are resident."""
+    reqs = _requests()[:6]
+    from coldcase_gb300.engine import slot_bytes
+    sizes = [slot_bytes(r["q"], r["n"], r["R"], r["M"]) for r in reqs]
+    budget = sorted(sizes)[-1] + sorted(sizes)[-2]
+    peak = []
+    with Server(max_slots=8, chunk=64, budget_bytes=budget) as srv:
+        orig = srv.step
+
+        def step():
+            peak.append((len(srv.active), srv.resident))
+            return orig()
+        srv.step = step
+        rep = srv.serve(reqs)
+    assert rep["requests"] == len(reqs)
+    assert max(p[1] for p in peak) <= budget
+    assert max(p[0] for p in peak) >= 2
