@@ -59,8 +59,7 @@ def _cpu_worker(args):
     idx, steps, moves, barrier = args
     sys.path.insert(0, HERE)
     from oracle.pyoracle import Oracle
-    from coldcase_gb300 import replicas
-    from coldcase_gb300.workloads import uniform_code
+    from coldcase_gb300.workloads import instance_seed, uniform_code
     seed = instance_seed(BASE_SEED, idx)
     o = Oracle(Q, N_, R_, M_, seed=seed, tabu=TENURE, threads=1)
     o.init(uniform_code(Q, N_, M_, seed))
@@ -257,6 +256,7 @@ def gpu_bench(args, rank, world, dist):
     if not args.no_e2e:
         pinned = [torch.from_numpy(c).pin_memory() for c in codes]
         e_moves, e_t = 0, 0.0
+        t_load = t_run = t_read = 0.0
         h2d = sum(int(c.numel()) for c in pinned)
         d2h = args.restarts * M_ * N_
         for k in range(args.e2e_steps):
@@ -264,16 +264,24 @@ def gpu_bench(args, rank, world, dist):
             t0 = time.monotonic()
             for i, sl in enumerate(slots):
                 pool.load(sl, code=pinned[i].numpy(), seed=seeds[i] + 1 + k)
+            t1 = time.monotonic()
             pool.run(S)
+            t2 = time.monotonic()
             stt = pool.status_all(args.restarts)
             for sl in slots:
                 pool.best(sl)
-            e_t += time.monotonic() - t0
+            t3 = time.monotonic()
+            e_t += t3 - t0
+            t_load += t1 - t0
+            t_run += t2 - t1
+            t_read += t3 - t2
             e_moves += sum(s["it"] for s in stt)
         e2e = dict(value=e_moves / e_t, unit="moves/s", h2d_bytes_per_step=h2d,
                    d2h_bytes_per_step=d2h + args.restarts * 72,
                    note="per step: %d restarts re-seeded from pinned host codes (state build included), "
-                        "%d moves each, every best code read back" % (args.restarts, S))
+                        "%d moves each from the fresh codes, every best code read back" % (args.restarts, S),
+                   ms_per_step=dict(load=1e3 * t_load / args.e2e_steps, run=1e3 * t_run / args.e2e_steps,
+                                    read=1e3 * t_read / args.e2e_steps))
     pool.close()
 
     # ---------------- plain: one instance, one wide cluster, same GPU
@@ -368,13 +376,16 @@ def gpu_bench(args, rank, world, dist):
     if not args.no_serve:
         from coldcase_gb300 import workloads
         from coldcase_gb300.serve import Server
+        from coldcase_gb300.batch import tune_batch
         reqs = replicas.shard(workloads.serve_requests(args.requests * world, lam=args.lam * world,
                                                        seed=2027), rank, world)
-        with Server(max_slots=256, chunk=args.serve_chunk) as srv:
+        splan, _, _ = tune_batch(reqs)
+        with Server(max_slots=256, chunk=args.serve_chunk, clusters=splan) as srv:
             if dist:
                 dist.barrier()
             rep = srv.serve(reqs)
-        served = dict(rep, lam_per_s=args.lam, unit="moves/s", value=rep["moves_per_s"])
+        served = dict(rep, lam_per_s=args.lam, unit="moves/s", value=rep["moves_per_s"], clusters=splan,
+                      elastic=True)
 
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
                 plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work, hetero=hetero,

@@ -1139,10 +1139,9 @@ __device__ void neg_chunks(const CovSlot &d, Smem &S, uint64_t pu, int nL, uint3
         const int cnt = (int)min((uint32_t)ULS, e1 - c0);
         for (int k = threadIdx.x; k < cnt; k += NT) {
             const uint32_t e = c0 + (uint32_t)k;
-            const uint32_t x = cov_ldcg(&d.ul_idx[e]);
             const uint64_t px = cov_ldcg(&d.ul_pk[e]);
             uint64_t hit = 0;
-            if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) {          // not a stale entry
+            {
                 uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0;
                 for (int j = 0; j < n; j++) {
                     const uint64_t m = S.cmask[j * q + cov_nib(px, j)];
@@ -1160,6 +1159,13 @@ __device__ void neg_chunks(const CovSlot &d, Smem &S, uint64_t pu, int nL, uint3
             for (uint64_t m = eq; m; m &= m - 1) E |= 1u << ((__ffsll((long long)m) - 1) >> 2);
             S.st_H[k] = hit;
             S.st_E[k] = (uint16_t)E;
+        }
+        cov_bar();
+        // entries some candidate hits: drop the stale ones (word covered
+        // again) -- the count is read for these few entries only
+        for (int k = threadIdx.x; k < cnt; k += NT) {
+            if (S.st_H[k] && (cov_ldcg(&d.cw[cov_ldcg(&d.ul_idx[c0 + (uint32_t)k])]) & 0xffffu) != 0)
+                S.st_H[k] = 0;
         }
         cov_bar();
         for (int l = warp; l < nL; l += NWARP) {

@@ -18,7 +18,10 @@ of a Pool and runs steps:
      the best code, check its uncovered count with the GPU verifier
      (cov_verify, the count of cov/verify_cov.py), free the slot.
 
-Requests that arrive while a step runs join at the next step.  Latency is
+Between steps the cluster sizes are rebalanced: while the GPU has CTAs to
+spare (few requests active), the requests with the most work per move get
+wider clusters.  Requests that arrive while a step runs join at the next
+step.  Latency is
 completion minus arrival; throughput is the moves of all requests over the
 wall time.
 """
@@ -28,7 +31,7 @@ import time
 import numpy as np
 
 from . import verify
-from .batch import size_class
+from .batch import RESIDENT_CTAS, size_class
 from .engine import Pool, device_memory, slot_bytes
 from .workloads import uniform_code
 
@@ -45,9 +48,32 @@ def default_cluster(q, n, R, M):
     return 8
 
 
+def _work_per_move(r):
+    return math.comb(r["n"] - 1, r["R"]) * (r["q"] - 1) ** r["R"] if r["R"] <= r["n"] - 1 else 1
+
+
+def elastic_clusters(base, work, ctas):
+    """Cluster size per request: its base size, doubled round by round for
+    the requests with the most work per move while the total stays within
+    `ctas` resident CTAs (at most 16 per request)."""
+    want = dict(base)
+    used = sum(want.values())
+    order = sorted(want, key=lambda s: -work[s])
+    grown = True
+    while grown:
+        grown = False
+        for s in order:
+            c = want[s]
+            if c < 16 and used + c <= ctas:
+                want[s] = 2 * c
+                used += c
+                grown = True
+    return want
+
+
 class Server:
     def __init__(self, max_slots=256, chunk=256, reserve_bytes=8 << 30, budget_bytes=None, clusters=None,
-                 verify_results=True, budget_s=120.0):
+                 verify_results=True, budget_s=120.0, elastic=True, ctas=RESIDENT_CTAS):
         self.pool = Pool(max_slots, cluster=1, budget_s=budget_s)
         self.max_slots = max_slots
         self.chunk = chunk
@@ -61,6 +87,8 @@ class Server:
         self.resident = 0          # device bytes of admitted requests
         self.moves = 0
         self.steps = 0
+        self.elastic = elastic
+        self.ctas = ctas
 
     def _cluster(self, r):
         if isinstance(self.clusters, dict):
@@ -99,7 +127,9 @@ class Server:
                     code = uniform_code(r["q"], r["n"], r["M"], r["seed"])
                 s = self.pool.add(r["q"], r["n"], r["R"], r["M"], code=code, seed=r["seed"],
                                   tabu=r.get("tabu", 0))
-                self.pool.set_slot_param(s, "cluster", self._cluster(r))
+                r["cluster"] = self._cluster(r)
+                self.pool.set_slot_param(s, "cluster", r["cluster"])
+                r["cur_cluster"] = r["cluster"]
                 self.pool.set_slot_param(s, "it_limit", r["moves"])
                 r["admitted"] = now
                 r["slot"] = s
@@ -112,10 +142,24 @@ class Server:
         self.waiting = keep
         return n
 
+    def _rebalance(self):
+        """Elastic cluster sizes: start from each request's own size; while
+        the GPU has CTAs to spare, double the cluster of the request with
+        the most work per move (up to 16).  Cluster size never changes a
+        trajectory, only how fast each request advances."""
+        base = {s: r["cluster"] for s, r in self.active.items()}
+        want = elastic_clusters(base, {s: _work_per_move(r) for s, r in self.active.items()}, self.ctas) \
+            if self.elastic else base
+        for s, c in want.items():
+            if self.active[s].get("cur_cluster") != c:
+                self.pool.set_slot_param(s, "cluster", c)
+                self.active[s]["cur_cluster"] = c
+
     def step(self):
         """One launch over every admitted request; retire the finished."""
         if not self.active:
             return []
+        self._rebalance()
         self.pool.run(self.chunk)
         self.steps += 1
         st = self.pool.status_all(self.max_slots)
@@ -188,3 +232,32 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def main(argv=None):
+    """Open-loop sweep: python -m coldcase_gb300.serve --lam 10 50 100 500"""
+    import argparse
+    import json
+    from .batch import tune_batch
+    from .workloads import serve_requests
+    ap = argparse.ArgumentParser(description="continuous-batching solve server, Poisson load sweep")
+    ap.add_argument("--lam", type=float, nargs="+", default=[10.0, 50.0, 100.0, 500.0])
+    ap.add_argument("--requests", type=int, default=100)
+    ap.add_argument("--chunk", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=2027)
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-elastic", action="store_true")
+    a = ap.parse_args(argv)
+    plan = None
+    if not a.no_tune:
+        plan, _, _ = tune_batch(serve_requests(a.requests, lam=a.lam[0], seed=a.seed))
+    for lam in a.lam:
+        reqs = serve_requests(a.requests, lam=lam, seed=a.seed)
+        with Server(chunk=a.chunk, clusters=plan, elastic=not a.no_elastic) as srv:
+            rep = srv.serve(reqs)
+        rep["lam_per_s"] = lam
+        print(json.dumps(rep), flush=True)
+
+
+if __name__ == "__main__":
+    main()

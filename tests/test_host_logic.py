@@ -4,7 +4,7 @@ import math
 
 from coldcase_gb300 import workloads
 from coldcase_gb300.batch import Tuner, size_class
-from coldcase_gb300.serve import default_cluster
+from coldcase_gb300.serve import default_cluster, elastic_clusters
 
 
 def test_hetero_cells_domain():
@@ -49,3 +49,14 @@ def test_tuner_plan_keeps_narrow_when_saturated():
     classes = {"big": (1000, {1: 300e-6, 2: 170e-6, 4: 90e-6})}
     choice, _ = Tuner.plan(classes, 20000, resident=152)
     assert choice["big"] == 1
+
+
+def test_elastic_clusters():
+    # few requests: everyone widened, the heaviest first, within the CTAs
+    w = elastic_clusters({1: 1, 2: 2, 3: 1}, {1: 10, 2: 90000, 3: 500}, 152)
+    assert w == {1: 16, 2: 16, 3: 16}
+    w = elastic_clusters({1: 1, 2: 2, 3: 1}, {1: 10, 2: 90000, 3: 500}, 20)
+    assert sum(w.values()) <= 20 and w[2] >= w[3] >= w[1]
+    # saturated: nothing changes
+    base = {k: 1 for k in range(200)}
+    assert elastic_clusters(base, {k: k for k in range(200)}, 152) == base
