@@ -1273,13 +1273,14 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
     if (S.ul_valid) {
         // every zero-count word is on the list: the first one after start is
         // the entry minimising (x - start) mod N
+        // a thread reads the count only for an entry that would lower its
+        // running minimum (a few per thread), not for every entry
         const int n0 = S.uln;
         unsigned best = 0xffffffffu;
         for (int e = tid; e < n0; e += NT) {
             uint32_t x = cov_ldcg(&d.ul_idx[e]);
-            if ((cov_ldcg(&d.cw[x]) & 0xffffu) != 0) continue;
             unsigned key = x >= start ? x - start : x + (d.N - start);
-            best = min(best, key);
+            if (key < best && (cov_ldcg(&d.cw[x]) & 0xffffu) == 0) best = key;
         }
         best = block_min_u32(S, best);
         if (best != 0xffffffffu) {
@@ -2217,10 +2218,13 @@ __global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
 // marks its ball there -- a ball of radius R - d(prefix) on the low digits --
 // so the M*V increments of covsearch2e.c:958-967 (rebuild = M x ball_apply)
 // are shared-memory atomics, and the coverage array is written to HBM once.
-// Before leaving, the CTA counts the tile's uncovered words and adds each
-// singly covered word at distance exactly R from its coverer k to
-// P[k] = (T_k, H_k) -- the counts the reference's shared-sphere walk
-// (covsearch2e.c:592-654) produces for k.
+// Before leaving, the CTA counts the tile's uncovered words (zeros[0]),
+// appends them to the uncovered-word list (zeros[1] counts the appends; the
+// list is complete if that stays within its capacity -- the rebuild of
+// covsearch2e.c:323-338 done in the same pass), and adds each singly covered
+// word at distance exactly R from its coverer k to P[k] = (T_k, H_k) -- the
+// counts the reference's shared-sphere walk (covsearch2e.c:592-654)
+// produces for k.  ul_bit must be clear beforehand.
 #define BT_MAX 24576           // words of a tile (96 KB of shared memory)
 #define BT_LCH 1024            // codewords staged per chunk
 #define BT_NT  512
@@ -2317,16 +2321,41 @@ __global__ void __launch_bounds__(BT_NT) k_build_state(CovSlot d, unsigned long 
 
     uint32_t *gout = d.cw + (size_t)blockIdx.x * T;
     unsigned long long z = 0;
-    for (uint32_t x = threadIdx.x; x < T; x += BT_NT) {
-        const uint32_t v = tile[x];
-        gout[x] = v;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t x0 = 0; x0 < T; x0 += BT_NT) {
+        const uint32_t x = x0 + threadIdx.x;
+        const bool in = x < T;
+        const uint32_t v = in ? tile[x] : 1u;
         const uint32_t c = v & 0xffffu;
-        z += c == 0;
-        if (c == 1) {
-            const int k = (int)(v >> 16);
-            uint64_t pk = hp;
+        uint64_t pk = hp;
+        if (in) {
+            gout[x] = v;
             uint32_t y = x;
-            for (int j = n - 1; j >= nh; --j) { pk |= (uint64_t)(y % (uint32_t)q) << (4 * j); y /= (uint32_t)q; }
+            if (c <= 1)
+                for (int j = n - 1; j >= nh; --j) { pk |= (uint64_t)(y % (uint32_t)q) << (4 * j); y /= (uint32_t)q; }
+        }
+        // uncovered words go on the uncovered-word list (order is free: the
+        // list only feeds sums and the first-after-start search)
+        const bool zero = in && c == 0;
+        const unsigned zm = __ballot_sync(FULL, zero);
+        if (zm) {
+            unsigned long long base = 0;
+            if (lane == __ffs(zm) - 1) base = atomicAdd(&zeros[1], (unsigned long long)__popc(zm));
+            base = __shfl_sync(FULL, base, __ffs(zm) - 1);
+            if (zero) {
+                const unsigned long long at = base + __popc(zm & ((1u << lane) - 1));
+                const uint32_t gx = blockIdx.x * T + x;
+                if (at < (unsigned long long)d.ul_cap) {
+                    d.ul_idx[at] = gx;
+                    d.ul_pk[at] = pk;
+                    atomicOr(&d.ul_bit[gx >> 5], 1u << (gx & 31));
+                }
+            }
+        }
+        z += zero;
+        if (in && c == 1) {
+            const int k = (int)(v >> 16);
             uint64_t D = cov_spread(pk ^ d.code[k]);
             if (__popcll(D) == R) {
                 int32_t *Pk = d.P + (size_t)k * (n + 1);
@@ -2985,23 +3014,29 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
         }
         CK(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
     }
-    // coverage array, uncovered count and private counts of the final M
-    // codewords, built tile by tile; then the best code
-    CK(cudaMemsetAsync(d_z, 0, 8, st));
+    // coverage array, uncovered count, uncovered-word list and private
+    // counts of the final M codewords, built tile by tile; then the best code
+    CK(cudaMemsetAsync(d_z, 0, 16, st));
     CK(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
+    CK(cudaMemsetAsync(d.ul_bit, 0, (size_t)((N + 31) / 32) * 4, st));
     k_build_state<<<(unsigned)ipow_h(q, d.bt_nh), BT_NT, bt_smem_bytes(d.bt_tw), st>>>(d, d_z);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(d.best, d.code, (size_t)M * 8, cudaMemcpyDeviceToDevice, st));
-    unsigned long long z = 0;
-    CK(cudaMemcpyAsync(&z, d_z, 8, cudaMemcpyDeviceToHost, st));
+    unsigned long long zl[2] = {0, 0};
+    CK(cudaMemcpyAsync(zl, d_z, 16, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    const unsigned long long z = zl[0];
     memset(&hs, 0, sizeof hs);
     for (int k = 0; k < 4; k++) hs.rng[k] = rng.s[k];
     hs.unc = (long long)z;
     hs.best_unc = hs.unc;
     hs.target = -1;
     hs.it_limit = -1;
-    hs.ul_valid = 0;
+    // the list is in use from the first move when the uncovered words are at
+    // most half its capacity -- when the reference's first iteration would
+    // rebuild it (covsearch2e.c:1326-1329)
+    hs.ul_valid = z <= (unsigned long long)d.ul_cap / 2 && zl[1] == z;
+    hs.ul_n = hs.ul_valid ? (int)z : 0;
     hs.finished = hs.unc == 0;
     CK(cudaMemcpyAsync(d.st, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
     int rc = push_slot(pool, s);
