@@ -47,21 +47,6 @@ __global__ void k_dt_bitmap(const uint8_t *__restrict__ code, int M, DtGeom g, u
     }
 }
 
-// line-min along one axis of a shared-memory block: elements e = o*q*s +
-// a*s + i (a < q, i < s) for every outer o and inner i
-__device__ __forceinline__ void dt_axis_smem(uint8_t *t, int total, int q, int s, int inf)
-{
-    const int fibers = total / q;
-    for (int f = threadIdx.x; f < fibers; f += blockDim.x) {
-        int o = f / s, i = f - o * s;
-        uint8_t *b = t + (size_t)o * q * s + i;
-        int m = inf;
-        for (int a = 0; a < q; a++) m = min(m, (int)b[a * s]);
-        int c = min(m + 1, inf);
-        for (int a = 0; a < q; a++) if (b[a * s] > c) b[a * s] = (uint8_t)c;
-    }
-}
-
 // histogram update aggregated over the lanes holding the same value
 __device__ __forceinline__ void dt_hist_add(int *sh, int v)
 {
@@ -70,32 +55,73 @@ __device__ __forceinline__ void dt_hist_add(int *sh, int v)
     if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&sh[v], __popc(same));
 }
 
-// Pass 1: tiles of q^k contiguous words, low k axes, from the code bitmap.
-// When k == n this is the whole transform and the histogram is taken here.
+// One line-min pass over packed bytes: `nfib` fibres of q 32-bit words, word
+// k of fibre f at  base(f) + a*stride  (a < q), base(f) = (f / inner) *
+// q*stride + (f % inner).  Each word holds 4 independent lines (one per byte),
+// so one __vminu4 serves four of them.
+__device__ __forceinline__ void dt_pass4(uint32_t *w, int nfib, int q, int stride, int inner, uint32_t inf4)
+{
+    for (int f = threadIdx.x; f < nfib; f += blockDim.x) {
+        const int o = f / inner, i = f - o * inner;
+        uint32_t *b = w + o * q * stride + i;
+        uint32_t m = inf4;
+        for (int a = 0; a < q; a++) m = __vminu4(m, b[a * stride]);
+        const uint32_t c = __vminu4(__vadd4(m, 0x01010101u), inf4);
+        for (int a = 0; a < q; a++) b[a * stride] = __vminu4(b[a * stride], c);
+    }
+}
+
+// Pass 1: tiles of T = q^k contiguous words (the low k axes), from the code
+// bitmap.  In shared memory a tile is T/q rows -- the q words of one line of
+// the lowest axis -- each padded to Q4 = 4*ceil(q/4) bytes, so that every
+// axis above the lowest moves whole 32-bit words.  The lowest axis is taken
+// while loading: a word is 0 on the code, 1 if its line holds a codeword,
+// else n+1.  When k == n this is the whole transform and the histogram is
+// taken here.
 __global__ void __launch_bounds__(DT_NT)
 k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__ D,
          unsigned long long *hist)
 {
-    extern __shared__ __align__(16) uint8_t dt_sm[];
+    extern __shared__ __align__(16) uint32_t dt_w[];
     __shared__ int sh[COV_MAXN + 2];
+    const int q = g.q;
     const uint32_t T = g.pw[k];
+    const int rows = (int)(T / (uint32_t)q);
+    const int wpr = (q + 3) >> 2;                 // 32-bit words per row
+    const uint32_t inf = (uint32_t)g.inf, inf4 = inf * 0x01010101u;
     const uint32_t ntile = g.N / T;
     const bool last = (k == g.n) && hist != nullptr;
+    uint8_t *dt_b = reinterpret_cast<uint8_t *>(dt_w);
     if (threadIdx.x < COV_MAXN + 2) sh[threadIdx.x] = 0;
     for (uint32_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const uint32_t x0 = tile * T;
         __syncthreads();
-        for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
-            uint32_t x = x0 + e;
-            dt_sm[e] = ((__ldg(&bm[x >> 5]) >> (x & 31)) & 1u) ? 0 : (uint8_t)g.inf;
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const uint32_t xr = x0 + (uint32_t)r * (uint32_t)q;
+            // q bits of the row from at most two bitmap words
+            const uint32_t lo = __ldg(&bm[xr >> 5]);
+            const uint32_t hi = ((xr & 31) + (uint32_t)q > 32) ? __ldg(&bm[(xr >> 5) + 1]) : 0u;
+            const uint64_t bits = ((((uint64_t)hi << 32) | lo) >> (xr & 31)) & ((1ull << q) - 1);
+            const uint32_t fill = bits ? 1u : inf;
+            for (int w = 0; w < wpr; w++) {
+                uint32_t v = 0;
+                for (int b = 0; b < 4; b++) {
+                    const int a = 4 * w + b;
+                    const uint32_t byte = a >= q ? inf : (((bits >> a) & 1) ? 0u : fill);
+                    v |= byte << (8 * b);
+                }
+                dt_w[r * wpr + w] = v;
+            }
         }
         __syncthreads();
-        for (int j = 0; j < k; j++) {          // in-tile stride q^j
-            dt_axis_smem(dt_sm, (int)T, g.q, (int)g.pw[j], g.inf);
+        for (int j = 1; j < k; j++) {          // rows of axis j: stride q^(j-1) rows
+            const int inner = (int)g.pw[j - 1] * wpr;
+            dt_pass4(dt_w, rows / q * wpr, q, inner, inner, inf4);
             __syncthreads();
         }
         for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
-            uint8_t v = dt_sm[e];
+            const uint32_t r = e / (uint32_t)q, a = e - r * (uint32_t)q;
+            const uint8_t v = dt_b[r * (uint32_t)(wpr * 4) + a];
             D[x0 + e] = v;
             if (last) dt_hist_add(sh, v);
         }
@@ -106,13 +132,17 @@ k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__
 }
 
 // Pass 2+: the axes of group [j0, j0+gsz) (in-word strides q^j0 .. ), for a
-// strip of up to DT_STRIP_W consecutive positions below the group.
+// strip of up to DT_STRIP_W consecutive positions below the group: rows of
+// DT_STRIP_W bytes, DT_STRIP_W/4 words, so each pass moves whole words.
 __global__ void __launch_bounds__(DT_NT)
 k_dt_high(DtGeom g, int j0, int gsz, int last_, uint8_t *__restrict__ D, unsigned long long *hist)
 {
     const bool last = last_ && hist != nullptr;
-    extern __shared__ __align__(16) uint8_t dt_sm[];
+    extern __shared__ __align__(16) uint32_t dt_w[];
     __shared__ int sh[COV_MAXN + 2];
+    constexpr int WW = DT_STRIP_W / 4;           // words per row
+    uint8_t *dt_b = reinterpret_cast<uint8_t *>(dt_w);
+    const uint32_t inf4 = (uint32_t)g.inf * 0x01010101u;
     const uint32_t s = g.pw[j0];                 // stride of the lowest axis in the group
     const uint32_t rows = g.pw[gsz];
     const uint32_t span = rows * s;              // words spanned by one value of the outer digits
@@ -126,20 +156,21 @@ k_dt_high(DtGeom g, int j0, int gsz, int last_, uint8_t *__restrict__ D, unsigne
         const int w = (int)min((uint32_t)DT_STRIP_W, s - c0);
         const uint32_t base = o * span + c0;
         __syncthreads();
-        // element (row r, column c) at base + r*s + c, kept at r*W + c
+        // element (row r, column c) at base + r*s + c, kept at byte r*W + c
         for (uint32_t e = threadIdx.x; e < rows * DT_STRIP_W; e += blockDim.x) {
             uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
-            dt_sm[e] = (c < (uint32_t)w) ? D[base + r * s + c] : (uint8_t)g.inf;
+            dt_b[e] = (c < (uint32_t)w) ? D[base + r * s + c] : (uint8_t)g.inf;
         }
         __syncthreads();
-        for (int j = 0; j < gsz; j++) {          // row stride q^j, column width W
-            dt_axis_smem(dt_sm, (int)(rows * DT_STRIP_W), g.q, (int)g.pw[j] * DT_STRIP_W, g.inf);
+        for (int j = 0; j < gsz; j++) {          // row stride q^j
+            const int inner = (int)g.pw[j] * WW;
+            dt_pass4(dt_w, (int)(rows / (uint32_t)g.q) * WW, g.q, inner, inner, inf4);
             __syncthreads();
         }
         for (uint32_t e = threadIdx.x; e < rows * DT_STRIP_W; e += blockDim.x) {
             uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
             if (c < (uint32_t)w) {
-                uint8_t v = dt_sm[e];
+                uint8_t v = dt_b[e];
                 D[base + r * s + c] = v;
                 if (last) dt_hist_add(sh, v);
             }
@@ -226,14 +257,15 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
         CK(cudaGetLastError());
     }
     // low group: as many axes as fit a tile
-    int k = 0;
-    while (k < g.n && (long long)g.pw[k + 1] <= DT_TILE_MAX) k++;
-    if (k == 0) k = 1;
+    const long long q4 = (g.q + 3) / 4 * 4;      // padded bytes of one lowest-axis line
+    auto low_bytes = [&](int kk) { return (long long)g.pw[kk] / g.q * q4; };
+    int k = 1;
+    while (k < g.n && low_bytes(k + 1) <= DT_TILE_MAX) k++;
     const int sms = 152;
     const uint32_t ntile = g.N / g.pw[k];
     {
         int grid = (int)std::min<uint32_t>(ntile, (uint32_t)sms * 4);
-        k_dt_low<<<grid, DT_NT, (size_t)g.pw[k], st>>>(g, k, d_bm, d_D, d_hist);
+        k_dt_low<<<grid, DT_NT, (size_t)low_bytes(k), st>>>(g, k, d_bm, d_D, d_hist);
         CK(cudaGetLastError());
     }
     // high groups
