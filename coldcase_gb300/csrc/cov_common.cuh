@@ -110,10 +110,11 @@ struct CovSlot {
     const uint8_t *ball_sub;     // concatenated r-subset tables, r = 0..R
     int ball_off[COV_MAXN + 2];  // start (in subsets) of radius r in ball_sub
     // state build by tiles: a tile is the q^bt_nl words that share their
-    // first bt_nh digits; bt_items lists the ball of radius <= min(R, bt_nl)
-    // on the low digits (nibble j = value index + 1 at position j, 0 = the
-    // centre's digit), by radius: bt_v[r] items have radius <= r
+    // first bt_nh digits; bt_items / bt_last list the ball of radius
+    // <= min(R, bt_nl) on the low digits as groups (cov_tiles.cuh), by
+    // radius: bt_v[r] groups have radius <= r
     const uint64_t *bt_items;
+    const uint8_t *bt_last;
     int bt_nh, bt_nl;
     uint32_t bt_tw;              // q^bt_nl
     uint32_t bt_v[COV_MAXN + 2];

@@ -34,6 +34,7 @@
 #include <algorithm>
 #include <cooperative_groups.h>
 #include "cov_common.cuh"
+#include "cov_tiles.cuh"
 #include "../../include/covgpu.h"
 
 namespace cg = cooperative_groups;
@@ -2213,11 +2214,9 @@ __global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
 }
 
 // Whole-state build, one CTA per tile of q^bt_nl consecutive words (the
-// words sharing their first bt_nh digits).  The tile's counters live in
-// shared memory while every codeword within distance R of the tile's prefix
-// marks its ball there -- a ball of radius R - d(prefix) on the low digits --
-// so the M*V increments of covsearch2e.c:958-967 (rebuild = M x ball_apply)
-// are shared-memory atomics, and the coverage array is written to HBM once.
+// words sharing their first bt_nh digits; cov_tiles.cuh marks the balls):
+// each covered word gets 1 + (id << 16) per coverer, and the tile's
+// counters are written to HBM once.
 // Before leaving, the CTA counts the tile's uncovered words (zeros[0]),
 // appends them to the uncovered-word list (zeros[1] counts the appends; the
 // list is complete if that stays within its capacity -- the rebuild of
@@ -2225,14 +2224,6 @@ __global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
 // word at distance exactly R from its coverer k to P[k] = (T_k, H_k) -- the
 // counts the reference's shared-sphere walk (covsearch2e.c:592-654)
 // produces for k.  ul_bit must be clear beforehand.
-#define BT_MAX 24576           // words of a tile (96 KB of shared memory)
-#define BT_LCH 1024            // codewords staged per chunk
-#define BT_NT  512
-
-static inline size_t bt_smem_bytes(uint32_t tw)
-{
-    return (size_t)BT_LCH * (8 + 4 + 4) + (size_t)tw * 4;
-}
 
 __global__ void __launch_bounds__(BT_NT) k_build_state(CovSlot d, unsigned long long *zeros)
 {
@@ -2242,82 +2233,18 @@ __global__ void __launch_bounds__(BT_NT) k_build_state(CovSlot d, unsigned long 
     uint32_t *lbase = lid + BT_LCH;                // [BT_LCH] their low-digit index
     uint32_t *tile = lbase + BT_LCH;               // [bt_tw]
     __shared__ int gcnt[COV_MAXN + 2], gpos[COV_MAXN + 2], gfill[COV_MAXN + 2];
-    constexpr int PER = BT_LCH / BT_NT;
 
     const int q = d.q, n = d.n, R = d.R, nh = d.bt_nh, nl = d.bt_nl;
     const uint32_t T = d.bt_tw;
-    const int rmax = min(R, nl);
     uint64_t hp = 0;
     {
         uint32_t t = blockIdx.x;
         for (int j = nh - 1; j >= 0; --j) { hp |= (uint64_t)(t % (uint32_t)q) << (4 * j); t /= (uint32_t)q; }
     }
-    const uint64_t hmask = (1ull << (4 * nh)) - 1;   // nh <= 15
     for (uint32_t x = threadIdx.x; x < T; x += BT_NT) tile[x] = 0;
-
-    for (int m0 = 0; m0 < d.M; m0 += BT_LCH) {
-        if (threadIdx.x < COV_MAXN + 2) gcnt[threadIdx.x] = 0;
-        __syncthreads();
-        int g[PER];
-        uint64_t pcv[PER];
-#pragma unroll
-        for (int u = 0; u < PER; u++) {
-            const int k = m0 + threadIdx.x + u * BT_NT;
-            g[u] = -1;
-            pcv[u] = 0;
-            if (k < d.M) {
-                const uint64_t pc = d.code[k];
-                pcv[u] = pc;
-                const int dh = __popcll(cov_spread((pc ^ hp) & hmask));
-                if (dh <= R) {
-                    g[u] = min(R - dh, nl);
-                    atomicAdd(&gcnt[g[u]], 1);
-                }
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int r = 0; r <= rmax; r++) { gpos[r] = acc; gfill[r] = acc; acc += gcnt[r]; }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int u = 0; u < PER; u++) {
-            if (g[u] < 0) continue;
-            const int at = atomicAdd(&gfill[g[u]], 1);
-            uint32_t lb = 0;
-            for (int j = nh; j < n; j++) lb += (uint32_t)cov_nib(pcv[u], j) * d.pw[j];
-            lpc[at] = pcv[u];
-            lid[at] = (uint32_t)(m0 + threadIdx.x + u * BT_NT);
-            lbase[at] = lb;
-        }
-        __syncthreads();
-        for (int r = 0; r <= rmax; r++) {
-            const uint32_t cnt = (uint32_t)gcnt[r];
-            if (!cnt) continue;
-            const uint32_t V = d.bt_v[r];
-            const uint64_t minv = (0x100000000ull + V - 1) / V;     // ceil(2^32 / V)
-            const uint32_t total = cnt * V;
-            const int p0 = gpos[r];
-            for (uint32_t t = threadIdx.x; t < total; t += BT_NT) {
-                uint32_t kk = (uint32_t)(((uint64_t)t * minv) >> 32);   // t / V or one more
-                if (kk * V > t) kk--;
-                const uint32_t it = t - kk * V;
-                const uint64_t pc = lpc[p0 + kk];
-                uint64_t sp = d.bt_items[it];
-                int off = (int)lbase[p0 + kk];
-                while (sp) {
-                    const int j = (__ffsll((long long)sp) - 1) >> 2;
-                    const int dig = (int)((sp >> (4 * j)) & 15u) - 1;
-                    sp &= ~(15ull << (4 * j));
-                    const int cj = cov_nib(pc, j);
-                    off += (dig + (dig >= cj) - cj) * (int)d.pw[j];
-                }
-                atomicAdd(&tile[off], cov_cw_unit((int)lid[p0 + kk]));
-            }
-        }
-        __syncthreads();
-    }
+    BtScratch sc{lpc, lid, lbase, gcnt, gpos, gfill};
+    bt_mark_tile(tile, d.q, d.n, R, d.M, d.code, d.pw, nh, nl, d.bt_items, d.bt_last, d.bt_v, hp, sc,
+                 [](uint32_t id) { return cov_cw_unit((int)id); });
 
     uint32_t *gout = d.cw + (size_t)blockIdx.x * T;
     unsigned long long z = 0;
@@ -2470,45 +2397,6 @@ static int padj_auto(int q, int n, int R, int M)
     return 2.0 * Sp * lam * std::exp(-lam) * (1.0 + lam / 2.0) >= 8192.0;
 }
 
-// tile geometry of the state build: the most low digits whose q^nl words fit
-// a tile
-static void bt_geom(int q, int n, int *nh, int *nl)
-{
-    int l = 1;
-    while (l < n && ipow_h(q, l + 1) <= BT_MAX) l++;
-    *nl = l;
-    *nh = n - l;
-}
-
-// the ball of radius <= min(R, nl) on the low digits nh..n-1, by radius
-static std::vector<uint64_t> bt_items_h(int q, int n, int R, int nh, uint32_t *vcum)
-{
-    const int nl = n - nh, rmax = std::min(R, nl);
-    std::vector<uint64_t> out;
-    for (int r = 0; r <= rmax; r++) {
-        std::vector<int> sub(r);
-        for (int k = 0; k < r; k++) sub[k] = k;
-        while (true) {
-            std::vector<int> dig(r, 0);
-            while (true) {
-                uint64_t sp = 0;
-                for (int k = 0; k < r; k++) sp |= (uint64_t)(dig[k] + 1) << (4 * (nh + sub[k]));
-                out.push_back(sp);
-                int k = r - 1;
-                while (k >= 0 && dig[k] == q - 2) dig[k--] = 0;
-                if (k < 0) break;
-                dig[k]++;
-            }
-            int k = r - 1;
-            while (k >= 0 && sub[k] == nl - r + k) k--;
-            if (k < 0) break;
-            sub[k]++;
-            for (int m = k + 1; m < r; m++) sub[m] = sub[m - 1] + 1;
-        }
-        vcum[r] = (uint32_t)out.size();
-    }
-    return out;
-}
 int fill_subsets_h(const int *pool, int np, int R, int rs, uint8_t *out)
 {
     if (binom_h(np, R) <= 0) return 0;
@@ -2791,7 +2679,10 @@ size_t cov_slot_bytes(const cov_params *prm)
         int nh, nl;
         bt_geom(q, n, &nh, &nl);
         uint32_t vc[COV_MAXN + 2];
-        add(bt_items_h(q, n, std::min(R, n), nh, vc).size() * 8);   // state-build ball table
+        std::vector<uint8_t> lst;
+        const size_t ni = bt_items_h(q, n, std::min(R, n), nh, vc, lst).size();
+        add(ni * 8);                                 // state-build ball groups
+        add(ni);
     }
     add(sizeof(CovSlotState));
     if (prm->trace) add((size_t)prm->trace_cap * sizeof(cov_move_rec));
@@ -2886,9 +2777,12 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.sub = dsub; d.ball_sub = dball; d.sub1 = dsub1;
     bt_geom(q, n, &d.bt_nh, &d.bt_nl);
     d.bt_tw = (uint32_t)ipow_h(q, d.bt_nl);
-    std::vector<uint64_t> bti = bt_items_h(q, n, R, d.bt_nh, d.bt_v);
+    std::vector<uint8_t> btl;
+    std::vector<uint64_t> bti = bt_items_h(q, n, R, d.bt_nh, d.bt_v, btl);
     uint64_t *dbt = (uint64_t *)take_(bti.size() * 8);
+    uint8_t *dbl = (uint8_t *)take_(btl.size());
     d.bt_items = dbt;
+    d.bt_last = dbl;
     d.st = pool->d_states + s;
     d.trace = prm->trace ? take_((size_t)prm->trace_cap * sizeof(cov_move_rec)) : nullptr;
     d.trace_cap = prm->trace ? prm->trace_cap : 0;
@@ -2901,6 +2795,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     if (e == cudaSuccess) e = cudaMemcpyAsync(dball, balls.data(), balls.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dsub1, subs1.data(), subs1.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dbt, bti.data(), bti.size() * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dbl, btl.data(), btl.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { cudaFree(arena); return -(100 + (int)e); }
     pool->slots[s] = h;

@@ -19,6 +19,7 @@
 #include <vector>
 #include <algorithm>
 #include "cov_common.cuh"
+#include "cov_tiles.cuh"
 #include "../../include/covgpu.h"
 
 #define DT_TILE_MAX   65536    // bytes of the contiguous low-axes tile
@@ -190,39 +191,56 @@ __global__ void k_count_above(const uint8_t *__restrict__ D, uint32_t N, int R, 
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
-// ball marking into uint16 counts (pairs updated with 32-bit atomics)
-__global__ void k_count_balls(CovSlot d, const uint8_t *__restrict__ code, int M, uint16_t *cnt)
+// ------------------------------------------------ coverage multiplicity ----
+__global__ void k_pack_code(const uint8_t *__restrict__ code, int M, int n, uint64_t *__restrict__ out)
 {
-    const int R = d.R;
-    uint32_t cum[COV_MAXN + 2];
-    cum[0] = 1;
-    for (int r = 1; r <= R; r++)
-        cum[r] = cum[r - 1] + (uint32_t)(d.ball_off[r + 1] - d.ball_off[r]) * d.ppow[r - 1];
-    const unsigned long long per = cum[R];
-    const unsigned long long total = per * (unsigned long long)M;
-    uint32_t *c32 = reinterpret_cast<uint32_t *>(cnt);
-    for (unsigned long long g = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
-         g += (unsigned long long)gridDim.x * blockDim.x) {
-        const int i = (int)(g / per);
-        const uint32_t t = (uint32_t)(g - (unsigned long long)i * per);
-        uint64_t pc = 0;
-        uint32_t base = 0;
-        for (int j = 0; j < d.n; j++) {
-            int v = code[(size_t)i * d.n + j];
-            pc |= (uint64_t)v << (4 * j);
-            base += (uint32_t)v * d.pw[j];
-        }
-        if (t == 0) { atomicAdd(&c32[base >> 1], (base & 1) ? 65536u : 1u); continue; }
-        int r = 1;
-        while (t >= cum[r]) r++;
-        const uint8_t *subs = d.ball_sub + (size_t)d.ball_off[r] * d.rs;
-        CovItem it = cov_item(d, subs, r, t - cum[r - 1], base, pc);
-        for (int kk = 0; kk < d.q - 1; kk++) {
-            uint32_t w; uint64_t pk;
-            cov_item_word(d, it, kk, w, pk);
-            atomicAdd(&c32[w >> 1], (w & 1) ? 65536u : 1u);
-        }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+        uint64_t v = 0;
+        for (int j = 0; j < n; j++) v |= (uint64_t)code[(size_t)i * n + j] << (4 * j);
+        out[i] = v;
     }
+}
+
+struct CountGeom {
+    int q, n, R, M, nh, nl;
+    uint32_t tw;                       // q^nl words per tile
+    uint32_t nitems;                   // ball groups (their last positions follow them)
+    uint32_t pw[COV_MAXN];             // q^(n-1-j)
+    uint32_t vcum[COV_MAXN + 2];
+};
+
+// cnt[x] = #{i : d(x, c_i) <= R} saturated at 65535 (the cnt[] of
+// covsearch2e.c:958-967, the OUT=2 map of cov/gemm2/dct.cu:360-411), one CTA
+// per tile (cov_tiles.cuh); the tile's uncovered words are counted too.
+__global__ void __launch_bounds__(BT_NT) k_count_tiles(CountGeom g, const uint64_t *__restrict__ code,
+                                                       const uint64_t *__restrict__ items, uint16_t *cnt,
+                                                       unsigned long long *zeros)
+{
+    extern __shared__ __align__(16) unsigned char ct_raw[];
+    uint64_t *lpc = (uint64_t *)ct_raw;
+    uint32_t *lid = (uint32_t *)(lpc + BT_LCH);
+    uint32_t *lbase = lid + BT_LCH;
+    uint32_t *tile = lbase + BT_LCH;
+    __shared__ int gcnt[COV_MAXN + 2], gpos[COV_MAXN + 2], gfill[COV_MAXN + 2];
+    uint64_t hp = 0;
+    {
+        uint32_t t = blockIdx.x;
+        for (int j = g.nh - 1; j >= 0; --j) { hp |= (uint64_t)(t % (uint32_t)g.q) << (4 * j); t /= (uint32_t)g.q; }
+    }
+    for (uint32_t x = threadIdx.x; x < g.tw; x += BT_NT) tile[x] = 0;
+    BtScratch sc{lpc, lid, lbase, gcnt, gpos, gfill};
+    bt_mark_tile(tile, g.q, g.n, g.R, g.M, code, g.pw, g.nh, g.nl, items,
+                 reinterpret_cast<const uint8_t *>(items + g.nitems), g.vcum, hp, sc,
+                 [](uint32_t) { return 1u; });
+    unsigned long long z = 0;
+    uint16_t *out = cnt + (size_t)blockIdx.x * g.tw;
+    for (uint32_t x = threadIdx.x; x < g.tw; x += BT_NT) {
+        const uint32_t v = tile[x];
+        out[x] = (uint16_t)min(v, 65535u);
+        z += v == 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+    if ((threadIdx.x & 31) == 0 && z && zeros) atomicAdd(zeros, z);
 }
 
 // ============================================================ host ========
@@ -241,6 +259,7 @@ int geom(int q, int n, DtGeom &g)
 }
 
 int g_dt_attr = 0;
+int g_ct_attr = 0;
 
 // the transform on device buffers; hist (device, n+2 entries) may be null
 int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned long long *d_hist,
@@ -283,38 +302,6 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
         j0 += gsz;
     }
     return 0;
-}
-
-void build_ball_tables(int n, int R, int rs, std::vector<uint8_t> &balls, int *ball_off)
-{
-    auto binom = [](int a, int b) -> long long {
-        if (b < 0 || b > a) return 0;
-        if (b > a - b) b = a - b;
-        long long r = 1;
-        for (int i = 0; i < b; i++) r = r * (a - i) / (i + 1);
-        return r;
-    };
-    int off = 0;
-    for (int r = 0; r <= R; r++) {
-        ball_off[r] = off;
-        int cnt = (int)binom(n, r);
-        balls.resize((size_t)(off + cnt) * rs, 0);
-        if (r > 0) {
-            int c[32], k = 0;
-            for (int t = 0; t < r; t++) c[t] = t;
-            for (;;) {
-                for (int t = 0; t < r; t++) balls[(size_t)(off + k) * rs + t] = (uint8_t)c[t];
-                k++;
-                int t = r - 1;
-                while (t >= 0 && c[t] == n - r + t) t--;
-                if (t < 0) break;
-                c[t]++;
-                for (int u = t + 1; u < r; u++) c[u] = c[u - 1] + 1;
-            }
-        }
-        off += cnt;
-    }
-    ball_off[R + 1] = off;
 }
 
 }  // namespace
@@ -457,33 +444,43 @@ int cov_verify(int32_t q, int32_t n, int32_t R, const uint8_t *code, int32_t M, 
 int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code, int32_t M, uint16_t *d_cnt,
                   void *stream)
 {
-    DtGeom g;
-    int rc = geom(q, n, g);
+    DtGeom dg;
+    int rc = geom(q, n, dg);
     if (rc) return rc;
     if (R < 0 || M < 0 || M > 65535 || (M > 0 && !d_code) || !d_cnt) return COV_EINVAL;
     if (R > n) R = n;
     cudaStream_t st = (cudaStream_t)stream;
-    CovSlot d;
-    memset(&d, 0, sizeof d);
-    d.q = q; d.n = n; d.R = R; d.M = M; d.N = g.N;
-    for (int j = 0; j < n; j++) d.pw[j] = g.pw[n - 1 - j];
-    d.rs = R ? R : 1;
-    for (int k = 0; k <= COV_MAXN; k++) d.ppow[k] = (uint32_t)std::min<long long>(ipw(q - 1, k), 0xffffffffLL);
-    std::vector<uint8_t> balls;
-    build_ball_tables(n, R, d.rs, balls, d.ball_off);
-    uint8_t *d_b = nullptr;
-    CK(cudaMallocAsync(&d_b, std::max<size_t>(balls.size(), 1), st));
-    CK(cudaMemcpyAsync(d_b, balls.data(), balls.size(), cudaMemcpyHostToDevice, st));
-    d.ball_sub = d_b;
-    // the uint16 array is updated in aligned 32-bit pairs: pad to even
-    CK(cudaMemsetAsync(d_cnt, 0, (size_t)g.N * 2, st));
+    if (!g_ct_attr) {
+        CK(cudaFuncSetAttribute(k_count_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bt_smem_bytes(BT_MAX)));
+        g_ct_attr = 1;
+    }
+    CountGeom g;
+    memset(&g, 0, sizeof g);
+    g.q = q; g.n = n; g.R = R; g.M = M;
+    bt_geom(q, n, &g.nh, &g.nl);
+    g.tw = (uint32_t)ipw(q, g.nl);
+    for (int j = 0; j < n; j++) g.pw[j] = dg.pw[n - 1 - j];
+    std::vector<uint8_t> last;
+    std::vector<uint64_t> items = bt_items_h(q, n, R, g.nh, g.vcum, last);
+    g.nitems = (uint32_t)items.size();
+    // one scratch allocation: the ball groups, their last positions, then
+    // the packed code
+    void *tmp = nullptr;
+    const size_t ib = items.size() * 8, lb = (last.size() + 7) / 8 * 8;
+    CK(cudaMallocAsync(&tmp, ib + lb + (size_t)std::max(M, 1) * 8, st));
+    uint64_t *d_items = (uint64_t *)tmp, *d_pk = d_items + (ib + lb) / 8;
+    CK(cudaMemcpyAsync(d_items, items.data(), ib, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_items + items.size(), last.data(), last.size(), cudaMemcpyHostToDevice, st));
     if (M > 0) {
-        k_count_balls<<<152 * 8, 256, 0, st>>>(d, d_code, M, d_cnt);
+        k_pack_code<<<std::min(1024, (M + 255) / 256), 256, 0, st>>>(d_code, M, n, d_pk);
         CK(cudaGetLastError());
     }
-    // balls is host memory: wait before it goes out of scope
+    k_count_tiles<<<(unsigned)ipw(q, g.nh), BT_NT, bt_smem_bytes(g.tw), st>>>(g, d_pk, d_items, d_cnt, nullptr);
+    CK(cudaGetLastError());
+    // items is pageable host memory: wait before it goes out of scope
     CK(cudaStreamSynchronize(st));
-    CK(cudaFreeAsync(d_b, st));
+    CK(cudaFreeAsync(tmp, st));
     return COV_OK;
 }
 
