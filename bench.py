@@ -358,7 +358,10 @@ def gpu_bench(args, rank, world, dist):
             if dist:
                 dist.barrier()
             a0.record(hs)
-            b.run_async(graph=True)
+            if args.cell_segment:
+                b.run(segment=args.cell_segment)
+            else:
+                b.run_async(graph=True)
             a1.record(hs)
             hs.synchronize()
             hms = a0.elapsed_time(a1)
@@ -369,7 +372,10 @@ def gpu_bench(args, rank, world, dist):
         hms_max, hmoves_all = replicas.combine(dist, hms, hmoves, device=dev)
         hetero = dict(value=hmoves_all / (hms_max / 1e3), unit="moves/s", cells=len(cells) * world,
                       moves_per_cell=args.cell_moves, ms=hms_max, clusters=plan, plan_estimate_s=est,
-                      tune_s=t_tune, launches="one graph: one persistent kernel per cluster size")
+                      tune_s=t_tune,
+                      launches=("launches of %d moves, clusters widened between them while SMs are spare"
+                                % args.cell_segment) if args.cell_segment else
+                      "one graph: one persistent kernel per cluster size")
 
     # ---------------- serving: Poisson arrivals, continuous batching
     served = None
@@ -415,6 +421,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--cells", type=int, default=256, help="heterogeneous cells per GPU")
     ap.add_argument("--cell-moves", type=int, default=20000)
+    ap.add_argument("--cell-segment", type=int, default=2000,
+                    help="moves per launch of the uneven-cells batch (0: the whole batch as one graph)")
     ap.add_argument("--requests", type=int, default=100, help="served requests per GPU")
     ap.add_argument("--lam", type=float, default=100.0, help="request arrival rate per GPU (1/s)")
     ap.add_argument("--serve-chunk", type=int, default=256)

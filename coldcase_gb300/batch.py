@@ -141,6 +141,30 @@ class Tuner:
         return choice, best
 
 
+def elastic_clusters(base, work, ctas=RESIDENT_CTAS):
+    """Cluster size per instance: its base size, doubled round by round for
+    the instances with the most work per move while the total stays within
+    `ctas` resident CTAs (at most 16 per instance)."""
+    want = dict(base)
+    used = sum(want.values())
+    order = sorted(want, key=lambda s: -work[s])
+    grown = True
+    while grown:
+        grown = False
+        for s in order:
+            c = want[s]
+            if c < 16 and used + c <= ctas:
+                want[s] = 2 * c
+                used += c
+                grown = True
+    return want
+
+
+def work_per_move(q, n, R):
+    """S' = C(n-1,R)(q-1)^R, the patterns of one commit."""
+    return math.comb(n - 1, R) * (q - 1) ** R if R <= n - 1 else 1
+
+
 class Batch:
     """Many instances in one pool; each runs exactly its own move budget.
 
@@ -174,9 +198,31 @@ class Batch:
         else:
             self.pool.run_async(self.max_moves)
 
-    def run(self, graph=True):
-        self.run_async(graph)
-        self.pool.sync()
+    def run(self, graph=True, segment=None):
+        """Run every instance to its budget.  With `segment` moves, the batch
+        runs in launches of that many moves and, between them, the clusters
+        of the instances still running are widened while SMs are spare
+        (elastic_clusters) -- small cells finish early and their SMs go to
+        the large ones."""
+        if not segment:
+            self.run_async(graph)
+            self.pool.sync()
+            return
+        base = dict(zip(self.slots, self.cluster_of))
+        cur = dict(base)
+        work = {s: work_per_move(sp["q"], sp["n"], sp["R"]) for s, sp in zip(self.slots, self.specs)}
+        while True:
+            st = self.pool.status_all(max(self.slots) + 1)
+            live = [s for s, sp in zip(self.slots, self.specs)
+                    if st[s]["it"] < sp["moves"] and not st[s]["finished"] and st[s]["status"] == 0]
+            if not live:
+                return
+            want = elastic_clusters({s: base[s] for s in live}, work)
+            for s in live:
+                if want[s] != cur[s]:
+                    self.pool.set_slot_param(s, "cluster", want[s])
+                    cur[s] = want[s]
+            self.pool.run(segment)
 
     def results(self):
         st = self.pool.status_all(max(self.slots) + 1 if self.slots else 0)

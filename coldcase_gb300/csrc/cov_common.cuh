@@ -103,6 +103,8 @@ struct CovSlot {
     uint32_t *ul_idx;            // [ul_cap] uncovered-list word indices
     uint64_t *ul_pk;             // [ul_cap] their packed digits
     uint32_t *ul_bit;            // [ceil(N/32)] list membership
+    uint32_t *zb;                // [ceil(N/32)] bit x set iff cnt[x] == 0 (kept when zbits)
+    int zbits;                   // dense coverage: the entering walk reads zb, not the counts
     int ul_cap;
     const uint8_t *sub;          // [n][nsub][rs]
     const uint8_t *sub1;         // [n][nsub1][rs]: (R-1)-subsets avoiding one position

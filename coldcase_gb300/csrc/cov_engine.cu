@@ -561,6 +561,16 @@ __device__ __forceinline__ void ul_insert(const CovSlot &d, int ul_valid, uint32
     }
 }
 
+// the uncovered-word bitmap of dense slots, kept with every 0 <-> 1 crossing
+__device__ __forceinline__ void zb_set(const CovSlot &d, uint32_t w)
+{
+    if (d.zbits) atomicOr(&d.zb[w >> 5], 1u << (w & 31));
+}
+__device__ __forceinline__ void zb_clear(const CovSlot &d, uint32_t w)
+{
+    if (d.zbits) atomicAnd(&d.zb[w >> 5], ~(1u << (w & 31)));
+}
+
 // word w loses coverage by codeword i (leaving side of a commit / -1 ball);
 // o is the word's counter as loaded
 __device__ __forceinline__ long long word_dec_v(const CovSlot &d, int ul_valid, int i, uint32_t w,
@@ -570,7 +580,7 @@ __device__ __forceinline__ long long word_dec_v(const CovSlot &d, int ul_valid, 
     if (c == 0) { set_error(d, COV_EDRIFT); return 0; }
     uint32_t nw = o - cov_cw_unit(i);
     cov_stcg(&d.cw[w], nw);
-    if (c == 1) { ul_insert(d, ul_valid, w, pk); return 1; }
+    if (c == 1) { ul_insert(d, ul_valid, w, pk); zb_set(d, w); return 1; }
     if (c == 2) private_adjust(d, (int)(nw >> 16), pk, +1, t);
     return 0;
 }
@@ -583,7 +593,7 @@ __device__ __forceinline__ long long word_inc_v(const CovSlot &d, int i, uint32_
     if (c == 0xffffu) { set_error(d, COV_EDRIFT); return 0; }
     uint32_t nw = o + cov_cw_unit(i);
     cov_stcg(&d.cw[w], nw);
-    if (c == 0) return -1;
+    if (c == 0) { zb_clear(d, w); return -1; }
     if (c == 1) private_adjust(d, (int)(o >> 16), pk, -1, t);
     return 0;
 }
@@ -754,9 +764,9 @@ __device__ __forceinline__ void commit_pairs_warp(const CovSlot &d, const OpPara
                         const uint32_t n1 = o1 - unit;
                         cov_stcg(&d.cw[a], n1);
                         cov_stcg(&d.cw[a + P.dv], o2 + unit);
-                        if (c1 == 1) { ul_insert(d, P.ul_valid, a, pka); dunc += 1; }
+                        if (c1 == 1) { ul_insert(d, P.ul_valid, a, pka); zb_set(d, a); dunc += 1; }
                         else if (c1 == 2) { evd = true; kd = (int)(n1 >> 16); }
-                        if (c2 == 0) dunc -= 1;
+                        if (c2 == 0) { zb_clear(d, a + P.dv); dunc -= 1; }
                         else if (c2 == 1) { evi = true; ki = (int)(o2 >> 16); }
                     }
                 }
@@ -969,17 +979,32 @@ __device__ void op_negwalk(const CovSlot &d, const OpParams &P, Smem &S, Smem *L
     const unsigned long long per_l = (unsigned long long)P.dtar * nit;
     const unsigned long long total = per_l * (unsigned long long)P.nL;
     const unsigned long long stride = (unsigned long long)csize * NT;
+    // A thread's consecutive items mostly share their (candidate, position):
+    // the item index advances incrementally and the candidate's codeword,
+    // position and word base are recomputed only when those change.
+    int l = -1, pi = 0, p = 0;
+    uint32_t tt = 0, b0 = 0;
+    uint64_t pc2 = 0;
+    int cur_l = -1, cur_pi = -1;
     for (unsigned long long t = (unsigned long long)rank * NT + threadIdx.x; t < total; t += stride) {
-        int l = (int)(t / per_l);
-        unsigned long long rem = t - (unsigned long long)l * per_l;
-        int pi = (int)(rem / nit);
-        uint32_t tt = (uint32_t)(rem - (unsigned long long)pi * nit);
-        int k = P.L_sm ? (int)Lp[l] : (int)cov_ldcg(&Lp[l]);
-        uint64_t pck = cov_ldcg(&d.code[k]);
-        int p = nth_set_pos(cov_spread(pck ^ P.pu), pi);
-        int v = cov_nib(P.pu, p), c = cov_nib(pck, p);
-        uint32_t b0 = widx_pk(d, pck) + (uint32_t)((long long)(v - c) * (long long)d.pw[p]);
-        uint64_t pc2 = cov_setnib(pck, p, v);
+        if (l < 0 || (unsigned long long)tt + stride >= nit) {
+            l = (int)(t / per_l);
+            const unsigned long long rem = t - (unsigned long long)l * per_l;
+            pi = (int)(rem / nit);
+            tt = (uint32_t)(rem - (unsigned long long)pi * nit);
+        } else {
+            tt += (uint32_t)stride;
+        }
+        if (l != cur_l || pi != cur_pi) {
+            const int k = P.L_sm ? (int)Lp[l] : (int)cov_ldcg(&Lp[l]);
+            const uint64_t pck = cov_ldcg(&d.code[k]);
+            p = nth_set_pos(cov_spread(pck ^ P.pu), pi);
+            const int v = cov_nib(P.pu, p), c = cov_nib(pck, p);
+            b0 = widx_pk(d, pck) + (uint32_t)((long long)(v - c) * (long long)d.pw[p]);
+            pc2 = cov_setnib(pck, p, v);
+            cur_l = l;
+            cur_pi = pi;
+        }
         int nz = 0;
         if (R == 0) {
             nz = (cnt_of(d, b0) == 0);
@@ -993,6 +1018,34 @@ __device__ void op_negwalk(const CovSlot &d, const OpParams &P, Smem &S, Smem *L
                     uint32_t w; uint64_t pk;
                     cov_item_word(d, it, kk, w, pk);
                     nz += (cnt_of(d, w) == 0);
+                }
+            } else if (d.zbits) {
+                // dense coverage: one bit per word, the bitmap stays in L2.
+                // The item's words rise by the last position's stride; a
+                // bitmap word they share is loaded once.
+                for (int kb = 0; kb < qm1; kb += WCH) {
+                    uint32_t cv[WCH];
+                    uint32_t prev = 0xffffffffu;
+#pragma unroll
+                    for (int kc = 0; kc < WCH; kc++) {
+                        if (kb + kc < qm1) {
+                            uint32_t w; uint64_t pk;
+                            cov_item_word(d, it, kb + kc, w, pk);
+                            if ((w >> 5) != prev) cv[kc] = cov_ldcg(&d.zb[w >> 5]);
+                            prev = w >> 5;
+                        }
+                    }
+                    prev = 0xffffffffu;
+#pragma unroll
+                    for (int kc = 0; kc < WCH; kc++) {
+                        if (kb + kc < qm1) {
+                            uint32_t w; uint64_t pk;
+                            cov_item_word(d, it, kb + kc, w, pk);
+                            if ((w >> 5) == prev) cv[kc] = cv[kc - 1];
+                            prev = w >> 5;
+                            nz += (int)((cv[kc] >> (w & 31)) & 1u);
+                        }
+                    }
                 }
             } else for (int kb = 0; kb < qm1; kb += WCH) {
                 uint32_t cv[WCH];
@@ -2278,6 +2331,7 @@ __global__ void __launch_bounds__(BT_NT) k_build_state(CovSlot d, unsigned long 
                     d.ul_pk[at] = pk;
                     atomicOr(&d.ul_bit[gx >> 5], 1u << (gx & 31));
                 }
+                if (d.zbits) atomicOr(&d.zb[gx >> 5], 1u << (gx & 31));
             }
         }
         z += zero;
@@ -2673,6 +2727,7 @@ size_t cov_slot_bytes(const cov_params *prm)
     add((size_t)UL_CAP_DEFAULT * 4);                 // ul_idx
     add((size_t)UL_CAP_DEFAULT * 8);                 // ul_pk
     add((size_t)((N + 31) / 32) * 4);                // ul_bit
+    add((size_t)((N + 31) / 32) * 4);                // zb
     add((size_t)M * n * 4 * 3 + (size_t)M * 4);      // g_perm, g_dval, g_neg, g_list
     add(65536);                                      // subset tables
     {
@@ -2723,6 +2778,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.neg_cluster_pairs = pool->neg_cluster_pairs;
     d.list_cost = pool->list_cost;
     d.padj_warp = padj_auto(q, n, R, M);
+    d.zbits = d.padj_warp;
     std::vector<uint8_t> subs((size_t)n * std::max(d.nsub, 1) * d.rs, 0);
     for (int p = 0; p < n; p++) {
         int pool_[32], np = 0;
@@ -2767,6 +2823,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.ul_idx = (uint32_t *)take_((size_t)d.ul_cap * 4);
     d.ul_pk = (uint64_t *)take_((size_t)d.ul_cap * 8);
     d.ul_bit = (uint32_t *)take_((size_t)((N + 31) / 32) * 4);
+    d.zb = (uint32_t *)take_((size_t)((N + 31) / 32) * 4);
     d.g_perm = (uint32_t *)take_((size_t)Mw * n * 4);
     d.g_dval = (int32_t *)take_((size_t)Mw * n * 4);
     d.g_neg = (int32_t *)take_((size_t)Mw * n * 4);
@@ -2914,6 +2971,7 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
     CK(cudaMemsetAsync(d_z, 0, 16, st));
     CK(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
     CK(cudaMemsetAsync(d.ul_bit, 0, (size_t)((N + 31) / 32) * 4, st));
+    CK(cudaMemsetAsync(d.zb, 0, (size_t)((N + 31) / 32) * 4, st));
     k_build_state<<<(unsigned)ipow_h(q, d.bt_nh), BT_NT, bt_smem_bytes(d.bt_tw), st>>>(d, d_z);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(d.best, d.code, (size_t)M * 8, cudaMemcpyDeviceToDevice, st));

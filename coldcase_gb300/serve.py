@@ -31,7 +31,7 @@ import time
 import numpy as np
 
 from . import verify
-from .batch import RESIDENT_CTAS, size_class
+from .batch import RESIDENT_CTAS, elastic_clusters, size_class
 from .engine import Pool, device_memory, slot_bytes
 from .workloads import uniform_code
 
@@ -50,25 +50,6 @@ def default_cluster(q, n, R, M):
 
 def _work_per_move(r):
     return math.comb(r["n"] - 1, r["R"]) * (r["q"] - 1) ** r["R"] if r["R"] <= r["n"] - 1 else 1
-
-
-def elastic_clusters(base, work, ctas):
-    """Cluster size per request: its base size, doubled round by round for
-    the requests with the most work per move while the total stays within
-    `ctas` resident CTAs (at most 16 per request)."""
-    want = dict(base)
-    used = sum(want.values())
-    order = sorted(want, key=lambda s: -work[s])
-    grown = True
-    while grown:
-        grown = False
-        for s in order:
-            c = want[s]
-            if c < 16 and used + c <= ctas:
-                want[s] = 2 * c
-                used += c
-                grown = True
-    return want
 
 
 class Server:

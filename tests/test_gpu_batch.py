@@ -24,6 +24,10 @@ CELLS = [  # q, n, R, M, moves, tabu
     (7, 6, 2, 300, 450, 5),
     (4, 8, 3, 30, 800, 0),
     (6, 7, 1, 7000, 250, 0),
+    # dense coverage (M = 1.3 q^n / |B|): warp-aggregated commit and the
+    # uncovered-word bitmap walk
+    (6, 7, 4, 14, 600, 0),
+    (7, 8, 3, 570, 300, 0),
 ]
 
 
@@ -126,3 +130,15 @@ def test_admission_by_device_bytes(covlib):
     assert rep["requests"] == len(reqs)
     assert max(p[1] for p in peak) <= budget
     assert max(p[0] for p in peak) >= 2
+
+
+def test_batch_segmented_elastic_bit_exact(covlib):
+    """Segments with clusters re-widened between them give the same results."""
+    sp = specs()
+    with Batch(sp, clusters=1) as b:
+        b.run(segment=173)
+        res = b.results()
+        for i, s in enumerate(sp):
+            o, tr = oracle_of(s["q"], s["n"], s["R"], s["M"], s["moves"], s["tabu"], s["seed"])
+            assert res[i]["iters"] == o.iters() and res[i]["uncovered"] == o.best_uncovered(), (s, res[i])
+            assert (b.best(i) == o.best()).all(), s

@@ -4,7 +4,8 @@ import math
 
 from coldcase_gb300 import workloads
 from coldcase_gb300.batch import Tuner, size_class
-from coldcase_gb300.serve import default_cluster, elastic_clusters
+from coldcase_gb300.batch import elastic_clusters
+from coldcase_gb300.serve import default_cluster
 
 
 def test_hetero_cells_domain():
