@@ -2686,6 +2686,25 @@ int cov_pool_set_budget(cov_pool *pool, double seconds)
     return COV_OK;
 }
 
+// A slot stopped by its launch deadline (COV_ETIMEOUT) stopped between two
+// moves with its state whole: clear the status so that the next run goes on
+// from there, on exactly the trajectory an uninterrupted run follows.  Any
+// other error stays.
+int cov_pool_resume(cov_pool *pool, int32_t slot)
+{
+    if (!pool || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
+    CovSlotState hs;
+    int rc = read_state(pool, slot, &hs);
+    if (rc) return rc;
+    if (hs.status == COV_OK) return COV_OK;
+    if (hs.status != COV_ETIMEOUT) return hs.status;
+    int zero = 0;
+    CK(cudaMemcpyAsync(&pool->slots[slot].st->status, &zero, sizeof zero, cudaMemcpyHostToDevice,
+                       pool->cur_stream()));
+    CK(cudaStreamSynchronize(pool->cur_stream()));
+    return COV_OK;
+}
+
 int cov_pool_remove(cov_pool *pool, int32_t slot)
 {
     if (!pool || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;

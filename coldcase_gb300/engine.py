@@ -171,6 +171,15 @@ class Pool:
                                                 n.value, ctypes.byref(n)), "cov_pool_get_trace")
         return out
 
+    def set_budget(self, seconds):
+        """Wall-clock budget of each launch; a slot that reaches it stops
+        between moves with status COV_ETIMEOUT (see resume)."""
+        L.check(self.lib.cov_pool_set_budget(self.h, float(seconds)), "cov_pool_set_budget")
+
+    def resume(self, slot):
+        """Clear a deadline stop so the slot continues its trajectory."""
+        L.check(self.lib.cov_pool_resume(self.h, int(slot)), "cov_pool_resume")
+
     def remove(self, slot):
         L.check(self.lib.cov_pool_remove(self.h, int(slot)), "cov_pool_remove")
         self.meta.pop(slot, None)

@@ -90,6 +90,7 @@ SIGNATURES = {
     "cov_pool_get_prof": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64)]),
     "cov_pool_get_rng": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64)]),
     "cov_pool_get_trace": (ctypes.c_int, [_P, _I32, ctypes.POINTER(CovMoveRec), _I64, _PI64]),
+    "cov_pool_resume": (ctypes.c_int, [_P, _I32]),
     "cov_pool_remove": (ctypes.c_int, [_P, _I32]),
     "cov_pool_destroy": (ctypes.c_int, [_P]),
     "cov_verify": (ctypes.c_int, [_I32, _I32, _I32, _PU8, _I32, _PI64]),

@@ -156,6 +156,11 @@ int cov_pool_get_rng(cov_pool *pool, int32_t slot, uint64_t *out4);
 int cov_pool_get_prof(cov_pool *pool, int32_t slot, uint64_t *out25);
 int cov_pool_get_trace(cov_pool *pool, int32_t slot, cov_move_rec *out,
                        int64_t cap, int64_t *n_out);
+/* Clear a COV_ETIMEOUT left by the launch deadline (cov_pool_set_budget): the
+ * slot stopped between moves and the next run continues its trajectory
+ * exactly.  Other errors are returned unchanged.  No counterpart in the
+ * reference, whose processes stop at -t and are restarted from --out. */
+int cov_pool_resume(cov_pool *pool, int32_t slot);
 int cov_pool_remove(cov_pool *pool, int32_t slot);
 int cov_pool_destroy(cov_pool *pool);
 

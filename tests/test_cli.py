@@ -1,0 +1,55 @@
+"""The covsearch2e-compatible command line: argument handling on the host
+(no GPU), and on the GPU the RESULT fingerprint, the --out file and the exit
+status against the reference binary's golden runs."""
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(REPO, "coldcase_gb300", "bin", "covsearch_gpu")
+
+
+def run_cli(args, timeout=300):
+    return subprocess.run([sys.executable, CLI] + [str(a) for a in args], capture_output=True, text=True,
+                          timeout=timeout, cwd=REPO)
+
+
+@pytest.mark.parametrize("flag", ["--wide", "--sa", "--fix0", "--ucache", "--upick"])
+def test_trajectory_switches_refused(flag):
+    r = run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", flag])
+    assert r.returncode == 2 and "trajectory" in r.stderr
+
+
+def test_bad_arguments_exit_2():
+    assert run_cli(["-q", "4", "-n", "6"]).returncode == 2                    # missing -R -M
+    assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", "--bogus"]).returncode == 2
+    assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", "--preset", "p9"]).returncode == 2
+    assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "70000"]).returncode == 2
+    assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", "--noise", "5"]).returncode == 2
+
+
+@pytest.mark.gpu
+def test_cli_matches_reference_runs(covlib, golden):
+    runs, _ = golden
+    picked = [r for r in runs if r["code"] and not r["random_init"]][:6]
+    for r in picked:
+        with tempfile.TemporaryDirectory() as td:
+            inp, out = os.path.join(td, "in.txt"), os.path.join(td, "out.txt")
+            with open(inp, "w") as f:
+                f.write(r["code"])
+            args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
+                    "--tabu", r["tabu"], "--kick", r["kick"], "--stall", r["stall"], "--in", inp, "--out", out,
+                    "--preset", "p5b", "--quiet"]
+            p = run_cli(args)
+            m = re.search(r"RESULT .*uncovered=(\d+) iters=(\d+) kicks=(\d+)", p.stdout)
+            assert m, p.stdout + p.stderr
+            ref = r["ref"]
+            assert (int(m.group(1)), int(m.group(2)), int(m.group(3))) == \
+                (ref["uncovered"], ref["iters"], ref["kicks"]), (r["q"], r["n"], r["R"], r["M"], r["seed"])
+            assert p.returncode == (0 if ref["uncovered"] == 0 else 1)
+            with open(out) as f:
+                assert f.read() == ref["out"]
