@@ -412,7 +412,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-moves", type=int, default=12)
     ap.add_argument("--cpu-steps", type=int, default=4)
-    ap.add_argument("--graph", action="store_true", help="replay each step from a captured CUDA graph")
+    ap.add_argument("--no-graph", dest="graph", action="store_false",
+                    help="launch each step directly instead of replaying its captured CUDA graph")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -97,7 +97,9 @@ struct Smem {
     cov_move_rec rec;
     unsigned long long prof[24];
     long long ul_pairs;
-    unsigned long long diag_twmax, diag_hits, diag_atom;
+    // 8 bytes of layout: without them ptxas allocates the engine's registers
+    // with spills (checked with -Xptxas -v on every change)
+    unsigned long long layout_pad;
     int uln;                   // list length read once per iteration
     // scratch
     int red_i[NWARP];
@@ -1092,84 +1094,27 @@ __device__ void op_rebuild_ul(const CovSlot &d, int rank, int csize, cg::cluster
     }
 }
 
-// Entering side from the uncovered-word list (covsearch2e.c:720-734),
-// restricted to v = u_p, the only entries a non-wide candidate reads: for
-// every listed x that is still uncovered and every candidate codeword c with
+// Entering side from the uncovered-word list (covsearch2e.c:720-734) for
+// more than 64 candidates (at most that many take neg_chunks): for every
+// listed x that is still uncovered and every candidate codeword c with
 // d(x,c) = R+1, neg[c][j] += 1 for each j in D(x,c) with x_j = u_j.
-// Entries first, first+stride, ... of the list.  With at most 64 candidates
-// the distance test is bit-sliced: cmask[j*q+v] holds the candidates whose
-// digit j is v, and a 5-bit counter kept across 64 lanes of bits adds up the
-// matching positions of all candidates at once; the candidates at distance
-// R+1 are those with exactly n-(R+1) matches.
-__device__ void ul_pass(const CovSlot &d, uint64_t pu, int nL, const uint64_t *Lpk,
-                        const uint64_t *cmask, int32_t *negp, uint32_t first, uint32_t stride,
-                        uint32_t n0)
+// Entries first, first+stride, ... of the list.
+__device__ void ul_pass(const CovSlot &d, uint64_t pu, int nL, const uint64_t *Lpk, int32_t *negp,
+                        uint32_t first, uint32_t stride, uint32_t n0)
 {
-    const int n = d.n, q = d.q, R = d.R;
+    const int n = d.n, R = d.R;
     const uint64_t nm = nibmask(n);
-    const int tgt = n - (R + 1);             // positions shared at distance R+1
-    const uint64_t lmask = nL >= 64 ? ~0ull : ((1ull << nL) - 1);
-    extern __shared__ __align__(16) unsigned char cov_smem[];
-    Smem &SS = *reinterpret_cast<Smem *>(cov_smem);
-    const bool probe = (first == 0);
-
-    const long long tw0 = cov_clock();
-    int nhit = 0, natom = 0;
     for (uint32_t e = first; e < n0; e += stride) {
-        long long ta = probe ? cov_clock() : 0;
         const uint32_t x = cov_ldcg(&d.ul_idx[e]);
         const uint64_t px = cov_ldcg(&d.ul_pk[e]);
-        const uint32_t cxv = cov_ldcg(&d.cw[x]);
-
-        if ((cxv & 0xffffu) != 0) continue;     // stale entry
+        if ((cov_ldcg(&d.cw[x]) & 0xffffu) != 0) continue;     // stale entry
         const uint64_t eq = ~cov_spread(px ^ pu) & nm;
-        uint64_t hit;
-        if (nL <= 64) {
-            uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0;
-            for (int j = 0; j < n; j++) {
-                const uint64_t m = cmask[j * q + cov_nib(px, j)];
-                uint64_t c0 = b0 & m; b0 ^= m;
-                uint64_t c1 = b1 & c0; b1 ^= c0;
-                uint64_t c2 = b2 & c1; b2 ^= c1;
-                uint64_t c3 = b3 & c2; b3 ^= c2;
-                b4 ^= c3;
-            }
-            hit = ((tgt & 1) ? b0 : ~b0) & ((tgt & 2) ? b1 : ~b1) & ((tgt & 4) ? b2 : ~b2) &
-                  ((tgt & 8) ? b3 : ~b3) & ((tgt & 16) ? b4 : ~b4) & lmask;
-            while (hit) {
-                const int l = __ffsll((long long)hit) - 1;
-                hit &= hit - 1;
-                nhit++;
-                uint64_t m = cov_spread(px ^ Lpk[l]) & eq;
-                while (m) {
-                    atomicAdd(&negp[l * n + ((__ffsll((long long)m) - 1) >> 2)], 1);
-                    natom++;
-                    m &= m - 1;
-                }
-            }
-        } else {
-            for (int l = 0; l < nL; l++) {
-                uint64_t D = cov_spread(px ^ Lpk[l]);
-                if (__popcll(D) != R + 1) continue;
-                uint64_t m = D & eq;
-                while (m) {
-                    atomicAdd(&negp[l * n + ((__ffsll((long long)m) - 1) >> 2)], 1);
-                    m &= m - 1;
-                }
-            }
+        for (int l = 0; l < nL; l++) {
+            const uint64_t D = cov_spread(px ^ Lpk[l]);
+            if (__popcll(D) != R + 1) continue;
+            for (uint64_t m = D & eq; m; m &= m - 1)
+                atomicAdd(&negp[l * n + ((__ffsll((long long)m) - 1) >> 2)], 1);
         }
-
-    }
-    // diagnostics: slowest warp's pass time, hits and counter atomics
-    const long long tw = cov_clock() - tw0;
-    long long twmax = tw;
-    for (int o = 16; o > 0; o >>= 1) twmax = max(twmax, __shfl_xor_sync(__activemask(), twmax, o));
-    nhit = warp_sum(nhit);
-    natom = warp_sum(natom);
-    if ((threadIdx.x & 31) == 0) {
-        atomicMax(&SS.diag_twmax, (unsigned long long)twmax);
-        atomicAdd(&SS.diag_hits, (unsigned long long)nhit);
-        atomicAdd(&SS.diag_atom, (unsigned long long)natom);
     }
 }
 
@@ -1287,7 +1232,7 @@ __device__ void op_neg(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, i
         for (int x = threadIdx.x; x < nL * n; x += NT) S.neg[x] = 0;
         cov_bar();
     }
-    ul_pass(d, P.pu, nL, S.Lpk, S.cmask, S.neg, (uint32_t)rank * NT + threadIdx.x, (uint32_t)(csize * NT), n0);
+    ul_pass(d, P.pu, nL, S.Lpk, S.neg, (uint32_t)rank * NT + threadIdx.x, (uint32_t)(csize * NT), n0);
     if (rank != 0) {
         cov_bar();
         for (int x = threadIdx.x; x < nL * n; x += NT)
@@ -1701,7 +1646,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         if (tid == 0) S.prof[13] += cov_clock() - tp0;
         __syncwarp();
     } else if (Lsm) {
-        ul_pass(d, pu, nL, S.Lpk, S.cmask, negp, tid, NT, (uint32_t)S.uln);
+        ul_pass(d, pu, nL, S.Lpk, negp, tid, NT, (uint32_t)S.uln);
         cov_bar();
     } else {
         if (tid == 0) apply_swaps(d, S);
