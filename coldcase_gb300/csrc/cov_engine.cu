@@ -1119,13 +1119,16 @@ __device__ void ul_pass(const CovSlot &d, uint64_t pu, int nL, const uint64_t *L
 }
 
 // The entering side for at most 64 candidates, without atomics.  The list
-// entries [e0, e1) are taken in chunks: every thread stages, for its
-// entries, the bit-sliced mask of candidates at distance R+1 (H) and the
-// positions where the entry equals the sampled word u (E).  Then each warp
-// owns whole candidates: for candidate l, neg[l][j] counts the staged
-// entries with l in H and j in E, for j among the positions where c_l
-// differs from u (exactly the j in D(x,c_l) with x_j = u_j).  Lane-private
-// byte counters are reduced over the warp; each counter has one writer.
+// entries [e0, e1) are taken in chunks of ULS, as groups of 32 (one per
+// lane of a warp).  For each group a warp records, by ballot, which of its
+// entries each candidate hits at distance R+1 (LM[l]) and which equal the
+// sampled word u at each position (EJ[j]); stale entries (covered again) hit
+// nothing.  For candidate l and a position j where c_l differs from u,
+// neg[l][j] then gains popc(LM[l] & EJ[j]) over the groups: exactly the
+// entries x with d(x,c_l) = R+1, j in D(x,c_l) and x_j = u_j.  Each thread
+// owns fixed (l, j) pairs and keeps their sums in registers until the end.
+// The masks live in st_H/st_E, rows XOR-swizzled by group so that threads
+// reading different rows hit different banks.
 __device__ void neg_chunks(const CovSlot &d, Smem &S, uint64_t pu, int nL, uint32_t e0, uint32_t e1,
                            int32_t *negp)
 {
@@ -1134,13 +1137,20 @@ __device__ void neg_chunks(const CovSlot &d, Smem &S, uint64_t pu, int nL, uint3
     const uint64_t nm = nibmask(n);
     const int tgt = n - (R + 1);
     const uint64_t lmask = nL >= 64 ? ~0ull : ((1ull << nL) - 1);
+    constexpr int NG = ULS / 32;                       // groups per chunk (32)
+    uint32_t *LM = reinterpret_cast<uint32_t *>(S.st_H);   // [64][NG]
+    uint32_t *EJ = reinterpret_cast<uint32_t *>(S.st_E);   // [16][NG]
+    const int npair = nL * n;
+    int acc0 = 0, acc1 = 0;                            // pairs threadIdx.x and threadIdx.x + NT
     for (uint32_t c0 = e0; c0 < e1; c0 += ULS) {
         const int cnt = (int)min((uint32_t)ULS, e1 - c0);
-        for (int k = threadIdx.x; k < cnt; k += NT) {
-            const uint32_t e = c0 + (uint32_t)k;
-            const uint64_t px = cov_ldcg(&d.ul_pk[e]);
-            uint64_t hit = 0;
-            {
+        const int ng = (cnt + 31) >> 5;
+        for (int g = warp; g < ng; g += NWARP) {
+            const int k = g * 32 + lane;
+            const bool valid = k < cnt;
+            uint64_t px = 0, hit = 0;
+            if (valid) {
+                px = cov_ldcg(&d.ul_pk[c0 + (uint32_t)k]);
                 uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0;
                 for (int j = 0; j < n; j++) {
                     const uint64_t m = S.cmask[j * q + cov_nib(px, j)];
@@ -1152,41 +1162,37 @@ __device__ void neg_chunks(const CovSlot &d, Smem &S, uint64_t pu, int nL, uint3
                 }
                 hit = ((tgt & 1) ? b0 : ~b0) & ((tgt & 2) ? b1 : ~b1) & ((tgt & 4) ? b2 : ~b2) &
                       ((tgt & 8) ? b3 : ~b3) & ((tgt & 16) ? b4 : ~b4) & lmask;
+                // the count is read only for entries some candidate hits
+                if (hit && (cov_ldcg(&d.cw[cov_ldcg(&d.ul_idx[c0 + (uint32_t)k])]) & 0xffffu) != 0) hit = 0;
             }
-            const uint64_t eq = ~cov_spread(px ^ pu) & nm;
-            uint32_t E = 0;
-            for (uint64_t m = eq; m; m &= m - 1) E |= 1u << ((__ffsll((long long)m) - 1) >> 2);
-            S.st_H[k] = hit;
-            S.st_E[k] = (uint16_t)E;
+            const uint64_t eq = valid ? (~cov_spread(px ^ pu) & nm) : 0ull;
+            for (int l = 0; l < nL; l++) {
+                const uint32_t m = __ballot_sync(0xffffffffu, (hit >> l) & 1ull);
+                if (lane == 0) LM[l * NG + (g ^ (l & (NG - 1)))] = m;
+            }
+            for (int j = 0; j < n; j++) {
+                const uint32_t m = __ballot_sync(0xffffffffu, (eq >> (4 * j)) & 1ull);
+                if (lane == 0) EJ[j * NG + (g ^ (j & (NG - 1)))] = m;
+            }
         }
         cov_bar();
-        // entries some candidate hits: drop the stale ones (word covered
-        // again) -- the count is read for these few entries only
-        for (int k = threadIdx.x; k < cnt; k += NT) {
-            if (S.st_H[k] && (cov_ldcg(&d.cw[cov_ldcg(&d.ul_idx[c0 + (uint32_t)k])]) & 0xffffu) != 0)
-                S.st_H[k] = 0;
-        }
-        cov_bar();
-        for (int l = warp; l < nL; l += NWARP) {
-            const uint32_t Pl = S.Pmask[l];
-            uint64_t lo = 0, hi = 0;
-            for (int k = lane; k < cnt; k += 32) {
-                if (!((S.st_H[k] >> l) & 1)) continue;
-                for (uint32_t m = S.st_E[k] & Pl; m; m &= m - 1) {
-                    const int j = __ffs(m) - 1;
-                    if (j < 8) lo += 1ull << (8 * j);
-                    else hi += 1ull << (8 * (j - 8));
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int t = (int)threadIdx.x + u * NT;
+            if (t < npair) {
+                const int l = t / n, j = t - l * n;
+                if ((S.Pmask[l] >> j) & 1) {
+                    int sum = 0;
+                    for (int g = 0; g < ng; g++)
+                        sum += __popc(LM[l * NG + (g ^ (l & (NG - 1)))] & EJ[j * NG + (g ^ (j & (NG - 1)))]);
+                    if (u == 0) acc0 += sum; else acc1 += sum;
                 }
-            }
-            for (uint32_t m = Pl; m; m &= m - 1) {
-                const int j = __ffs(m) - 1;
-                int v = (int)(((j < 8) ? (lo >> (8 * j)) : (hi >> (8 * (j - 8)))) & 255u);
-                v = warp_sum(v);
-                if (lane == 0 && v) atomicAdd(&negp[l * n + j], v);
             }
         }
         cov_bar();
     }
+    if (acc0) atomicAdd(&negp[threadIdx.x], acc0);
+    if (acc1) atomicAdd(&negp[threadIdx.x + NT], acc1);
 }
 
 // candidate mask table for the bit-sliced list pass (nL <= 64)
