@@ -97,9 +97,6 @@ struct Smem {
     cov_move_rec rec;
     unsigned long long prof[24];
     long long ul_pairs;
-    // 8 bytes of layout: without them ptxas allocates the engine's registers
-    // with spills (checked with -Xptxas -v on every change)
-    unsigned long long layout_pad;
     int uln;                   // list length read once per iteration
     // scratch
     int red_i[NWARP];
@@ -1275,7 +1272,10 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
     if (tid == 0) S.rs_use += consumed;
     __syncwarp();
     if (first >= 0 || S.unc <= 0) return result;     // no zero anywhere: -1
-    if (S.ul_valid) {
+    // Both searches below return the first zero after start.  The list is
+    // scanned whole; the linear scan stops at the first zero, about q^n/unc
+    // words on: it is the cheaper one while that distance is short.
+    if (S.ul_valid && (unsigned long long)S.unc * 16384ull < (unsigned long long)d.N) {
         // every zero-count word is on the list: the first one after start is
         // the entry minimising (x - start) mod N
         // a thread reads the count only for an entry that would lower its
