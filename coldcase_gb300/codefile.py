@@ -13,8 +13,11 @@ separated by spaces, commas or tabs for q > 36.  '#' starts a comment.
                    renamed into place.
 """
 import os
+import re
 
 import numpy as np
+
+_LEADING_INT = re.compile(r"[+-]?\d+")
 
 DIGITS = "0123456789abcdefghijklmnopqrstuvwxyz"
 _DIGVAL = {c: i for i, c in enumerate(DIGITS)}
@@ -43,12 +46,12 @@ def read_code(path, n):
             line = line.split("#")[0]
             if any(ch in line for ch in " ,\t"):
                 toks = [t for t in line.replace(",", " ").replace("\t", " ").split() if t]
+                # atoi: the leading integer of the token (0 if none), then
+                # the uint8_t cast of the reader (modulo 256)
                 w = []
                 for t in toks[:n]:
-                    try:
-                        w.append(int(t))
-                    except ValueError:
-                        w.append(0)
+                    m = _LEADING_INT.match(t)
+                    w.append((int(m.group(0)) if m else 0) & 0xff)
             else:
                 w = [_DIGVAL[ch] for ch in line.rstrip("\r\n") if ch in _DIGVAL][:n]
             if not w:
