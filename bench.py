@@ -305,6 +305,30 @@ def gpu_bench(args, rank, world, dist):
                      moves=pm)
         eng.close()
 
+    # ---------------- the other plain configurations (one instance each)
+    plain_cfgs = None
+    if not args.no_plain and rank == 0:
+        from coldcase_gb300 import workloads
+        plain_cfgs = {}
+        for key, w, cl, mv in (("q6n9_M700", workloads.PLAIN_GPU, 16, 2000),
+                               ("q4n6_M420", workloads.PLAIN_CPU, 1, 2000)):
+            eng = Search(w["q"], w["n"], w["R"], w["M"], seed=1, tabu=w["tabu"], cluster=cl, budget_s=120.0)
+            eng.load(uniform_code(w["q"], w["n"], w["M"], 1))
+            ps = torch.cuda.Stream(device=dev)
+            eng.pool.set_stream(ps.cuda_stream)
+            eng.pool.run(200)
+            i0 = eng.status()["it"]
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(ps)
+            eng.pool.run_async(mv)
+            b.record(ps)
+            ps.synchronize()
+            m = eng.status()["it"] - i0
+            plain_cfgs[key] = dict(value=m / (a.elapsed_time(b) / 1e3) if m else None, unit="moves/s", moves=m,
+                                   cluster=cl, workload=w["name"],
+                                   note=None if m == mv else "the search covered after %d moves" % m)
+            eng.close()
+
     # ---------------- coverage words/s: distance transform and count
     cov = None
     if rank == 0 and not args.no_cov:
@@ -395,7 +419,7 @@ def gpu_bench(args, rank, world, dist):
 
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
                 plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work, hetero=hetero,
-                served=served)
+                served=served, plain_cfgs=plain_cfgs)
 
 
 def main():
@@ -493,6 +517,7 @@ def main():
             gpu_launches=2 * args.steps,
             plain=r["plain"],
             batched_over_plain=(r["value"] / world / r["plain"]["value"]) if r["plain"] else None,
+            plain_configs=r["plain_cfgs"],
             hetero=r["hetero"],
             served=r["served"],
             served_over_plain=(r["served"]["value"] / r["plain"]["value"])
