@@ -276,6 +276,7 @@ def gpu_bench(args, rank, world, dist):
             t_run += t2 - t1
             t_read += t3 - t2
             e_moves += sum(s["it"] for s in stt)
+        e_t, e_moves = replicas.combine(dist, e_t, e_moves, device=dev)     # slowest rank, all moves
         e2e = dict(value=e_moves / e_t, unit="moves/s", h2d_bytes_per_step=h2d,
                    d2h_bytes_per_step=d2h + args.restarts * 72,
                    note="per step: %d restarts re-seeded from pinned host codes (state build included), "
@@ -414,7 +415,16 @@ def gpu_bench(args, rank, world, dist):
             if dist:
                 dist.barrier()
             rep = srv.serve(reqs)
-        served = dict(rep, lam_per_s=args.lam, unit="moves/s", value=rep["moves_per_s"], clusters=splan,
+            lat = [r["done"] - r["arrival"] for r in srv.done]
+        if dist:
+            # the whole job: every rank's requests, the slowest rank's wall time
+            lats = [None] * world
+            dist.all_gather_object(lats, lat)
+            lat = [x for part in lats for x in part]
+            wall, moves = replicas.combine(dist, rep["wall_s"], rep["moves"], device=dev)
+            rep = dict(rep, requests=len(lat), moves=int(moves), wall_s=wall, moves_per_s=moves / wall,
+                       p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)))
+        served = dict(rep, lam_per_s=args.lam * world, unit="moves/s", value=rep["moves_per_s"], clusters=splan,
                       elastic=True)
 
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,

@@ -16,8 +16,8 @@
 //     codeword's sphere is walked again.  pos_p = T_k - H_k[p] exactly as in
 //     covsearch2e.c:755-758.
 //   * the entering side (neg) is read off the uncovered-word list as in
-//     covsearch2e.c:720-734, or by the per-position walk of :735-753 while
-//     the list is not valid.
+//     covsearch2e.c:720-734, or by the per-position walk of :735-753,
+//     whichever costs less (the list while it is valid and short enough).
 //
 // Execution: one thread-block cluster per search instance ("slot").  The
 // leader CTA (rank 0) runs the serial, RNG-ordered part of each iteration;
