@@ -75,21 +75,25 @@ class Tuner:
                 self.table = {}
 
     def _save(self):
+        """Best effort: the cache only saves re-measuring."""
         if not self.cache:
             return
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
-        data = {}
-        if os.path.exists(self.path):
-            try:
-                with open(self.path) as f:
-                    data = json.load(f)
-            except (OSError, ValueError):
-                data = {}
-        data[self.dev] = self.table
-        tmp = self.path + ".tmp"
-        with open(tmp, "w") as f:
-            json.dump(data, f, indent=1, sort_keys=True)
-        os.replace(tmp, self.path)
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            data = {}
+            if os.path.exists(self.path):
+                try:
+                    with open(self.path) as f:
+                        data = json.load(f)
+                except (OSError, ValueError):
+                    data = {}
+            data[self.dev] = self.table
+            tmp = "%s.%d.tmp" % (self.path, os.getpid())
+            with open(tmp, "w") as f:
+                json.dump(data, f, indent=1, sort_keys=True)
+            os.replace(tmp, self.path)
+        except OSError:
+            pass
 
     def measure(self, key, specs):
         """Seconds per move of class `key` at every cluster size (sample of

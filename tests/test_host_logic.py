@@ -61,3 +61,17 @@ def test_elastic_clusters():
     # saturated: nothing changes
     base = {k: 1 for k in range(200)}
     assert elastic_clusters(base, {k: k for k in range(200)}, 152) == base
+
+
+def test_tuner_cache_unwritable(tmp_path, monkeypatch):
+    """An unwritable cache location does not break tuning."""
+    import os
+    from coldcase_gb300 import batch
+    ro = tmp_path / "ro"
+    ro.mkdir()
+    os.chmod(ro, 0o500)
+    monkeypatch.setenv("COLDCASE_GB300_CACHE", str(ro / "sub"))
+    t = batch.Tuner()
+    t.table["s04"] = {"1": 1e-5}
+    t._save()                       # must not raise
+    os.chmod(ro, 0o700)
