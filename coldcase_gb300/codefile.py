@@ -96,6 +96,36 @@ def parse_code(path, q, n):
     return uniq, len(words) - len(uniq)
 
 
+def read_code_finisher(path, q, n, M):
+    """covcount's reader (cov/engine/covcount.c:94-118): at most M words;
+    lines of the wrong length or with a digit >= q are skipped, not errors;
+    a missing file reads as no words."""
+    rows = []
+    try:
+        f = open(path)
+    except OSError:
+        return np.zeros((0, n), dtype=np.uint8)
+    with f:
+        for line in f:
+            if len(rows) >= M:
+                break
+            line = line.split("#")[0]
+            if any(ch in line for ch in " ,\t"):
+                toks = [t for t in line.replace(",", " ").replace("\t", " ").split() if t][:n]
+                w = []
+                for t in toks:
+                    m = _LEADING_INT.match(t)
+                    w.append((int(m.group(0)) if m else 0) & 0xff)
+            else:
+                w = [_DIGVAL[ch] for ch in line.rstrip("\r\n") if ch in _DIGVAL][:n]
+            if len(w) != n or any(v >= q for v in w):
+                continue
+            rows.append(w)
+    if not rows:
+        return np.zeros((0, n), dtype=np.uint8)
+    return np.array(rows, dtype=np.uint8)
+
+
 def word_index(code, q):
     code = np.asarray(code, dtype=np.int64)
     n = code.shape[1]

@@ -243,6 +243,149 @@ __global__ void __launch_bounds__(BT_NT) k_count_tiles(CountGeom g, const uint64
     if ((threadIdx.x & 31) == 0 && z && zeros) atomicAdd(zeros, z);
 }
 
+// ------------------------------------------------------------ finisher ----
+struct FinishGeom {
+    int q, n, R, M;
+    uint32_t N;
+    uint32_t pw[COV_MAXN];             // q^(n-1-j)
+    uint32_t ngroups;                  // ball groups of radius <= R (cov_tiles.cuh, nh = 0)
+};
+
+__device__ __forceinline__ uint64_t fin_xorshift(uint64_t r)
+{
+    r ^= r << 13;
+    r ^= r >> 7;
+    r ^= r << 17;
+    return r;
+}
+
+// +1 (saturating) over the ball of the packed word pc into cnt; all threads
+__device__ void fin_mark(const FinishGeom &g, uint16_t *cnt, uint64_t pc, const uint64_t *items,
+                         const uint8_t *last)
+{
+    uint32_t base = 0;
+    for (int j = 0; j < g.n; j++) base += (uint32_t)cov_nib(pc, j) * g.pw[j];
+    for (uint32_t it = threadIdx.x; it < g.ngroups; it += blockDim.x) {
+        uint64_t sp = items[it];
+        int off = (int)base;
+        while (sp) {
+            const int j = (__ffsll((long long)sp) - 1) >> 2;
+            const int dig = (int)((sp >> (4 * j)) & 15u) - 1;
+            sp &= ~(15ull << (4 * j));
+            const int cj = cov_nib(pc, j);
+            off += (dig + (dig >= cj) - cj) * (int)g.pw[j];
+        }
+        const int lj = last[it];
+        if (lj == 0xff) {
+            if (cnt[off] != 0xffffu) cnt[off]++;
+        } else {
+            const int step = (int)g.pw[lj], cj = cov_nib(pc, lj);
+            int o2 = off - cj * step;
+            for (int v = 0; v < g.q; v++, o2 += step)
+                if (v != cj && cnt[o2] != 0xffffu) cnt[o2]++;
+        }
+    }
+}
+
+// Top-up of covcount (cov/engine/covcount.c:163-195), one CTA: words m0..M-1
+// of code[] (packed) are chosen in order -- the first of 64 xorshift64
+// draws (seeded 88172645463325252 ^ m0) that is still uncovered, else the
+// first uncovered word from the scan position on, else any draw not yet in
+// the code -- and each one's ball is marked before the next is chosen.
+// Words of one ball are distinct, so the marking needs no atomics.
+__global__ void __launch_bounds__(512) k_topup(FinishGeom g, uint16_t *cnt, uint64_t *code, int m0,
+                                               const uint64_t *__restrict__ items,
+                                               const uint8_t *__restrict__ last)
+{
+    __shared__ uint64_t draw_st[64];
+    __shared__ uint32_t draw_x[64];
+    __shared__ unsigned hit[2];
+    __shared__ uint64_t s_rs;
+    __shared__ long long s_w, s_scan;
+    __shared__ int s_dup;
+    __shared__ uint64_t s_new;
+    if (threadIdx.x == 0) { s_rs = 88172645463325252ull ^ (uint64_t)m0; s_scan = 0; }
+    __syncthreads();
+    for (int m = m0; m < g.M; m++) {
+        if (threadIdx.x == 0) {
+            uint64_t r = s_rs;
+            for (int t = 0; t < 64; t++) { r = fin_xorshift(r); draw_st[t] = r; draw_x[t] = (uint32_t)(r % g.N); }
+        }
+        __syncthreads();
+        if (threadIdx.x < 64) {
+            const unsigned b = __ballot_sync(0xffffffffu, cnt[draw_x[threadIdx.x]] == 0);
+            if ((threadIdx.x & 31) == 0) hit[threadIdx.x >> 5] = b;
+        }
+        __syncthreads();
+        int f = -1;
+        if (hit[0]) f = __ffs(hit[0]) - 1;
+        else if (hit[1]) f = 32 + __ffs(hit[1]) - 1;
+        long long w = -1;
+        if (f >= 0) {
+            w = draw_x[f];
+        } else {
+            // first zero at or after the scan position, in chunks of the block
+            for (long long x0 = s_scan; x0 < (long long)g.N && w < 0; x0 += blockDim.x) {
+                const long long x = x0 + threadIdx.x;
+                const int z = x < (long long)g.N && cnt[x] == 0;
+                const int any = __syncthreads_or(z);
+                if (any) {
+                    if (threadIdx.x == 0) s_w = 0x7fffffffffffffffll;
+                    __syncthreads();
+                    if (z) atomicMin((unsigned long long *)&s_w, (unsigned long long)x);
+                    __syncthreads();
+                    w = s_w;
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_rs = f >= 0 ? draw_st[f] : draw_st[63];
+            s_scan = f >= 0 ? s_scan : (w >= 0 ? w : (long long)g.N);
+        }
+        __syncthreads();
+        if (w >= 0) {
+            if (threadIdx.x == 0) {
+                uint64_t pk = 0;
+                uint32_t y = (uint32_t)w;
+                for (int j = g.n - 1; j >= 0; j--) { pk |= (uint64_t)(y % (uint32_t)g.q) << (4 * j); y /= (uint32_t)g.q; }
+                s_new = pk;
+            }
+        } else {
+            // everything covered: any draw that is not yet a codeword
+            for (;;) {
+                if (threadIdx.x == 0) {
+                    s_rs = fin_xorshift(s_rs);
+                    uint32_t y = (uint32_t)(s_rs % g.N);
+                    uint64_t pk = 0;
+                    for (int j = g.n - 1; j >= 0; j--) { pk |= (uint64_t)(y % (uint32_t)g.q) << (4 * j); y /= (uint32_t)g.q; }
+                    s_new = pk;
+                    s_dup = 0;
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < m; i += blockDim.x)
+                    if (code[i] == s_new) s_dup = 1;
+                __syncthreads();
+                if (!s_dup) break;
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) code[m] = s_new;
+        fin_mark(g, cnt, s_new, items, last);
+        __syncthreads();
+    }
+}
+
+__global__ void k_count_zero16(const uint16_t *cnt, uint32_t N, unsigned long long *out)
+{
+    unsigned long long c = 0;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x)
+        c += cnt[x] == 0;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
 // ============================================================ host ========
 namespace {
 
@@ -482,6 +625,117 @@ int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code, int32_
     CK(cudaStreamSynchronize(st));
     CK(cudaFreeAsync(tmp, st));
     return COV_OK;
+}
+
+// The finisher of cov/engine/covcount.c: de-duplicate the m words (first
+// occurrences kept), top them up to M distinct words and count the
+// uncovered words of the result.  fast: top-up in base-q counting order, no
+// coverage (uncovered = -1).
+int cov_finish(int32_t q, int32_t n, int32_t R, int32_t M, const uint8_t *code, int32_t m, int32_t fast,
+               uint8_t *out, int32_t *words, int64_t *uncovered)
+{
+    DtGeom dg;
+    int rc = geom(q, n, dg);
+    if (rc) return rc;
+    if (R < 0 || M < 1 || m < 0 || (m > 0 && !code) || !out) return COV_EINVAL;
+    if ((long long)M > (long long)dg.N) return COV_EINVAL;           // no M distinct words exist
+    if (R > n) R = n;
+    for (long long i = 0; i < (long long)m * n; i++) if (code[i] >= q) return COV_EINVAL;
+    std::vector<uint64_t> pk;
+    {
+        pk.reserve((size_t)std::min(m, M));
+        // covcount reads at most M words, then drops the repeats among them
+        for (int i = 0; i < std::min(m, M); i++) {
+            uint64_t v = 0;
+            for (int j = 0; j < n; j++) v |= (uint64_t)code[(size_t)i * n + j] << (4 * j);
+            if (std::find(pk.begin(), pk.end(), v) == pk.end()) pk.push_back(v);
+        }
+    }
+    const int m0 = (int)pk.size();
+    auto unpack = [&](const std::vector<uint64_t> &v) {
+        for (int i = 0; i < M; i++)
+            for (int j = 0; j < n; j++) out[(size_t)i * n + j] = (uint8_t)((v[i] >> (4 * j)) & 15u);
+    };
+    if (fast) {
+        // base-q counting order, skipping words already present
+        std::vector<uint64_t> v = pk;
+        for (uint32_t x = 0; (int)v.size() < M; x++) {
+            uint64_t w = 0;
+            uint32_t y = x;
+            for (int j = n - 1; j >= 0; j--) { w |= (uint64_t)(y % (uint32_t)q) << (4 * j); y /= (uint32_t)q; }
+            if (std::find(v.begin(), v.end(), w) == v.end()) v.push_back(w);
+        }
+        unpack(v);
+        if (words) *words = M;
+        if (uncovered) *uncovered = -1;
+        return COV_OK;
+    }
+    if (dg.N > 1200000000u) return COV_ERANGE;                        // covcount's limit without --fast
+    if (!g_ct_attr) {
+        CK(cudaFuncSetAttribute(k_count_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bt_smem_bytes(BT_MAX)));
+        g_ct_attr = 1;
+    }
+    // tile count of the deduplicated words
+    CountGeom g;
+    memset(&g, 0, sizeof g);
+    g.q = q; g.n = n; g.R = R; g.M = m0;
+    bt_geom(q, n, &g.nh, &g.nl);
+    g.tw = (uint32_t)ipw(q, g.nl);
+    for (int j = 0; j < n; j++) g.pw[j] = dg.pw[n - 1 - j];
+    std::vector<uint8_t> tlast, blast;
+    std::vector<uint64_t> titems = bt_items_h(q, n, R, g.nh, g.vcum, tlast);
+    g.nitems = (uint32_t)titems.size();
+    // whole-ball groups for the top-up (no high digits)
+    uint32_t bcum[COV_MAXN + 2];
+    std::vector<uint64_t> bitems = bt_items_h(q, n, R, 0, bcum, blast);
+    FinishGeom fg;
+    memset(&fg, 0, sizeof fg);
+    fg.q = q; fg.n = n; fg.R = R; fg.M = M; fg.N = dg.N;
+    for (int j = 0; j < n; j++) fg.pw[j] = dg.pw[n - 1 - j];
+    fg.ngroups = bcum[std::min(R, n)];
+    const size_t tib = titems.size() * 8, tlb = (tlast.size() + 7) / 8 * 8;
+    const size_t bib = bitems.size() * 8, blb = (blast.size() + 7) / 8 * 8;
+    const size_t cb = ((size_t)dg.N * 2 + 15) / 16 * 16;
+    char *buf = nullptr;
+    if (cudaMalloc(&buf, tib + tlb + bib + blb + (size_t)M * 8 + cb + 16) != cudaSuccess) {
+        cudaGetLastError();
+        return COV_ENOMEM;
+    }
+    uint64_t *d_ti = (uint64_t *)buf;
+    uint64_t *d_bi = (uint64_t *)(buf + tib + tlb);
+    uint8_t *d_bl = (uint8_t *)(buf + tib + tlb + bib);
+    uint64_t *d_code = (uint64_t *)(buf + tib + tlb + bib + blb);
+    uint16_t *d_cnt = (uint16_t *)(buf + tib + tlb + bib + blb + (size_t)M * 8);
+    unsigned long long *d_z = (unsigned long long *)(buf + tib + tlb + bib + blb + (size_t)M * 8 + cb);
+    auto done = [&](int r) { cudaFree(buf); return r; };
+    cudaError_t e = cudaSuccess;
+    e = cudaMemcpy(d_ti, titems.data(), tib, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_ti + titems.size(), tlast.data(), tlast.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_bi, bitems.data(), bib, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_bl, blast.data(), blast.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && m0 > 0) e = cudaMemcpy(d_code, pk.data(), (size_t)m0 * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_z, 0, 8);
+    if (e != cudaSuccess) return done(-(100 + (int)e));
+    k_count_tiles<<<(unsigned)ipw(q, g.nh), BT_NT, bt_smem_bytes(g.tw)>>>(g, d_code, d_ti, d_cnt, nullptr);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && m0 < M) {
+        k_topup<<<1, 512>>>(fg, d_cnt, d_code, m0, d_bi, d_bl);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_count_zero16<<<152 * 4, 256>>>(d_cnt, dg.N, d_z);
+        e = cudaGetLastError();
+    }
+    std::vector<uint64_t> v((size_t)M);
+    unsigned long long z = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(v.data(), d_code, (size_t)M * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&z, d_z, 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return done(-(100 + (int)e));
+    unpack(v);
+    if (words) *words = M;
+    if (uncovered) *uncovered = (int64_t)z;
+    return done(COV_OK);
 }
 
 int cov_count(int32_t q, int32_t n, int32_t R, const uint8_t *code, int32_t M, uint16_t *cnt,

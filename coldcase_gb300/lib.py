@@ -100,6 +100,7 @@ SIGNATURES = {
     "cov_count_dev": (ctypes.c_int, [_I32, _I32, _I32, _P, _I32, _P, _P]),
     "cov_count_above_dev": (ctypes.c_int64, [_I32, _I32, _P, _I32, _P]),
     "cov_mindist_dev_static": (ctypes.c_int, [_I32, _I32, _P, _I32, _P, _P]),
+    "cov_finish": (ctypes.c_int, [_I32, _I32, _I32, _I32, _PU8, _I32, _I32, _PU8, _PI32, _PI64]),
 }
 
 _lib = None

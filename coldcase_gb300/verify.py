@@ -73,3 +73,17 @@ def count(code, q, n, R):
                           cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)), ctypes.byref(u)),
             "cov_count")
     return cnt, int(u.value)
+
+
+def finish(code, q, n, R, M, fast=False):
+    """covcount's finisher (cov/engine/covcount.c): (M distinct words,
+    uncovered count or -1 with fast).  The top-up and the recount run on the
+    GPU; with fast only the de-duplication and counting-order top-up."""
+    lib = L.load()
+    a = _code(code, q, n)
+    out = np.zeros((M, n), dtype=np.uint8)
+    words = ctypes.c_int32(0)
+    unc = ctypes.c_int64(0)
+    L.check(lib.cov_finish(q, n, R, M, L.u8ptr(a) if a.size else None, int(a.shape[0]), 1 if fast else 0,
+                           L.u8ptr(out), ctypes.byref(words), ctypes.byref(unc)), "cov_finish")
+    return out, int(unc.value)

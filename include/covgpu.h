@@ -190,6 +190,14 @@ int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code,
                   int32_t M, uint16_t *d_cnt, void *stream);
 int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist,
                             int32_t R, void *stream);
+/* The finisher of cov/engine/covcount.c (main, :66-216): de-duplicate the
+ * m words (first occurrences kept), top up to M distinct words -- with fast,
+ * in base-q counting order; else on still-uncovered words chosen as covcount
+ * does (64 xorshift64 probes, a linear scan, then any unused word), marking
+ * each new word's ball -- and count the uncovered words (-1 with fast).
+ * out: M*n digits.  M must not exceed q^n; without fast q^n <= 1.2e9. */
+int cov_finish(int32_t q, int32_t n, int32_t R, int32_t M, const uint8_t *code, int32_t m, int32_t fast,
+               uint8_t *out, int32_t *words, int64_t *uncovered);
 /* cov_mindist_dev without any device allocation, for callers that cannot
  * allocate (their device memory belongs to another allocator, or they run
  * where an allocation is not allowed).  No counterpart in the reference.

@@ -181,3 +181,103 @@ def dilate(code, q, n, R):
     cov = np.zeros(q ** n, dtype=np.uint8)
     ok = lib.orc_dilate(q, n, R, _u8(a), a.shape[0], _u8(cov))
     return bool(ok), cov.astype(bool)
+
+
+# ---------------------------------------------------------------- finisher --
+# Restatement of the reference finisher cov/engine/covcount.c: read at most
+# M well-formed words (:94-118), drop repeats keeping first occurrences
+# (:120-131), top up to M distinct words -- in base-q counting order with
+# --fast (:133-160), else on still-uncovered words found by 64 xorshift64
+# probes, then a linear scan, then any unused word (:163-195) -- marking each
+# added word's ball, and count the uncovered words (:197-199).  Pure Python:
+# small cases only.
+_DIG = "0123456789abcdefghijklmnopqrstuvwxyz"
+
+
+def finish_read(text, q, n, M):
+    import re
+    out = []
+    for line in text.splitlines(True):
+        if len(out) >= M:
+            break
+        line = line.split("#")[0]
+        if any(ch in line for ch in " ,\t"):
+            toks = [t for t in re.split(r"[ ,\t\r\n]+", line) if t][:n]
+            w = []
+            for t in toks:
+                m = re.match(r"[+-]?\d+", t)
+                w.append((int(m.group(0)) if m else 0) & 0xff)
+        else:
+            w = [_DIG.index(ch) for ch in line.rstrip("\r\n") if ch in _DIG][:n]
+        if len(w) != n or any(v >= q for v in w):
+            continue
+        out.append(w)
+    return out
+
+
+def finish(text, q, n, R, M, fast=False):
+    """(words as lists, uncovered or -1, exit status) of covcount."""
+    N = q ** n
+    pw = [q ** (n - 1 - j) for j in range(n)]
+    code = []
+    seen = set()
+    for w in finish_read(text, q, n, M):
+        t = tuple(w)
+        if t not in seen:
+            seen.add(t)
+            code.append(list(w))
+    digits = lambda x: [(x // pw[j]) % q for j in range(n)]
+    if fast:
+        x = 0
+        while len(code) < M:
+            t = tuple(digits(x))
+            x += 1
+            if t in seen:
+                continue
+            seen.add(t)
+            code.append(list(t))
+        return code, -1, 1
+    cov = np.zeros(N, dtype=bool)
+
+    def mark(c):
+        cov[cover_count(np.array([c], dtype=np.uint8), q, n, R) > 0] = True
+
+    for c in code:
+        mark(c)
+    mask = (1 << 64) - 1
+    rs = 88172645463325252 ^ len(code)
+
+    def step(r):
+        r ^= (r << 13) & mask
+        r ^= r >> 7
+        r ^= (r << 17) & mask
+        return r
+
+    scan = 0
+    while len(code) < M:
+        w = -1
+        for _ in range(64):
+            rs = step(rs)
+            c2 = rs % N
+            if not cov[c2]:
+                w = c2
+                break
+        if w < 0:
+            while scan < N and cov[scan]:
+                scan += 1
+            if scan < N:
+                w = scan
+        if w < 0:
+            while True:
+                rs = step(rs)
+                cand = digits(rs % N)
+                if tuple(cand) not in seen:
+                    break
+            new = cand
+        else:
+            new = digits(w)
+        seen.add(tuple(new))
+        code.append(new)
+        mark(new)
+    unc = int((~cov).sum())
+    return code, unc, 0 if unc == 0 else 1

@@ -11,6 +11,11 @@ Runs in the build container only (it needs the reference checkout):
                           small --stall (kicks) and --random-init.  Stored:
                           arguments, input code, the RESULT fingerprint
                           uncovered/iters/kicks and the --out file.
+  * finish_cases.json  -- the reference finisher (oracle/_ref/covcount,
+                          compiled from cov/engine/covcount.c) on code files
+                          with duplicates, malformed lines, too few and too
+                          many words: COUNT line, exit status and --out file,
+                          with and without --fast.
   * verify_cases.json  -- codes with their uncovered counts from the
                           reference verifiers verify_pure and verify_numpy
                           (cov/verify_cov.py) and the distance histogram and
@@ -163,6 +168,44 @@ def verify_cases(ref):
     return out
 
 
+def finish_cases(binary):
+    """The reference finisher (cov/engine/covcount.c, compiled into
+    oracle/_ref/covcount) on code files with duplicates, malformed lines,
+    too few and too many words, with and without --fast."""
+    rng = np.random.default_rng(20261203)
+    cases = []
+    specs = [(4, 6, 1, 420, 400, 0), (3, 5, 2, 20, 30, 1), (5, 4, 1, 60, 40, 2), (2, 8, 2, 30, 10, 3),
+             (6, 6, 3, 25, 25, 4), (7, 5, 2, 80, 70, 5), (4, 6, 2, 120, 0, 6), (3, 4, 1, 81, 90, 7),
+             (6, 9, 4, 700, 690, 8), (2, 6, 5, 3, 2, 9)]
+    for q, n, R, M, m, seed in specs:
+        code = rng.integers(0, q, (m, n), dtype=np.uint8)
+        if m > 4:
+            code[m // 2] = code[1]
+            code[m - 1] = code[0]
+        text = code_text(code)
+        if m > 3:
+            lines = text.splitlines(True)
+            lines.insert(2, "# a comment\n")
+            lines.insert(3, DIG[q % 36] * n + "\n")      # a digit out of range: skipped
+            lines.insert(4, "0" * (n + 1) + "\n")         # wrong length: skipped
+            text = "".join(lines)
+        for fast in (False, True):
+            with tempfile.TemporaryDirectory() as td:
+                inp, out = os.path.join(td, "in.txt"), os.path.join(td, "out.txt")
+                with open(inp, "w") as f:
+                    f.write(text)
+                cmd = [binary, "-q", str(q), "-n", str(n), "-R", str(R), "-M", str(M), "--in", inp, "--out", out]
+                if fast:
+                    cmd.append("--fast")
+                p = subprocess.run(cmd, capture_output=True, text=True)
+                m2 = re.search(r"COUNT .*words=(\d+) uncovered=(-?\d+)", p.stdout)
+                with open(out) as f:
+                    body = f.read()
+                cases.append(dict(q=q, n=n, R=R, M=M, fast=fast, input=text, rc=p.returncode,
+                                  words=int(m2.group(1)), uncovered=int(m2.group(2)), out=body))
+    return cases
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -175,7 +218,10 @@ def main():
     vc = verify_cases(a.ref)
     with open(os.path.join(HERE, "verify_cases.json"), "w") as f:
         json.dump(vc, f)
-    print("engine runs: %d, verify cases: %d" % (len(runs), len(vc)))
+    fc = finish_cases(os.path.join(REPO, "oracle", "_ref", "covcount"))
+    with open(os.path.join(HERE, "finish_cases.json"), "w") as f:
+        json.dump(fc, f)
+    print("engine runs: %d, verify cases: %d, finish cases: %d" % (len(runs), len(vc), len(fc)))
 
 
 if __name__ == "__main__":
