@@ -65,6 +65,7 @@ _I64 = ctypes.c_int64
 _PI32 = ctypes.POINTER(ctypes.c_int32)
 _PI64 = ctypes.POINTER(ctypes.c_int64)
 _PU8 = ctypes.POINTER(ctypes.c_uint8)
+_PU32 = ctypes.POINTER(ctypes.c_uint32)
 
 SIGNATURES = {
     "cov_pool_create": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_P)]),
@@ -101,6 +102,18 @@ SIGNATURES = {
     "cov_count_above_dev": (ctypes.c_int64, [_I32, _I32, _P, _I32, _P]),
     "cov_mindist_dev_static": (ctypes.c_int, [_I32, _I32, _P, _I32, _P, _P]),
     "cov_finish": (ctypes.c_int, [_I32, _I32, _I32, _I32, _PU8, _I32, _I32, _PU8, _PI32, _PI64]),
+    "cov_lns_create": (ctypes.c_int, [_I32, _I32, _I32, ctypes.POINTER(_P)]),
+    "cov_lns_destroy": (ctypes.c_int, [_P]),
+    "cov_lns_recount": (ctypes.c_int, [_P, _PU32, _I32]),
+    "cov_lns_map": (ctypes.c_int, [_P, _I32]),
+    "cov_lns_map_max": (ctypes.c_int, [_P, _PI32]),
+    "cov_lns_map_hist": (ctypes.c_int, [_P, _I32, _I32, _PI64]),
+    "cov_lns_map_extract": (ctypes.c_int, [_P, _I32, _I64, _PU32, _PI32, _PI64]),
+    "cov_lns_map_read": (ctypes.c_int, [_P, _PU32, _I32, _PI32]),
+    "cov_lns_ball": (ctypes.c_int, [_P, _PU32, _I32, _I32, _I32, _PI32]),
+    "cov_lns_count": (ctypes.c_int, [_P, _I32, _PI64]),
+    "cov_lns_get_cnt": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint16)]),
+    "cov_lns_get_map": (ctypes.c_int, [_P, _PI32]),
 }
 
 _lib = None

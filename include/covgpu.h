@@ -190,6 +190,36 @@ int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code,
                   int32_t M, uint16_t *d_cnt, void *stream);
 int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist,
                             int32_t R, void *stream);
+/* ------------------------------------------------------------------------
+ * Transform-engine primitives for one cell (q, n, R): the GPU side of the
+ * LNS solver, replacing cov/gemm2/dct.cu's C ABI (dct_init, dct_transform,
+ * dct_map_max, dct_map_hist, dct_map_extract, dct_map_read_at,
+ * dct_ball_gather, dct_ball_update, dct_count_eq, dct_free;
+ * dct.cu:299-504).  Word indices are MSB-first uint32; all buffers are
+ * host memory.
+ * --------------------------------------------------------------------- */
+typedef struct cov_lns cov_lns;
+int cov_lns_create(int32_t q, int32_t n, int32_t R, cov_lns **out);
+int cov_lns_destroy(cov_lns *h);
+/* coverage multiplicity of the m listed words (repeats count) */
+int cov_lns_recount(cov_lns *h, const uint32_t *idx, int32_t m);
+/* map[x] = #{y : d(x,y) <= R, cnt[y] == target}: target 0 = gain, 1 = loss */
+int cov_lns_map(cov_lns *h, int32_t target);
+int cov_lns_map_max(cov_lns *h, int32_t *out);
+/* counts of map values v >= 1 in bins (v-1)*nbins/vmax, v capped at vmax */
+int cov_lns_map_hist(cov_lns *h, int32_t nbins, int32_t vmax, int64_t *hist);
+/* positions with map >= thr in increasing index order (at most cap), and
+ * how many there are */
+int cov_lns_map_extract(cov_lns *h, int32_t thr, int64_t cap, uint32_t *idx, int32_t *val, int64_t *found);
+int cov_lns_map_read(cov_lns *h, const uint32_t *idx, int32_t k, int32_t *out);
+/* op 0: out[i] = #{y in the ball of idx[i] : cnt[y] == arg};
+ * op 1: add arg to cnt over the ball of every idx[i], one after another */
+int cov_lns_ball(cov_lns *h, const uint32_t *idx, int32_t k, int32_t op, int32_t arg, int32_t *out);
+/* #{x : cnt[x] == target} */
+int cov_lns_count(cov_lns *h, int32_t target, int64_t *out);
+int cov_lns_get_cnt(cov_lns *h, uint16_t *out);
+int cov_lns_get_map(cov_lns *h, int32_t *out);
+
 /* The finisher of cov/engine/covcount.c (main, :66-216): de-duplicate the
  * m words (first occurrences kept), top up to M distinct words -- with fast,
  * in base-q counting order; else on still-uncovered words chosen as covcount
