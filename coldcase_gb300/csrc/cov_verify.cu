@@ -120,11 +120,15 @@ k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__
             dt_pass4(dt_w, rows / q * wpr, q, inner, inner, inf4);
             __syncthreads();
         }
-        for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
-            const uint32_t r = e / (uint32_t)q, a = e - r * (uint32_t)q;
-            const uint8_t v = dt_b[r * (uint32_t)(wpr * 4) + a];
-            D[x0 + e] = v;
-            if (last) dt_hist_add(sh, v);
+        // out by rows: a thread writes the q words of its row
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const uint8_t *src = dt_b + r * (wpr * 4);
+            uint8_t *dst = D + x0 + (uint32_t)r * (uint32_t)q;
+            for (int a = 0; a < q; a++) {
+                const uint8_t v = src[a];
+                dst[a] = v;
+                if (last) dt_hist_add(sh, v);
+            }
         }
     }
     __syncthreads();
@@ -157,10 +161,22 @@ k_dt_high(DtGeom g, int j0, int gsz, int last_, uint8_t *__restrict__ D, unsigne
         const int w = (int)min((uint32_t)DT_STRIP_W, s - c0);
         const uint32_t base = o * span + c0;
         __syncthreads();
-        // element (row r, column c) at base + r*s + c, kept at byte r*W + c
-        for (uint32_t e = threadIdx.x; e < rows * DT_STRIP_W; e += blockDim.x) {
-            uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
-            dt_b[e] = (c < (uint32_t)w) ? D[base + r * s + c] : (uint8_t)g.inf;
+        // element (row r, column c) at base + r*s + c, kept at byte r*W + c;
+        // eight loads of a thread in flight before their stores
+        const uint32_t tot = rows * DT_STRIP_W;
+        for (uint32_t e0 = threadIdx.x; e0 < tot; e0 += 8 * blockDim.x) {
+            uint8_t v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const uint32_t e = e0 + (uint32_t)u * blockDim.x;
+                const uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
+                v[u] = (e < tot && c < (uint32_t)w) ? D[base + r * s + c] : (uint8_t)g.inf;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const uint32_t e = e0 + (uint32_t)u * blockDim.x;
+                if (e < tot) dt_b[e] = v[u];
+            }
         }
         __syncthreads();
         for (int j = 0; j < gsz; j++) {          // row stride q^j
