@@ -149,8 +149,9 @@ class LNS:
 
     RUIN_MODES = ("low", "hole", "hole", "cluster", "random")
 
-    def __init__(self, q, n, R, seed=1, out=None, log=None, deadline=None):
+    def __init__(self, q, n, R, seed=1, out=None, log=None, deadline=None, bound_cap=1 << 14):
         self.q, self.n, self.R = q, n, R
+        self.bound_cap = bound_cap      # most stale bounds kept per refresh of the gain map
         self.rng = np.random.default_rng(seed * 1000003 + 12345)
         self.out = out
         self.log = log or (lambda *a: None)
@@ -222,7 +223,7 @@ class LNS:
         top = eng.map_max()
         if top <= 0:
             return [], 0
-        cap = min(eng.extract_cap, 1 << 18)
+        cap = min(eng.extract_cap, self.bound_cap)
         thr = 1
         if top > 1:
             hist = eng.map_hist(1024, top)
