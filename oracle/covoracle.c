@@ -6,8 +6,9 @@
  * product never loads it.
  *
  * The algorithm is that of cov/engine/covsearch2e.c run as
- * `--preset p5b` (opt_hoist=1, opt_st=2, opt_eval=2; covsearch2e.c:1090)
- * without --wide, --fix0, --sa, --noise, --ucache or --upick.  Each function
+ * `--preset p5b` (opt_hoist=1, opt_st=2, opt_eval=2; covsearch2e.c:1090),
+ * with or without --wide (orc_set_wide), without --fix0, --sa, --noise,
+ * --ucache or --upick.  Each function
  * names the reference lines it restates.  Everything that decides the search
  * trajectory -- RNG consumption order, candidate order, tie-breaking, tabu
  * arithmetic -- is reproduced exactly; what only affects speed (offset
@@ -80,6 +81,8 @@ struct cov_oracle {
     int32_t *tabu;
     orng rng;
     int tenure, kick, cand, threads;
+    int wide;                       /* --wide: all n(q-1) moves per codeword */
+    size_t cand_cap;                /* entries of ci/cp/cv/cd */
     long long stall;
     long long it, since_improve, nkicks;
     int inited;
@@ -452,7 +455,8 @@ cov_oracle *orc_create(int q, int n, int R, int M, uint64_t seed, int tabu,
     o->ul_dig = malloc((size_t)UL_CAP * n);
     o->ul_bit = calloc((size_t)((o->N + 63) / 64), 8);
     o->tabu = calloc((size_t)M * n * q, sizeof(int32_t));
-    size_t cap = (size_t)M * (R + 2);
+    size_t cap = (size_t)M * n;     /* ncand <= (codewords at dtar) * dtar */
+    o->cand_cap = cap;
     o->ci = malloc(sizeof(int) * cap); o->cp = malloc(sizeof(int) * cap);
     o->cv = malloc(sizeof(int) * cap); o->cd = malloc(sizeof(long long) * cap);
     o->dist = malloc(sizeof(int) * M); o->cwl = malloc(sizeof(int) * M);
@@ -579,10 +583,23 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
             if (d < dmin) dmin = d;
         }
         int dtar = (dmin <= R + 1) ? R + 1 : dmin;
+        /* --wide: every single-coordinate move of the codewords at dtar,
+         * decided before collecting so that candidates and evaluator agree
+         * (covsearch2e.c:1353-1376) */
+        const int wide_now = o->wide && o->ul_valid &&
+                             ((long long)o->ul_n * n < (long long)(R + 1) * o->totpat);
         int ncand = 0;
         for (int i = 0; i < M; i++) {
             if (o->dist[i] != dtar) continue;
             const uint8_t *c = o->code + (size_t)i * n;
+            if (wide_now) {
+                for (int p = 0; p < n; p++)
+                    for (int v = 0; v < q; v++) {
+                        if (v == c[p]) continue;
+                        o->ci[ncand] = i; o->cp[ncand] = p; o->cv[ncand] = v; ncand++;
+                    }
+                continue;
+            }
             for (int p = 0; p < n; p++) {
                 if (c[p] == u[p]) continue;
                 o->ci[ncand] = i; o->cp[ncand] = p; o->cv[ncand] = u[p]; ncand++;
@@ -687,6 +704,32 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
         if (o->best_unc == 0) break;
     }
     return done;
+}
+
+/* --wide (covsearch2e.c:1076): the candidate arrays grow to M*n*(q-1) */
+int orc_set_wide(cov_oracle *o, int wide)
+{
+    const size_t cap = wide ? (size_t)o->M * o->n * (o->q - 1) : (size_t)o->M * o->n;
+    if (cap > o->cand_cap) {
+        int *ci = realloc(o->ci, sizeof(int) * cap);
+        if (ci) o->ci = ci;
+        int *cp = realloc(o->cp, sizeof(int) * cap);
+        if (cp) o->cp = cp;
+        int *cv = realloc(o->cv, sizeof(int) * cap);
+        if (cv) o->cv = cv;
+        long long *cd = realloc(o->cd, sizeof(long long) * cap);
+        if (cd) o->cd = cd;
+        if (!ci || !cp || !cv || !cd) return -1;
+        o->cand_cap = cap;
+    }
+    o->wide = wide ? 1 : 0;
+    return 0;
+}
+
+void orc_ul_state(const cov_oracle *o, int *valid, int *n)
+{
+    *valid = o->ul_valid;
+    *n = o->ul_n;
 }
 
 long long orc_uncovered(const cov_oracle *o) { return o->unc; }

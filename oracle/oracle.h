@@ -61,6 +61,13 @@ long long orc_init(cov_oracle *o, const uint8_t *code, int m, int random_init);
 long long orc_run(cov_oracle *o, long long max_moves, long long target,
                   cov_move_rec *trace);
 
+/* --wide (covsearch2e.c:1353-1376): while the uncovered-word list is
+ * valid and short, the candidates are all n(q-1) moves of each codeword at
+ * the target distance.  Returns 0, or -1 when out of memory. */
+int orc_set_wide(cov_oracle *o, int wide);
+/* the uncovered-word list: valid flag and length, stale entries included */
+void orc_ul_state(const cov_oracle *o, int *valid, int *n);
+
 long long orc_uncovered(const cov_oracle *o);
 long long orc_best_uncovered(const cov_oracle *o);
 long long orc_iters(const cov_oracle *o);

@@ -55,6 +55,9 @@ def load():
     lib.orc_get_tabu.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
     lib.orc_get_rng.argtypes = [P, ctypes.POINTER(ctypes.c_uint64)]
     lib.orc_eval_codeword.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+    lib.orc_set_wide.restype = ctypes.c_int
+    lib.orc_set_wide.argtypes = [P, ctypes.c_int]
+    lib.orc_ul_state.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     lib.orc_distinct_code.restype = ctypes.c_int
     lib.orc_distinct_code.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int, u8p]
     lib.orc_cover_count.restype = ctypes.c_int
@@ -76,12 +79,16 @@ def _u8(a):
 class Oracle:
     """One restated covsearch2e p5b search (covsearch2e.c:1023-1621)."""
 
-    def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000, threads=1):
+    def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000, threads=1,
+                 wide=False):
         self.lib = load()
         self.q, self.n, self.R, self.M = q, n, R, M
         self.h = self.lib.orc_create(q, n, R, M, seed, tabu, kick, stall, cand, threads)
         if not self.h:
             raise ValueError("oracle: bad parameters")
+        if wide and self.lib.orc_set_wide(self.h, 1) != 0:
+            self.close()
+            raise MemoryError("oracle: no memory for the wide candidate set")
 
     def init(self, code=None, random_init=False):
         a = np.zeros((0, self.n), dtype=np.uint8) if code is None else \
@@ -107,6 +114,12 @@ class Oracle:
 
     def kicks(self):
         return self.lib.orc_kicks(self.h)
+
+    def ul_state(self):
+        """(valid, length) of the uncovered-word list."""
+        v, n = ctypes.c_int(), ctypes.c_int()
+        self.lib.orc_ul_state(self.h, ctypes.byref(v), ctypes.byref(n))
+        return v.value, n.value
 
     def code(self):
         out = np.zeros((self.M, self.n), dtype=np.uint8)

@@ -8,7 +8,7 @@ Runs in the build container only (it needs the reference checkout):
                           cell list of cov/engine/selftest.sh:27-38 plus runs
                           that exercise --in (exact M, fewer words = greedy
                           top-up, more words = remove-and-repair), --tabu,
-                          small --stall (kicks) and --random-init.  Stored:
+                          small --stall (kicks), --random-init and --wide.  Stored:
                           arguments, input code, the RESULT fingerprint
                           uncovered/iters/kicks and the --out file.
   * finish_cases.json  -- the reference finisher (oracle/_ref/covcount,
@@ -99,11 +99,25 @@ def engine_runs(binary):
         code = np.random.default_rng(s).integers(0, 4, (420, 6), dtype=np.uint8)
         runs.append(dict(q=4, n=6, R=1, M=420, seed=s, iters=10000, tabu=10, stall=5000, kick=2,
                          random_init=False, code=code_text(code)))
+    # --wide: all n(q-1) moves of each candidate codeword while the uncovered
+    # list is valid and short (covsearch2e.c:1353-1376); the K_3(11,4) runs
+    # cross that threshold in both directions
+    for (q, n, R, M, it) in [(6, 6, 3, 41, 400), (3, 11, 4, 81, 400), (6, 8, 4, 169, 60),
+                             (6, 6, 3, 45, 400), (5, 6, 2, 60, 300)]:
+        for s in (1, 2):
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=s, iters=it, tabu=7, stall=50, kick=2,
+                             random_init=False, code=None, wide=True))
+    for (q, n, R, M, m, it) in [(6, 6, 3, 41, 41, 600), (3, 11, 4, 81, 90, 300)]:
+        code = np.random.default_rng(7000 + q + n + m).integers(0, q, (m, n), dtype=np.uint8)
+        runs.append(dict(q=q, n=n, R=R, M=M, seed=3, iters=it, tabu=10, stall=40, kick=2,
+                         random_init=False, code=code_text(code), wide=True))
     for r in runs:
         args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"],
                 "--iters", r["iters"], "--tabu", r["tabu"], "--stall", r["stall"], "--kick", r["kick"]]
         if r["random_init"]:
             args.append("--random-init")
+        if r.get("wide"):
+            args.append("--wide")
         r["ref"] = run_ref(binary, args, r["code"])
     return runs
 
