@@ -108,7 +108,7 @@ class Tuner:
                 for sp in sample:
                     pool.add(sp["q"], sp["n"], sp["R"], sp["M"], code=uniform_code(sp["q"], sp["n"], sp["M"],
                                                                                     sp["seed"]),
-                             seed=sp["seed"], tabu=sp.get("tabu", 0))
+                             seed=sp["seed"], tabu=sp.get("tabu", 0), wide=sp.get("wide", False))
                 pool.run(self.warm)
                 t0 = time.perf_counter()
                 pool.run(self.moves)
@@ -172,7 +172,7 @@ def work_per_move(q, n, R):
 class Batch:
     """Many instances in one pool; each runs exactly its own move budget.
 
-    specs: dicts with q, n, R, M, seed, moves and optionally tabu, code.
+    specs: dicts with q, n, R, M, seed, moves and optionally tabu, code, wide.
     clusters: {size class: cluster size} (e.g. from Tuner.plan) or an int.
     """
 
@@ -186,7 +186,7 @@ class Batch:
             if code is None:
                 code = uniform_code(sp["q"], sp["n"], sp["M"], sp["seed"])
             s = self.pool.add(sp["q"], sp["n"], sp["R"], sp["M"], code=code, seed=sp["seed"],
-                              tabu=sp.get("tabu", 0))
+                              tabu=sp.get("tabu", 0), wide=sp.get("wide", False))
             c = clusters if isinstance(clusters, int) else clusters.get(size_class(sp["q"], sp["n"], sp["R"],
                                                                                      sp["M"]), 1)
             self.pool.set_slot_param(s, "cluster", c)

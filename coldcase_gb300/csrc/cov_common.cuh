@@ -94,6 +94,9 @@ struct CovSlot {
     int padj_warp;               // private-count events of a commit aggregated per warp
     int list_cost;               // cost of one list entry in walked words: the entering side
                                  // reads the list while U_n * list_cost < ncw (R+1) S
+    int wide;                    // --wide: every single-coordinate move of a candidate codeword
+                                 // while the list is valid and U_n n < (R+1) S'
+    int wide_sliced;             // its list pass finds hits by bit-sliced counts (<= 64 candidates)
     // device arrays
     uint32_t *cw;                // [N]  cnt (bits 0-15) | sum of covering ids mod 2^16 (16-31)
     uint64_t *code;              // [M]  packed codewords
@@ -121,10 +124,11 @@ struct CovSlot {
     uint32_t bt_tw;              // q^bt_nl
     uint32_t bt_v[COV_MAXN + 2];
     // per-slot global scratch for the rare large cases
-    uint32_t *g_perm;            // [M*n]
-    int32_t *g_dval;             // [M*n]
+    uint32_t *g_perm;            // [M*n], [M*n*(q-1)] when wide
+    int32_t *g_dval;             // same
     uint32_t *g_list;            // [M]
     int32_t *g_neg;              // [M*n]
+    int32_t *g_negw;             // [M*n*q] entering counts of every move (wide only)
     void *trace;                 // cov_move_rec[trace_cap] or null
     long long trace_cap;
     struct CovSlotState *st;

@@ -72,6 +72,7 @@ struct OpParams {
     int nL, dtar;
     int L_sm, neg_sm;          // list / neg arrays live in the leader's smem
     int uln;                   // uncovered-list length for OP_NEG
+    int wide;                  // OP_NEG counts every (candidate, position, value) into g_negw
 };
 
 struct Smem {
@@ -92,6 +93,7 @@ struct Smem {
     long long guard;
     int ul_valid, status, phase, kick_t, finished, greedy_i, mode;
     int nL, dtar, ncand, take, improved, dokick, swaps_pending;
+    int cpw, wide_now;         // candidate moves per codeword; --wide in force this move
     uint64_t pu;
     long long uw;
     cov_move_rec rec;
@@ -385,7 +387,7 @@ __device__ int block_scan_int(Smem &S, int v, int ident, Op op, int &total)
 __device__ void apply_swaps(const CovSlot &d, Smem &S)
 {
     if (!S.swaps_pending) return;
-    const int take = S.take, ncand = S.ncand, dtar = S.dtar;
+    const int take = S.take, ncand = S.ncand, cpw = S.cpw;
     const int psm = ncand <= PERM_CAP;
     uint32_t *perm = psm ? S.perm : d.g_perm;
     int32_t *dval = psm ? S.dval : d.g_dval;
@@ -396,8 +398,8 @@ __device__ void apply_swaps(const CovSlot &d, Smem &S)
     if (take < ncand) {
         int c = 0;
         for (int s = 0; s < take; s++) {
-            int l = (int)(perm[s] / (uint32_t)dtar), dup = 0;
-            for (int t = 0; t < s; t++) if ((int)(perm[t] / (uint32_t)dtar) == l) { dup = 1; break; }
+            int l = (int)(perm[s] / (uint32_t)cpw), dup = 0;
+            for (int t = 0; t < s; t++) if ((int)(perm[t] / (uint32_t)cpw) == l) { dup = 1; break; }
             c += !dup;
         }
         S.rec.ncw = c;
@@ -1210,12 +1212,74 @@ __device__ void build_cmask(const CovSlot &d, Smem &S, int nL, uint64_t pu)
     }
 }
 
+// Entering counts of every single-coordinate move of the candidate
+// codewords (--wide, covsearch2e.c:720-733): for each current list entry x
+// and each candidate l at distance exactly R+1 from it, negw[l][j][x_j]
+// gains 1 at the R+1 positions j where they differ.  Up to 64 candidates
+// held in shared memory find their hits by the bit-sliced count of equal
+// positions over cmask; more are tested one by one.
+__device__ __noinline__ void ul_pass_wide(const CovSlot &d, const Smem &S, int nL, bool sm, const uint32_t *Lp,
+                             int32_t *negw, uint32_t first, uint32_t stride, uint32_t n0)
+{
+    const int n = d.n, q = d.q, R = d.R;
+    const int tgt = n - (R + 1);
+    const bool sliced = sm && nL <= 64 && d.wide_sliced;
+    const uint64_t lmask = nL >= 64 ? ~0ull : ((1ull << nL) - 1);
+    for (uint32_t e = first; e < n0; e += stride) {
+        const uint64_t px = cov_ldcg(&d.ul_pk[e]);
+        if (sliced) {
+            uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0;
+            for (int j = 0; j < n; j++) {
+                const uint64_t m = S.cmask[j * q + cov_nib(px, j)];
+                uint64_t c1 = b0 & m; b0 ^= m;
+                uint64_t c2 = b1 & c1; b1 ^= c1;
+                uint64_t c3 = b2 & c2; b2 ^= c2;
+                uint64_t c4 = b3 & c3; b3 ^= c3;
+                b4 ^= c4;
+            }
+            uint64_t hit = ((tgt & 1) ? b0 : ~b0) & ((tgt & 2) ? b1 : ~b1) & ((tgt & 4) ? b2 : ~b2) &
+                           ((tgt & 8) ? b3 : ~b3) & ((tgt & 16) ? b4 : ~b4) & lmask;
+            if (!hit) continue;
+            if ((cov_ldcg(&d.cw[cov_ldcg(&d.ul_idx[e])]) & 0xffffu) != 0) continue;   // stale entry
+            for (; hit; hit &= hit - 1) {
+                const int l = __ffsll((long long)hit) - 1;
+                for (uint64_t m = cov_spread(px ^ S.Lpk[l]); m; m &= m - 1) {
+                    const int j = (__ffsll((long long)m) - 1) >> 2;
+                    atomicAdd(&negw[(l * n + j) * q + cov_nib(px, j)], 1);
+                }
+            }
+            continue;
+        }
+        if ((cov_ldcg(&d.cw[cov_ldcg(&d.ul_idx[e])]) & 0xffffu) != 0) continue;
+        for (int l = 0; l < nL; l++) {
+            const uint64_t pk = sm ? S.Lpk[l] : cov_ldcg(&d.code[Lp[l]]);
+            const uint64_t D = cov_spread(px ^ pk);
+            if (__popcll(D) != R + 1) continue;
+            for (uint64_t m = D; m; m &= m - 1) {
+                const int j = (__ffsll((long long)m) - 1) >> 2;
+                atomicAdd(&negw[(l * n + j) * q + cov_nib(px, j)], 1);
+            }
+        }
+    }
+}
+
 // the list pass shared by the whole cluster: every CTA takes a slice of
 // the list; the followers accumulate locally and add into the leader's counts
 __device__ void op_neg(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank, int csize)
 {
     const int nL = P.nL, n = d.n;
     const uint32_t n0 = (uint32_t)P.uln;
+    if (P.wide) {
+        // every CTA adds its strided share of the list straight into g_negw
+        if (rank != 0) {
+            for (int l = threadIdx.x; l < nL; l += NT) S.Lpk[l] = LS->Lpk[l];
+            for (int t = threadIdx.x; t < d.n * d.q; t += NT) S.cmask[t] = LS->cmask[t];
+            cov_bar();
+        }
+        ul_pass_wide(d, S, nL, true, nullptr, d.g_negw, (uint32_t)rank * NT + threadIdx.x,
+                     (uint32_t)(csize * NT), n0);
+        return;
+    }
     if (nL <= 64) {
         // contiguous slice of the list per CTA; counts go straight into the
         // leader's neg (one atomic per candidate and position per chunk)
@@ -1542,7 +1606,14 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     }
     const int Lsm = nL <= L_SM;
     uint32_t *Lp = Lsm ? S.L : d.g_list;
-    const int ncand = nL * dtar;
+    // --wide (covsearch2e.c:1353-1376): while the list is valid and
+    // U_n n < (R+1) S', the candidates are all n(q-1) moves of each
+    // codeword at dtar (p outer, v inner, v != c_p); else the dtar moves
+    // towards u
+    const bool wide_now = d.wide && S.ul_valid &&
+        (long long)S.uln * n < (long long)(R + 1) * (long long)d.nsub * (long long)d.ppow[R];
+    const int cpw = wide_now ? n * (d.q - 1) : dtar;
+    const int ncand = nL * cpw;
     if (ncand == 0) {     // impossible for an uncovered target word
         if (tid == 0) { S.status = COV_EDRIFT; S.opp.op = OP_STOP; S.phase = PH_STOPPED; }
         __syncwarp();
@@ -1582,8 +1653,8 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         if (take < ncand && tid == 0) {
             int c = 0;
             for (int s2 = 0; s2 < take; s2++) {
-                int l = (int)(perm[s2] / (uint32_t)dtar), dup = 0;
-                for (int t2 = 0; t2 < s2; t2++) if ((int)(perm[t2] / (uint32_t)dtar) == l) { dup = 1; break; }
+                int l = (int)(perm[s2] / (uint32_t)cpw), dup = 0;
+                for (int t2 = 0; t2 < s2; t2++) if ((int)(perm[t2] / (uint32_t)cpw) == l) { dup = 1; break; }
                 c += !dup;
             }
             S.ibc[2] = c;
@@ -1593,6 +1664,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     if (tid == 0) {
         S.swaps_pending = pending;
         S.nL = nL; S.dtar = dtar; S.ncand = ncand; S.take = take;
+        S.cpw = cpw; S.wide_now = wide_now;
         S.rec.ncand = ncand; S.rec.ncw = (!pending && take < ncand) ? S.ibc[2] : nL;
         long long t1 = cov_clock();
         S.prof[1] += t1 - t0;
@@ -1610,6 +1682,36 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         S.prof[20] += (unsigned long long)nL;
         S.prof[21] += S.ul_valid ? (unsigned long long)S.uln : 0ull;
         S.prof[22] += 1;
+    }
+    if (wide_now) {
+        // one list pass gives the entering count of every (l, j, v)
+        int32_t *negw = d.g_negw;
+        for (int x = tid; x < nL * n * d.q; x += NT) cov_stcg(&negw[x], 0);
+        if (Lsm && nL <= 64) build_cmask(d, S, nL, pu);
+        cov_bar();
+        const long long pairs = (long long)S.uln * nL;
+        if (csize > 1 && Lsm && pairs >= d.neg_cluster_pairs) {
+            if (tid == 0) {
+                OpParams &o = S.opp;
+                o.op = OP_NEG; o.nL = nL; o.dtar = dtar; o.pu = pu; o.uln = S.uln;
+                o.L_sm = 1; o.neg_sm = 1; o.ul_valid = 1; o.wide = 1;
+                S.phase = PH_SELECT;
+                S.prof[2] += cov_clock() - t0;
+                S.ul_pairs += pairs;
+            }
+            __syncwarp();
+            return;
+        }
+        ul_pass_wide(d, S, nL, Lsm, Lp, negw, tid, NT, (uint32_t)S.uln);
+        cov_bar();
+        if (tid == 0) {
+            S.phase = PH_SELECT;
+            S.prof[2] += cov_clock() - t0;
+            S.ul_pairs += pairs;
+        }
+        __syncwarp();
+        S.opp.op = -1;
+        return;
     }
     // The list and the walk give the same counts (covsearch2e.c:720-753);
     // the reference picks the list while U_n n < (R+1) S' (:1466-1467).  Here
@@ -1639,7 +1741,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         if (tid == 0) {
             OpParams &o = S.opp;
             o.op = OP_NEG; o.nL = nL; o.dtar = dtar; o.pu = pu; o.uln = S.uln;
-            o.L_sm = 1; o.neg_sm = 1; o.ul_valid = 1;
+            o.L_sm = 1; o.neg_sm = 1; o.ul_valid = 1; o.wide = 0;
             S.phase = PH_SELECT;
             S.prof[2] += cov_clock() - t0;
             S.ul_pairs += pairs;
@@ -1688,13 +1790,37 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     S.opp.op = -1;   // no op yet: select follows
 }
 
+// Candidate r of codeword pk: position and value (covsearch2e.c:1359-1376).
+// Plain: the r-th position where pk differs from u, moved to u's digit.
+// Wide: r = p (q-1) + the rank of v among the values other than c_p.
+__device__ __forceinline__ void cand_pv(const CovSlot &d, bool wide, int r, uint64_t pk, uint64_t pu,
+                                        int &p, int &v)
+{
+    if (wide) {
+        const int qm1 = d.q - 1;
+        p = r / qm1;
+        const int vv = r - p * qm1;
+        v = vv + (vv >= cov_nib(pk, p));
+    } else {
+        p = nth_set_pos(cov_spread(pk ^ pu), r);
+        v = cov_nib(pu, p);
+    }
+}
+
+// entering count of candidate l's move (p, v)
+__device__ __forceinline__ int cand_neg(const CovSlot &d, bool wide, const int32_t *negp, int l, int p, int v)
+{
+    return wide ? cov_ldcg(&d.g_negw[(l * d.n + p) * d.q + v]) : negp[l * d.n + p];
+}
+
 // Deltas of the sampled candidates and the tabu/aspiration/reservoir
 // selection of covsearch2e.c:1503-1518; emits OP_MOVE.
 __device__ void leader_select(const CovSlot &d, Smem &S)
 {
     const int tid = threadIdx.x;
     const int n = d.n, q = d.q;
-    const int nL = S.nL, dtar = S.dtar, ncand = S.ncand, take = S.take;
+    const int nL = S.nL, cpw = S.cpw, ncand = S.ncand, take = S.take;
+    const bool wide = S.wide_now;
     const uint64_t pu = S.pu;
     const int psm = ncand <= PERM_CAP, Lsm = nL <= L_SM;
     uint32_t *perm = psm ? S.perm : d.g_perm;
@@ -1710,13 +1836,13 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
     if (psm) {
         for (int s = tid; s < take; s += NT) {
             uint32_t c = perm[s];
-            int l = (int)(c / (uint32_t)dtar), r = (int)(c - (uint32_t)l * dtar);
+            int l = (int)(c / (uint32_t)cpw), r = (int)(c - (uint32_t)l * cpw);
             int k = (int)Lp[l];
             uint64_t pk = Lsm ? S.Lpk[l] : cov_ldcg(&d.code[k]);
-            int p = nth_set_pos(cov_spread(pk ^ pu), r);
-            int v = cov_nib(pu, p);
+            int p, v;
+            cand_pv(d, wide, r, pk, pu, p, v);
             const int32_t *Pk = d.P + (size_t)k * (n + 1);
-            dval[s] = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
+            dval[s] = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - cand_neg(d, wide, negp, l, p, v);
             S.tflag[s] = (uint8_t)((long long)cov_ldcg(&d.tabu[((size_t)k * n + p) * q + v]) > S.it);
         }
     }
@@ -1806,13 +1932,13 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
                 if (psm) { dd = dval[s]; tb = S.tflag[s]; }
                 else {
                     uint32_t c = perm[s];
-                    int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
+                    int l = (int)(c / (uint32_t)cpw), rr = (int)(c - (uint32_t)l * cpw);
                     int k = (int)Lp[l];
                     uint64_t pk = cov_ldcg(&d.code[k]);
-                    int p = nth_set_pos(cov_spread(pk ^ pu), rr);
-                    int v = cov_nib(pu, p);
+                    int p, v;
+                    cand_pv(d, wide, rr, pk, pu, p, v);
                     const int32_t *Pk = d.P + (size_t)k * (n + 1);
-                    dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
+                    dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - cand_neg(d, wide, negp, l, p, v);
                     tb = (long long)cov_ldcg(&d.tabu[((size_t)k * n + p) * q + v]) > S.it;
                 }
                 if (tb && S.unc + dd >= S.best_unc) continue;
@@ -1827,13 +1953,13 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
         long long ts2 = cov_clock();
         S.prof[9] += ts2 - ts1;
         uint32_t c = perm[bs];
-        int l = (int)(c / (uint32_t)dtar), rr = (int)(c - (uint32_t)l * dtar);
+        int l = (int)(c / (uint32_t)cpw), rr = (int)(c - (uint32_t)l * cpw);
         int k = (int)Lp[l];
         uint64_t pk = cov_ldcg(&d.code[k]);
-        int p = nth_set_pos(cov_spread(pk ^ pu), rr);
-        int v = cov_nib(pu, p);
+        int p, v;
+        cand_pv(d, wide, rr, pk, pu, p, v);
         const int32_t *Pk = d.P + (size_t)k * (n + 1);
-        long long dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - negp[l * n + p];
+        long long dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - cand_neg(d, wide, negp, l, p, v);
         S.chosen_delta = dd;
         OpParams &o = S.opp;
         o.op = OP_MOVE;
@@ -2698,7 +2824,9 @@ size_t cov_slot_bytes(const cov_params *prm)
     add((size_t)UL_CAP_DEFAULT * 8);                 // ul_pk
     add((size_t)((N + 31) / 32) * 4);                // ul_bit
     add((size_t)((N + 31) / 32) * 4);                // zb
-    add((size_t)M * n * 4 * 3 + (size_t)M * 4);      // g_perm, g_dval, g_neg, g_list
+    const size_t ce = (size_t)M * n * (prm->wide ? (size_t)(q - 1) : 1u);
+    add(ce * 4 * 2 + (size_t)M * n * 4 + (size_t)M * 4);   // g_perm, g_dval, g_neg, g_list
+    if (prm->wide) add((size_t)M * n * q * 4);      // g_negw
     add(65536);                                      // subset tables
     {
         int nh, nl;
@@ -2725,6 +2853,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     if (cap > 65535) return COV_ERANGE;
     long long N = ipow_h(q, n);
     if (N >= (1LL << 32) - 1) return COV_EINVAL;
+    if (prm->wide < 0 || prm->wide > 1) return COV_EINVAL;
     if (R > n) R = n;
     int s = -1;
     for (int k = 0; k < pool->max_slots; k++) if (!pool->slots[k].used) { s = k; break; }
@@ -2747,6 +2876,8 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.ul_cap = UL_CAP_DEFAULT;
     d.neg_cluster_pairs = pool->neg_cluster_pairs;
     d.list_cost = pool->list_cost;
+    d.wide = prm->wide ? 1 : 0;
+    d.wide_sliced = 1;
     d.padj_warp = padj_auto(q, n, R, M);
     d.zbits = d.padj_warp;
     std::vector<uint8_t> subs((size_t)n * std::max(d.nsub, 1) * d.rs, 0);
@@ -2794,10 +2925,12 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.ul_pk = (uint64_t *)take_((size_t)d.ul_cap * 8);
     d.ul_bit = (uint32_t *)take_((size_t)((N + 31) / 32) * 4);
     d.zb = (uint32_t *)take_((size_t)((N + 31) / 32) * 4);
-    d.g_perm = (uint32_t *)take_((size_t)Mw * n * 4);
-    d.g_dval = (int32_t *)take_((size_t)Mw * n * 4);
+    const size_t ce = (size_t)Mw * n * (prm->wide ? (size_t)(q - 1) : 1u);
+    d.g_perm = (uint32_t *)take_(ce * 4);
+    d.g_dval = (int32_t *)take_(ce * 4);
     d.g_neg = (int32_t *)take_((size_t)Mw * n * 4);
     d.g_list = (uint32_t *)take_((size_t)Mw * 4);
+    d.g_negw = prm->wide ? (int32_t *)take_((size_t)Mw * n * q * 4) : nullptr;
     uint8_t *dsub = (uint8_t *)take_(subs.size());
     uint8_t *dball = (uint8_t *)take_(balls.size());
     uint8_t *dsub1 = (uint8_t *)take_(subs1.size());
@@ -3117,6 +3250,9 @@ int cov_device_memory(int64_t *free_bytes, int64_t *total_bytes)
 //                        number of events (the default)
 //   "it_limit"           iteration count at which the slot stops (-1: none);
 //                        each run advances it by at most the remainder
+//   "wide_sliced"        --wide list pass: 1 finds the hits of up to 64
+//                        candidates by bit-sliced counts (the default), 0
+//                        tests every candidate against every entry
 int cov_pool_set_slot_param(cov_pool *pool, int32_t slot, const char *name, int64_t value)
 {
     if (!pool || !name || slot < 0 || slot >= pool->max_slots || !pool->slots[slot].used) return COV_EINVAL;
@@ -3139,10 +3275,11 @@ int cov_pool_set_slot_param(cov_pool *pool, int32_t slot, const char *name, int6
         if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
         return COV_OK;
     }
-    if (!strcmp(name, "adjust_mode")) {
+    if (!strcmp(name, "adjust_mode") || !strcmp(name, "wide_sliced")) {
         // 0: per-lane private-count updates, 1: warp-aggregated, -1: by estimate
-        if (value < -1 || value > 1) return COV_EINVAL;
-        h.d.padj_warp = value < 0 ? padj_auto(h.d.q, h.d.n, h.d.R, h.d.M) : (int)value;
+        if (value < (name[0] == 'a' ? -1 : 0) || value > 1) return COV_EINVAL;
+        if (name[0] == 'w') h.d.wide_sliced = (int)value;
+        else h.d.padj_warp = value < 0 ? padj_auto(h.d.q, h.d.n, h.d.R, h.d.M) : (int)value;
         pool->all_dirty = true;
         int rc = push_slot(pool, slot);
         if (rc) return rc;

@@ -50,7 +50,8 @@ class CovParams(ctypes.Structure):
     _fields_ = [("q", ctypes.c_int32), ("n", ctypes.c_int32), ("R", ctypes.c_int32),
                 ("M", ctypes.c_int32), ("seed", ctypes.c_uint64), ("tabu", ctypes.c_int32),
                 ("kick", ctypes.c_int32), ("cand", ctypes.c_int32), ("trace", ctypes.c_int32),
-                ("stall", ctypes.c_int64), ("trace_cap", ctypes.c_int64)]
+                ("stall", ctypes.c_int64), ("trace_cap", ctypes.c_int64), ("wide", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class CovStatus(ctypes.Structure):

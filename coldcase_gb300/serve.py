@@ -83,7 +83,8 @@ class Server:
     def submit(self, req, now=None):
         req = dict(req)
         req.setdefault("arrival", now if now is not None else time.monotonic())
-        req["bytes"] = slot_bytes(req["q"], req["n"], req["R"], req["M"], tabu=req.get("tabu", 0))
+        req["bytes"] = slot_bytes(req["q"], req["n"], req["R"], req["M"], tabu=req.get("tabu", 0),
+                                  wide=req.get("wide", False))
         if req["bytes"] == 0:
             raise ValueError("request outside the engine's domain: %r" % (req,))
         self.waiting.append(req)
@@ -107,7 +108,7 @@ class Server:
                 if code is None:
                     code = uniform_code(r["q"], r["n"], r["M"], r["seed"])
                 s = self.pool.add(r["q"], r["n"], r["R"], r["M"], code=code, seed=r["seed"],
-                                  tabu=r.get("tabu", 0))
+                                  tabu=r.get("tabu", 0), wide=r.get("wide", False))
                 r["cluster"] = self._cluster(r)
                 self.pool.set_slot_param(s, "cluster", r["cluster"])
                 r["cur_cluster"] = r["cluster"]

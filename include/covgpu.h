@@ -63,7 +63,7 @@ typedef struct {
  *
  * Replaces the process boundary covengine / campaign.py cross today
  * (cov/engine/covengine:624-643, cov/campaign.py:54-86): the arguments are
- * covsearch2e's -q -n -R -M -s --tabu --kick --stall --cand
+ * covsearch2e's -q -n -R -M -s --tabu --kick --stall --cand --wide
  * (cov/engine/covsearch2e.c:1042-1095).
  * --------------------------------------------------------------------- */
 typedef struct cov_pool cov_pool;
@@ -77,6 +77,9 @@ typedef struct {
     int32_t trace;        /* 1 = keep a cov_move_rec per move               */
     int64_t stall;        /* --stall  moves without improvement (5000)      */
     int64_t trace_cap;    /* records kept when trace = 1                    */
+    int32_t wide;         /* --wide  all n(q-1) moves of a candidate codeword
+                           *         (covsearch2e.c:1353-1376); 0 = off     */
+    int32_t reserved;     /* 0                                              */
 } cov_params;
 
 typedef struct {
@@ -106,7 +109,9 @@ int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value);
  * "neg_cluster_pairs" and "list_cost" (this slot only), "adjust_mode"
  * (private-count upkeep of a commit: 0 per thread, 1 aggregated per warp,
  * -1 chosen from the expected event count), "it_limit" (iteration count at which
- * the slot stops; -1 none).  chain_run (cov/gemm2/chainsolve.cu:370-375)
+ * the slot stops; -1 none), "wide_sliced" (the --wide list pass finds the
+ * hits of up to 64 candidates by bit-sliced counts: 1, the default; or tests
+ * every pair: 0).  None changes a trajectory.  chain_run (cov/gemm2/chainsolve.cu:370-375)
  * takes one iteration budget for all chains; covengine gives each chain its
  * own time budget (cov/engine/covengine:624-643). */
 int cov_pool_set_slot_param(cov_pool *pool, int32_t slot, const char *name, int64_t value);

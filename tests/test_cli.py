@@ -18,7 +18,7 @@ def run_cli(args, timeout=300):
                           timeout=timeout, cwd=REPO)
 
 
-@pytest.mark.parametrize("flag", ["--wide", "--sa", "--fix0", "--ucache", "--upick"])
+@pytest.mark.parametrize("flag", ["--sa", "--fix0", "--ucache", "--upick"])
 def test_trajectory_switches_refused(flag):
     r = run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", flag])
     assert r.returncode == 2 and "trajectory" in r.stderr
@@ -36,6 +36,7 @@ def test_bad_arguments_exit_2():
 def test_cli_matches_reference_runs(covlib, golden):
     runs, _ = golden
     picked = [r for r in runs if r["code"] and not r["random_init"]][:6]
+    picked += [r for r in runs if r["code"] and r.get("wide")]
     for r in picked:
         with tempfile.TemporaryDirectory() as td:
             inp, out = os.path.join(td, "in.txt"), os.path.join(td, "out.txt")
@@ -43,7 +44,7 @@ def test_cli_matches_reference_runs(covlib, golden):
                 f.write(r["code"])
             args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
                     "--tabu", r["tabu"], "--kick", r["kick"], "--stall", r["stall"], "--in", inp, "--out", out,
-                    "--preset", "p5b", "--quiet"]
+                    "--preset", "p5b", "--quiet"] + (["--wide"] if r.get("wide") else [])
             p = run_cli(args)
             m = re.search(r"RESULT .*uncovered=(\d+) iters=(\d+) kicks=(\d+)", p.stdout)
             assert m, p.stdout + p.stderr

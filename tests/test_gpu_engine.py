@@ -35,7 +35,7 @@ def gpu_run(run, cluster):
     code = code_from_text(run["code"], run["n"]) if run["code"] else None
     s = pool.add(run["q"], run["n"], run["R"], run["M"], code=code, random_init=run["random_init"],
                  seed=run["seed"], tabu=run["tabu"], kick=run["kick"], stall=run["stall"],
-                 trace=1, trace_cap=max(1, run["iters"]))
+                 trace=1, trace_cap=max(1, run["iters"]), wide=run.get("wide", False))
     pool.run(run["iters"])
     return pool, s
 
@@ -119,3 +119,46 @@ def test_chunked_runs_equal_one_run(covlib, golden):
         b.run(k)
         left -= k
     assert a.trace(sa).tobytes() == b.trace(sb).tobytes()
+
+
+def test_wide_variants_match_oracle(covlib, golden):
+    """--wide through every entering-side route: the bit-sliced and the
+    pairwise list pass, one CTA or the whole cluster sharing the pass, and a
+    candidate cap below the candidate count (sampled subsets)."""
+    from oracle.pyoracle import Oracle
+    runs, _ = golden
+    wide = [r for r in runs if r.get("wide")]
+    assert wide
+    cases = []
+    for r in wide[:4]:
+        cases.append((r, dict(cluster=1, wide_sliced=0), 100000))
+        cases.append((r, dict(cluster=4, neg_cluster_pairs=0), 100000))
+        cases.append((r, dict(cluster=2, neg_cluster_pairs=0, wide_sliced=0), 100000))
+    for r in wide[:3]:
+        cases.append((r, dict(cluster=2), 37))
+    bad = []
+    for r, prm, cand in cases:
+        pool = Pool(1, cluster=prm.get("cluster", 1))
+        code = code_from_text(r["code"], r["n"]) if r["code"] else None
+        s = pool.add(r["q"], r["n"], r["R"], r["M"], code=code, random_init=r["random_init"], seed=r["seed"],
+                     tabu=r["tabu"], kick=r["kick"], stall=r["stall"], cand=cand, trace=1,
+                     trace_cap=r["iters"], wide=True)
+        for k, v in prm.items():
+            if k != "cluster":
+                pool.set_slot_param(s, k, v)
+        pool.run(r["iters"])
+        o = Oracle(r["q"], r["n"], r["R"], r["M"], seed=r["seed"], tabu=r["tabu"], kick=r["kick"],
+                   stall=r["stall"], cand=cand, wide=True)
+        o.init(code, random_init=r["random_init"])
+        otr = o.run(r["iters"], trace=True)
+        gtr = pool.trace(s)
+        st = pool.status(s)
+        ok = st["status"] == 0 and gtr.tobytes() == otr.tobytes() and (pool.cnt(s) == o.cnt()).all()
+        ok = ok and (st["ul_valid"], st["ul_n"]) == o.ul_state()
+        if not ok:
+            k, g1, o1 = first_diff(gtr, otr)
+            bad.append(dict(cell=(r["q"], r["n"], r["R"], r["M"], r["seed"]), prm=prm, cand=cand, first=k,
+                            status=st["status"], ul=((st["ul_valid"], st["ul_n"]), o.ul_state()),
+                            gpu=None if g1 is None else g1.tolist(), orc=None if o1 is None else o1.tolist()))
+        pool.close()
+    assert not bad, bad[:3]
