@@ -21,6 +21,9 @@
  *   - initial code: exact-M rebuild, greedy placement,
  *     remove-and-repair descent                         covsearch2e.c:1156-1240
  *   - code-file writer (M distinct words, top-up)       covsearch2e.c:791-853
+ * the quotient search (symoracle.c):
+ *   - orbit balls, sphere-difference move, estimate,
+ *     greedy init, kicks                                symsearch.c:135-475
  * and the verification side:
  *   - verify_pure ball marking                          cov/verify_cov.py:109-152
  *   - run_mindist per-word minimum distance             cov/verify_independent.py:144-186
@@ -85,6 +88,28 @@ void orc_eval_codeword(cov_oracle *o, int i, long long *dvec);
  * with the lowest unused word indices.  out holds M*n digits. */
 int orc_distinct_code(int q, int n, int M, const uint8_t *cw, int nw,
                       uint8_t *out);
+
+/* ---- quotient search (cov/engine/symsearch.c) ----------------------- */
+typedef struct sym_oracle sym_oracle;
+/* symsearch's -q -n -R -M --orbits -s --kick --stall --cand; NULL where the
+ * reference exits 2 or 3 (symsearch.c:311-333).  orbits <= 0: M / q. */
+sym_oracle *sym_create(int q, int n, int R, int M, int orbits, uint64_t seed,
+                       int kick, long long stall, int cand);
+void sym_destroy(sym_oracle *o);
+/* greedy orbit placement; returns the uncovered quotient words */
+long long sym_init(sym_oracle *o);
+/* up to max_moves iterations; trace (capacity max_moves) gets one
+ * cov_move_rec per move, with ncw = the candidate sample size */
+long long sym_run(sym_oracle *o, long long max_moves, cov_move_rec *trace);
+long long sym_uncovered(const sym_oracle *o);
+long long sym_best_uncovered(const sym_oracle *o);
+long long sym_iters(const sym_oracle *o);
+long long sym_kicks(const sym_oracle *o);
+int sym_orbits(const sym_oracle *o);
+void sym_get_rep(const sym_oracle *o, uint8_t *out);    /* orbits x (n-1) */
+void sym_get_best(const sym_oracle *o, uint8_t *out);   /* orbits x (n-1) */
+void sym_get_cnt(const sym_oracle *o, uint16_t *out);   /* q^(n-1) */
+void sym_get_rng(const sym_oracle *o, uint64_t out[4]);
 
 /* ---- verification side ---------------------------------------------- */
 /* multiplicity cnt[x] = #{i : d(x, c_i) <= R} (multiset), saturated at 65535 */

@@ -58,6 +58,23 @@ def load():
     lib.orc_set_wide.restype = ctypes.c_int
     lib.orc_set_wide.argtypes = [P, ctypes.c_int]
     lib.orc_ul_state.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    lib.sym_create.restype = P
+    lib.sym_create.argtypes = [ctypes.c_int] * 5 + [ctypes.c_uint64, ctypes.c_int, ctypes.c_longlong,
+                                                    ctypes.c_int]
+    lib.sym_destroy.argtypes = [P]
+    lib.sym_init.restype = ctypes.c_longlong
+    lib.sym_init.argtypes = [P]
+    lib.sym_run.restype = ctypes.c_longlong
+    lib.sym_run.argtypes = [P, ctypes.c_longlong, ctypes.POINTER(MoveRec)]
+    for f in ("sym_uncovered", "sym_best_uncovered", "sym_iters", "sym_kicks"):
+        getattr(lib, f).restype = ctypes.c_longlong
+        getattr(lib, f).argtypes = [P]
+    lib.sym_orbits.restype = ctypes.c_int
+    lib.sym_orbits.argtypes = [P]
+    lib.sym_get_rep.argtypes = [P, u8p]
+    lib.sym_get_best.argtypes = [P, u8p]
+    lib.sym_get_cnt.argtypes = [P, ctypes.POINTER(ctypes.c_uint16)]
+    lib.sym_get_rng.argtypes = [P, ctypes.POINTER(ctypes.c_uint64)]
     lib.orc_distinct_code.restype = ctypes.c_int
     lib.orc_distinct_code.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int, u8p]
     lib.orc_cover_count.restype = ctypes.c_int
@@ -294,3 +311,66 @@ def finish(text, q, n, R, M, fast=False):
         mark(new)
     unc = int((~cov).sum())
     return code, unc, 0 if unc == 0 else 1
+
+
+class SymOracle:
+    """One restated symsearch run (cov/engine/symsearch.c:282-491)."""
+
+    def __init__(self, q, n, R, M, orbits=0, seed=12345, kick=2, stall=3000, cand=100000):
+        self.lib = load()
+        self.q, self.n, self.R, self.M = q, n, R, M
+        self.h = self.lib.sym_create(q, n, R, M, orbits, seed, kick, stall, cand)
+        if not self.h:
+            raise ValueError("symsearch oracle: bad parameters")
+        self.orbits = self.lib.sym_orbits(self.h)
+
+    def init(self):
+        return self.lib.sym_init(self.h)
+
+    def run(self, moves, trace=False):
+        tr = (MoveRec * max(1, int(moves)))() if trace else None
+        made = self.lib.sym_run(self.h, int(moves), tr)
+        if not trace:
+            return made
+        return np.frombuffer(tr, dtype=MOVE_DTYPE, count=max(1, int(moves)))[:made].copy()
+
+    def uncovered(self):
+        return self.lib.sym_uncovered(self.h)
+
+    def best_uncovered(self):
+        return self.lib.sym_best_uncovered(self.h)
+
+    def iters(self):
+        return self.lib.sym_iters(self.h)
+
+    def kicks(self):
+        return self.lib.sym_kicks(self.h)
+
+    def _reps(self, fn):
+        out = np.zeros((self.orbits, self.n - 1), dtype=np.uint8)
+        fn(self.h, _u8(out))
+        return out
+
+    def rep(self):
+        return self._reps(self.lib.sym_get_rep)
+
+    def best(self):
+        return self._reps(self.lib.sym_get_best)
+
+    def cnt(self):
+        out = np.zeros(self.q ** (self.n - 1), dtype=np.uint16)
+        self.lib.sym_get_cnt(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)))
+        return out
+
+    def rng(self):
+        out = np.zeros(4, dtype=np.uint64)
+        self.lib.sym_get_rng(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.sym_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

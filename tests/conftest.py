@@ -30,3 +30,12 @@ def golden():
     with open(os.path.join(here, "verify_cases.json")) as f:
         cases = json.load(f)
     return runs, cases
+
+
+@pytest.fixture(scope="session")
+def sym_golden():
+    """The reference quotient search's runs (tests/golden/sym_runs.json)."""
+    import json
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    with open(os.path.join(here, "sym_runs.json")) as f:
+        return json.load(f)

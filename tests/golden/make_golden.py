@@ -16,6 +16,12 @@ Runs in the build container only (it needs the reference checkout):
                           with duplicates, malformed lines, too few and too
                           many words: COUNT line, exit status and --out file,
                           with and without --fast.
+  * sym_runs.json      -- the reference quotient search (oracle/_ref/symsearch,
+                          compiled from cov/engine/symsearch.c) on a cell
+                          list with plain, short-stall and kick-3 runs and
+                          --orbits below M/q: its SYMRESULT fingerprint
+                          (iterations reached, best quotient uncovered,
+                          kicks), exit status and --out file.
   * verify_cases.json  -- codes with their uncovered counts from the
                           reference verifiers verify_pure and verify_numpy
                           (cov/verify_cov.py) and the distance histogram and
@@ -220,6 +226,43 @@ def finish_cases(binary):
     return cases
 
 
+def sym_text(rep, q):
+    """symsearch's --out file: orbit by orbit, its q words (j, e + j)."""
+    return "".join(DIG[j] + "".join(DIG[(int(x) + j) % q] for x in e) + "\n" for e in rep for j in range(q))
+
+
+def sym_runs(binary):
+    """The reference quotient search on a fixed cell list.  It stops on a
+    wall-clock limit only, so each run records the iteration count it
+    reached; a replay makes exactly that many moves."""
+    runs = []
+    cells = [(6, 6, 3, 42, 0, 0.15), (3, 7, 2, 30, 0, 0.1), (4, 6, 2, 40, 0, 0.1), (5, 6, 2, 100, 0, 0.1),
+             (8, 6, 2, 400, 0, 0.2), (6, 8, 4, 168, 0, 0.3), (3, 9, 2, 150, 0, 0.1), (4, 7, 1, 400, 0, 0.1),
+             (3, 6, 0, 300, 0, 0.05), (6, 8, 4, 240, 20, 0.3), (4, 6, 1, 500, 0, 0.1), (7, 5, 2, 140, 0, 0.1),
+             (4, 5, 1, 64, 0, 0.1), (3, 5, 1, 27, 0, 0.1)]
+    for (q, n, R, M, orbits, t) in cells:
+        for s, stall, kick in ((1, 3000, 2), (2, 30, 2), (3, 20, 3)):
+            args = ["-q", q, "-n", n, "-R", R, "-M", M, "-t", t, "-s", s, "--stall", stall, "--kick", kick,
+                    "--threads", 1]
+            if orbits:
+                args += ["--orbits", orbits]
+            with tempfile.TemporaryDirectory() as td:
+                out = os.path.join(td, "out.txt")
+                p = subprocess.run([binary] + [str(a) for a in args] + ["--out", out], capture_output=True,
+                                   text=True)
+                m = re.search(r"SYMRESULT .*orbits=(\d+) red_uncovered=(\d+) word_uncovered=(\d+) "
+                              r"iters=(\d+) kicks=(\d+)", p.stdout)
+                if not m:
+                    raise RuntimeError("no SYMRESULT from %s: %s %s" % (args, p.stdout, p.stderr))
+                with open(out) as f:
+                    body = f.read()
+            runs.append(dict(q=q, n=n, R=R, M=M, orbits=orbits, seed=s, stall=stall, kick=kick,
+                             ref=dict(orbits=int(m.group(1)), red_uncovered=int(m.group(2)),
+                                      word_uncovered=int(m.group(3)), iters=int(m.group(4)),
+                                      kicks=int(m.group(5)), rc=p.returncode, out=body)))
+    return runs
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -235,7 +278,11 @@ def main():
     fc = finish_cases(os.path.join(REPO, "oracle", "_ref", "covcount"))
     with open(os.path.join(HERE, "finish_cases.json"), "w") as f:
         json.dump(fc, f)
-    print("engine runs: %d, verify cases: %d, finish cases: %d" % (len(runs), len(vc), len(fc)))
+    sr = sym_runs(os.path.join(REPO, "oracle", "_ref", "symsearch"))
+    with open(os.path.join(HERE, "sym_runs.json"), "w") as f:
+        json.dump(sr, f)
+    print("engine runs: %d, verify cases: %d, finish cases: %d, quotient runs: %d"
+          % (len(runs), len(vc), len(fc), len(sr)))
 
 
 if __name__ == "__main__":

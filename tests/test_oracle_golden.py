@@ -70,3 +70,18 @@ def test_distinct_code_matches_writer():
         b = codefile.distinct_code(code, q, n, M)
         assert a.tobytes() == b.tobytes()
         assert len({tuple(x) for x in b.tolist()}) == len(b) == min(M, q ** n)
+
+
+def test_sym_runs_match_reference(sym_golden):
+    """The quotient-search restatement against the reference binary: each
+    run replayed for the iterations the reference reached."""
+    from tests.util import sym_oracle_run, sym_text
+    bad = []
+    for r in sym_golden:
+        o, tr = sym_oracle_run(r)
+        ref = r["ref"]
+        got = (o.orbits, o.best_uncovered(), o.iters(), o.kicks())
+        want = (ref["orbits"], ref["red_uncovered"], ref["iters"], ref["kicks"])
+        if got != want or sym_text(o.best(), r["q"]) != ref["out"] or (ref["rc"] == 0) != (got[1] == 0):
+            bad.append((r["q"], r["n"], r["R"], r["M"], r["seed"], got, want))
+    assert not bad, bad

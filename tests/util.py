@@ -22,3 +22,18 @@ def oracle_run(run, threads=1):
     o.init(code, random_init=run["random_init"])
     tr = o.run(run["iters"], trace=True)
     return o, tr
+
+
+def sym_text(rep, q):
+    """symsearch's --out file: orbit by orbit, its q words (j, e + j)."""
+    return "".join(DIG[j] + "".join(DIG[(int(x) + j) % q] for x in e) + "\n" for e in rep for j in range(q))
+
+
+def sym_oracle_run(run, moves=None):
+    """Replay one golden quotient-search run on the oracle: (oracle, trace)."""
+    from oracle.pyoracle import SymOracle
+    o = SymOracle(run["q"], run["n"], run["R"], run["M"], orbits=run["orbits"], seed=run["seed"],
+                  kick=run["kick"], stall=run["stall"])
+    o.init()
+    tr = o.run(run["ref"]["iters"] if moves is None else moves, trace=True)
+    return o, tr
