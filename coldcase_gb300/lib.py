@@ -60,6 +60,13 @@ class CovStatus(ctypes.Structure):
                 ("finished", ctypes.c_int32), ("ul_valid", ctypes.c_int32), ("ul_n", ctypes.c_int32)]
 
 
+class CovSymParams(ctypes.Structure):
+    _fields_ = [("q", ctypes.c_int32), ("n", ctypes.c_int32), ("R", ctypes.c_int32), ("M", ctypes.c_int32),
+                ("orbits", ctypes.c_int32), ("kick", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("stall", ctypes.c_int64), ("cand", ctypes.c_int32), ("trace", ctypes.c_int32),
+                ("trace_cap", ctypes.c_int64)]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _I64 = ctypes.c_int64
@@ -103,6 +110,22 @@ SIGNATURES = {
     "cov_count_above_dev": (ctypes.c_int64, [_I32, _I32, _P, _I32, _P]),
     "cov_mindist_dev_static": (ctypes.c_int, [_I32, _I32, _P, _I32, _P, _P]),
     "cov_finish": (ctypes.c_int, [_I32, _I32, _I32, _I32, _PU8, _I32, _I32, _PU8, _PI32, _PI64]),
+    "cov_sym_create": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_P)]),
+    "cov_sym_destroy": (ctypes.c_int, [_P]),
+    "cov_sym_set_budget": (ctypes.c_int, [_P, ctypes.c_double]),
+    "cov_sym_orbits": (ctypes.c_int, [ctypes.POINTER(CovSymParams)]),
+    "cov_sym_slot_bytes": (ctypes.c_size_t, [ctypes.POINTER(CovSymParams)]),
+    "cov_sym_add": (ctypes.c_int, [_P, ctypes.POINTER(CovSymParams), _PI32]),
+    "cov_sym_remove": (ctypes.c_int, [_P, _I32]),
+    "cov_sym_set_slot_param": (ctypes.c_int, [_P, _I32, ctypes.c_char_p, _I64]),
+    "cov_sym_run": (ctypes.c_int, [_P, _I64]),
+    "cov_sym_status": (ctypes.c_int, [_P, _I32, ctypes.POINTER(CovStatus)]),
+    "cov_sym_resume": (ctypes.c_int, [_P, _I32]),
+    "cov_sym_get_rep": (ctypes.c_int, [_P, _I32, _PU8]),
+    "cov_sym_get_best": (ctypes.c_int, [_P, _I32, _PU8]),
+    "cov_sym_get_cnt": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint16)]),
+    "cov_sym_get_trace": (ctypes.c_int, [_P, _I32, ctypes.POINTER(CovMoveRec), _I64, _PI64]),
+    "cov_sym_get_rng": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64)]),
     "cov_lns_create": (ctypes.c_int, [_I32, _I32, _I32, ctypes.POINTER(_P)]),
     "cov_lns_destroy": (ctypes.c_int, [_P]),
     "cov_lns_recount": (ctypes.c_int, [_P, _PU32, _I32]),

@@ -196,6 +196,55 @@ int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code,
 int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist,
                             int32_t R, void *stream);
 /* ------------------------------------------------------------------------
+ * Quotient search: cov/engine/symsearch.c (the process covengine starts as
+ * BIN['symsearch'], covengine:654-660) as a pool of instances on the GPU.
+ * A code is a union of orbits {(j, e + j) : j in Z_q} of the diagonal
+ * translation; the search runs on the q^(n-1) quotient counters with the
+ * reference's trajectory.  Arguments are symsearch's -q -n -R -M --orbits
+ * -s --kick --stall --cand (symsearch.c:282-310).
+ * --------------------------------------------------------------------- */
+typedef struct cov_sym cov_sym;
+
+typedef struct {
+    int32_t q, n, R, M;
+    int32_t orbits;       /* --orbits (0: M / q)                            */
+    int32_t kick;         /* --kick   (symsearch default 2)                 */
+    uint64_t seed;        /* -s       (12345)                               */
+    int64_t stall;        /* --stall  (3000)                                */
+    int32_t cand;         /* --cand   (100000)                              */
+    int32_t trace;        /* 1 = keep a cov_move_rec per move; its ncw field
+                           * holds the candidate sample size                */
+    int64_t trace_cap;
+} cov_sym_params;
+
+int cov_sym_create(int32_t max_slots, int32_t cluster, cov_sym **out);
+int cov_sym_destroy(cov_sym *pool);
+int cov_sym_set_budget(cov_sym *pool, double seconds);   /* per-launch wall limit */
+/* Orbit count of these parameters, or COV_EINVAL where symsearch exits 2
+ * and COV_ERANGE where it exits 3 (symsearch.c:311-333). */
+int cov_sym_orbits(const cov_sym_params *prm);
+size_t cov_sym_slot_bytes(const cov_sym_params *prm);
+/* Add an instance and place its orbits greedily (symsearch.c:340-356). */
+int cov_sym_add(cov_sym *pool, const cov_sym_params *prm, int32_t *slot);
+int cov_sym_remove(cov_sym *pool, int32_t slot);
+/* "cluster" (CTAs per instance, 1..16) or "it_limit" (stop at exactly this
+ * iteration count; -1 none).  Neither changes a trajectory. */
+int cov_sym_set_slot_param(cov_sym *pool, int32_t slot, const char *name, int64_t value);
+/* Advance every instance by up to `moves` iterations (symsearch.c:376-475);
+ * an instance stops early once its quotient is covered. */
+int cov_sym_run(cov_sym *pool, int64_t moves);
+/* it, uncovered and best count QUOTIENT words (SYMRESULT red_uncovered=);
+ * the code's uncovered words are q times as many. */
+int cov_sym_status(cov_sym *pool, int32_t slot, cov_status *out);
+int cov_sym_resume(cov_sym *pool, int32_t slot);          /* after COV_ETIMEOUT */
+int cov_sym_get_rep(cov_sym *pool, int32_t slot, uint8_t *out);   /* orbits x (n-1) */
+int cov_sym_get_best(cov_sym *pool, int32_t slot, uint8_t *out);  /* orbits x (n-1) */
+int cov_sym_get_cnt(cov_sym *pool, int32_t slot, uint16_t *out);  /* q^(n-1)        */
+int cov_sym_get_trace(cov_sym *pool, int32_t slot, cov_move_rec *out, int64_t cap,
+                      int64_t *n_out);
+int cov_sym_get_rng(cov_sym *pool, int32_t slot, uint64_t *out);  /* 4 words        */
+
+/* ------------------------------------------------------------------------
  * Transform-engine primitives for one cell (q, n, R): the GPU side of the
  * LNS solver, replacing cov/gemm2/dct.cu's C ABI (dct_init, dct_transform,
  * dct_map_max, dct_map_hist, dct_map_extract, dct_map_read_at,

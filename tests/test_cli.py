@@ -54,3 +54,43 @@ def test_cli_matches_reference_runs(covlib, golden):
             assert p.returncode == (0 if ref["uncovered"] == 0 else 1)
             with open(out) as f:
                 assert f.read() == ref["out"]
+
+
+SYM_CLI = os.path.join(REPO, "coldcase_gb300", "bin", "symsearch_gpu")
+
+
+def run_sym_cli(args, timeout=300):
+    return subprocess.run([sys.executable, SYM_CLI] + [str(a) for a in args], capture_output=True, text=True,
+                          timeout=timeout, cwd=REPO)
+
+
+def test_sym_cli_argument_errors():
+    """symsearch.c:311-333: usage errors exit 2, impossible orbit counts,
+    quotients or M exit 3."""
+    assert run_sym_cli(["-q", "4", "-n", "6"]).returncode == 2                     # missing -R -M
+    assert run_sym_cli(["-q", "4", "-n", "6", "-R", "8", "-M", "40"]).returncode == 2  # R > 7
+    assert run_sym_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "3"]).returncode == 2   # M < q
+    assert run_sym_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "40", "--bogus"]).returncode == 2
+    assert run_sym_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "40", "--orbits", "11"]).returncode == 3
+    assert run_sym_cli(["-q", "2", "-n", "6", "-R", "1", "-M", "65536"]).returncode == 3
+
+
+@pytest.mark.gpu
+def test_sym_cli_matches_reference_runs(covlib, sym_golden):
+    for r in [x for x in sym_golden if x["seed"] == 3][:8]:
+        with tempfile.TemporaryDirectory() as td:
+            out = os.path.join(td, "out.txt")
+            args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--kick", r["kick"],
+                    "--stall", r["stall"], "--iters", r["ref"]["iters"], "-t", 120, "--out", out, "--threads", 1]
+            if r["orbits"]:
+                args += ["--orbits", r["orbits"]]
+            p = run_sym_cli(args)
+            m = re.search(r"SYMRESULT .*orbits=(\d+) red_uncovered=(\d+) word_uncovered=(\d+) iters=(\d+) "
+                          r"kicks=(\d+)", p.stdout)
+            assert m, p.stdout + p.stderr
+            ref = r["ref"]
+            assert (int(m.group(1)), int(m.group(2)), int(m.group(4)), int(m.group(5))) == \
+                (ref["orbits"], ref["red_uncovered"], ref["iters"], ref["kicks"]), (r["q"], r["n"], r["R"], r["M"])
+            assert p.returncode == ref["rc"]
+            with open(out) as f:
+                assert f.read() == ref["out"]

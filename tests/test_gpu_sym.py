@@ -1,0 +1,97 @@
+"""CUDA quotient search vs the oracle and the reference's golden runs.
+
+Bit-exact: every move record (picked quotient word, candidate count and
+sample size, committed move, its estimate, uncovered counts, kicks), the
+final RNG state, the quotient counters and the best representatives must
+equal the oracle's; the SYMRESULT fingerprint and the --out file must equal
+the reference binary's.
+"""
+import numpy as np
+import pytest
+
+from coldcase_gb300.sym import SymPool, format_code
+from tests.util import sym_oracle_run
+
+pytestmark = pytest.mark.gpu
+
+
+def first_diff(a, b):
+    for k in range(min(len(a), len(b))):
+        if a[k].tobytes() != b[k].tobytes():
+            return k, a[k], b[k]
+    return min(len(a), len(b)), None, None
+
+
+def gpu_sym(pool, r, iters):
+    s = pool.add(r["q"], r["n"], r["R"], r["M"], orbits=r["orbits"], seed=r["seed"], kick=r["kick"],
+                 stall=r["stall"], trace=1, trace_cap=max(1, iters))
+    return s
+
+
+@pytest.mark.parametrize("cluster", [1, 4])
+def test_sym_golden_runs_bit_exact(covlib, sym_golden, cluster):
+    bad = []
+    for r in sym_golden:
+        ref = r["ref"]
+        pool = SymPool(1, cluster=cluster)
+        s = gpu_sym(pool, r, ref["iters"])
+        pool.run(ref["iters"])
+        st = pool.status(s)
+        o, otr = sym_oracle_run(r)
+        gtr = pool.trace(s)
+        got = (st["best"], st["it"], st["kicks"])
+        want = (ref["red_uncovered"], ref["iters"], ref["kicks"])
+        ok = st["status"] == 0 and got == want and format_code(pool.best(s), r["q"]) == ref["out"]
+        ok = ok and gtr.tobytes() == otr.tobytes() and (pool.rng(s) == o.rng()).all()
+        ok = ok and (pool.cnt(s) == o.cnt()).all() and (pool.rep(s) == o.rep()).all()
+        if not ok:
+            k, g1, o1 = first_diff(gtr, otr)
+            bad.append(dict(cell=(r["q"], r["n"], r["R"], r["M"], r["orbits"], r["seed"]), got=got, want=want,
+                            status=st["status"], ntr=(len(gtr), len(otr)), first=k,
+                            gpu=None if g1 is None else g1.tolist(), orc=None if o1 is None else o1.tolist()))
+        pool.close()
+    assert not bad, bad[:3]
+
+
+def test_sym_chunks_and_batch_equal_single_runs(covlib, sym_golden):
+    """Short launches equal one long one, and instances sharing a pool (one
+    launch per cluster size) each follow their own trajectory."""
+    runs = [r for r in sym_golden if r["seed"] == 2][:6]
+    single = []
+    for r in runs:
+        pool = SymPool(1, cluster=2)
+        s = gpu_sym(pool, r, 3000)
+        left = 3000
+        while left > 0:
+            k = min(left, 257)
+            pool.run(k)
+            left -= k
+        single.append(pool.trace(s))
+        pool.close()
+    pool = SymPool(len(runs), cluster=1)
+    slots = [gpu_sym(pool, r, 3000) for r in runs]
+    for k, s in enumerate(slots):
+        pool.set_slot_param(s, "cluster", 1 + (k % 3))
+    pool.run(3000)
+    for r, s, tr in zip(runs, slots, single):
+        o, otr = sym_oracle_run(r, moves=3000)
+        assert tr.tobytes() == otr.tobytes(), (r["q"], r["n"], r["R"], r["M"])
+        assert pool.trace(s).tobytes() == otr.tobytes(), (r["q"], r["n"], r["R"], r["M"])
+    pool.close()
+
+
+def test_sym_big_quotient_parity(covlib):
+    """K_8(9,4) shape (quotient 8^8 = 16.7M counters, 117 orbits) for 40
+    moves at cluster 16 against the oracle."""
+    from oracle.pyoracle import SymOracle
+    q, n, R, M = 8, 9, 4, 940
+    o = SymOracle(q, n, R, M, seed=1000)
+    o.init()
+    otr = o.run(40, trace=True)
+    with SymPool(1, cluster=16) as pool:
+        s = pool.add(q, n, R, M, seed=1000, trace=1, trace_cap=40)
+        pool.run(40)
+        gtr = pool.trace(s)
+        k, g1, o1 = first_diff(gtr, otr)
+        assert len(gtr) == len(otr) and k == len(otr), (k, g1, o1)
+        assert (pool.cnt(s) == o.cnt()).all()
