@@ -19,7 +19,10 @@
 // go out through the leader's shared memory and CTAs meet only at hardware
 // cluster barriers.  Counters are 16 bits (as the reference's), two to a
 // 32-bit word, updated by 32-bit atomics: a count never exceeds 65000 and
-// never drops below zero, so one half never carries into the other.
+// never drops below zero, so one half never carries into the other.  Beside
+// them a 2-bit shadow min(cnt, 2) (4 words a byte, the layout of
+// covsearch2e's opt_st = 2) serves the estimates and the pick: 8 MB for the
+// 16.7M quotient words of K_8(9,4), so that many instances stay in L2.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -35,6 +38,8 @@ namespace cg = cooperative_groups;
 #define SYM_TS 4096             // candidates held in shared memory
 #define SYM_MAXR 7              // symsearch.c:311
 #define SYM_PB 16               // pick probes drawn per batch
+#define SYM_CT 2048             // centre-table entries (sampled candidates x q)
+#define SYM_INV 2048            // moduli with a reciprocal in shared memory
 #define SYM_CYCLES_PER_NS 2ull
 
 enum { SOP_STOP = 0, SOP_ORBIT = 1, SOP_EVAL = 2, SOP_COMMIT = 3 };
@@ -47,6 +52,10 @@ struct SymState {
     long long it, unc, best_unc, since_improve, nkicks, trace_n, moves_left, it_limit;
     int init_i;                  // orbits placed by the greedy initialisation
     int status, finished, pad;
+    // leader cycles by phase, accumulated over launches: 0 pick, 1
+    // candidates, 2 sample, 3 estimate op, 4 selection, 5 commit op, 6 orbit
+    // ops, 7 the rest; 8 moves counted
+    unsigned long long prof[9];
 };
 
 struct SymSlot {
@@ -66,7 +75,14 @@ struct SymSlot {
     int boff[SYM_MAXR + 2];      // first r-subset of bsub
     const uint8_t *wsub[2];      // [NR][wnc][rs]: subsets avoiding position p
     const uint8_t *bsub;         // r-subsets of all NR positions, r = 1..R
+    uint32_t inv_qm1;            // ceil(2^32 / (q-1))
+    uint64_t inv_pp[SYM_MAXR + 1];   // ceil(2^64 / (q-1)^k)
+    uint64_t inv_wit1, inv_bit1;     // ceil(2^64 / witems[1]), ceil(2^64 / bitems[1])
+    uint64_t inv_ipc;                // ceil(2^64 / ipc)
+    uint64_t inv_N;                  // floor((2^64-1) / N)
     uint32_t *cnt2;              // [ceil(N/2)] two 16-bit counters per word
+    uint32_t *st2;               // min(cnt, 2) per word, 2 bits each; padded to whole
+                                 // 16-byte windows plus one
     uint64_t *rep, *best;        // [norb] representatives, packed digits
     uint32_t *cands;             // [norb*q*NR + 8] candidates (oversized case)
     int32_t *cd;                 // [norb*q*NR + 8] estimates
@@ -75,8 +91,16 @@ struct SymSlot {
     SymState *st;
 };
 
+// centres of one orbit's q balls and, for a move, their word offsets
+struct SymCentres {
+    uint64_t cpk[COV_MAXQ];
+    uint32_t base[COV_MAXQ];
+    uint32_t dv[COV_MAXQ];
+};
+
 struct SymSmem {
     SymSlot slot;
+    SymCentres ct;
     // op broadcast by the leader (read by every CTA through DSMEM)
     int op, oi, opos, oval, osign, take;
     unsigned long long acc;      // uncovered change accumulated by an op
@@ -86,6 +110,8 @@ struct SymSmem {
     int init_i, status, finished, phase, kick_t, cand_sm;
     unsigned long long deadline;
     long long guard, est;
+    unsigned long long prof[9];
+    long long t_mark;
     cov_move_rec rec;
     // scratch
     int red_i[SNW];
@@ -94,7 +120,10 @@ struct SymSmem {
     uint32_t probe[SYM_PB];
     CovRng pstate[SYM_PB];
     uint32_t cand[SYM_TS];       // candidates (leader); the sample (every CTA)
-    uint64_t samp_pk[SYM_TS];    // representative of each sampled candidate's orbit
+    uint64_t tcpk[SYM_CT];       // centres of the sampled candidates: [s*q + delta]
+    uint32_t tbase[SYM_CT];
+    uint32_t tdv[SYM_CT];
+    uint64_t inv[SYM_INV + 1];   // floor((2^64-1)/m): leader's modular reductions
     int32_t cdv[SYM_TS];
     uint8_t skip[SYM_TS];
 };
@@ -111,6 +140,23 @@ __device__ __forceinline__ int sym_add(const SymSlot &d, uint32_t w, int s)
     const uint32_t sh = (w & 1u) * 16u;
     const uint32_t old = atomicAdd(&d.cnt2[w >> 1], (uint32_t)s << sh);
     return (int)((old >> sh) & 0xffffu);
+}
+
+// min(cnt[w], 2) from the shadow
+__device__ __forceinline__ int sym_st(const SymSlot &d, uint32_t w)
+{
+    return (int)((cov_ldcg(&d.st2[w >> 4]) >> (2u * (w & 15u))) & 3u);
+}
+
+// bring the shadow of w in line with its (final) count
+__device__ __forceinline__ void sym_fix(const SymSlot &d, uint32_t w)
+{
+    const int c = min(sym_cnt(d, w), 2);
+    const uint32_t sh = 2u * (w & 15u);
+    uint32_t *word = &d.st2[w >> 4];
+    if ((int)((cov_ldcg(word) >> sh) & 3u) == c) return;
+    atomicAnd(word, ~(3u << sh));
+    if (c) atomicOr(word, (uint32_t)c << sh);
 }
 
 __device__ __forceinline__ void sym_error(const SymSlot &d, int code)
@@ -194,92 +240,164 @@ __device__ __forceinline__ uint32_t sym_centre(const SymSlot &d, uint64_t e, int
 }
 
 // ----------------------------------------------------------- the walks ----
-// Walk item `loc` of the sub-move delta of candidate (e, p, v): one subset
-// of positions other than p and values for all but its last position; the
-// q-1 values of the last position are the inner loop.  Each word a differs
-// from the centre exactly on the subset; b = a with position p moved
-// (symsearch.c:177-205).  mode 0: (cnt[a]==1) - (cnt[b]==0) against the
-// unchanged counters; mode 1: the exact move.
-template <int MODE>
-__device__ __forceinline__ long long sym_walk_item(const SymSlot &d, uint64_t e, int p, int v, int delta,
-                                                   uint32_t loc)
+// Divisions by the slot's fixed divisors go through multiply-high with
+// precomputed reciprocals: x / (q-1) for x < 2^24 with a 32-bit one, x / m
+// for x < 2^32 with a 64-bit one (both exact in those ranges).
+__device__ __forceinline__ uint32_t sym_div_qm1(const SymSlot &d, uint32_t x)
 {
-    const int q = d.q, t = delta ? 1 : 0, rad = d.R - t;
-    const uint32_t base = sym_centre(d, e, delta);
-    const int cp = sym_cdig(d, e, delta, p);
-    int nv = v + delta;
-    if (nv >= q) nv -= q;
-    const uint32_t dv = (uint32_t)((nv - cp) * (int)d.pw[p]);
+    return d.q == 2 ? x : __umulhi(x, d.inv_qm1);
+}
+__device__ __forceinline__ uint32_t sym_div64(uint32_t x, uint32_t m, uint64_t inv)
+{
+    return m == 1 ? x : (uint32_t)__umul64hi((uint64_t)x, inv);
+}
+
+// Centres of the q balls of orbit e (radius R at e, R-1 at e + delta) and,
+// for a move of position p to v, the offset each centre's word index moves
+// by (symsearch.c:162-174, :216-224); built by threads 0..q-1.
+__device__ void sym_centres(const SymSlot &d, SymCentres &C, uint64_t e, int p, int v)
+{
+    const int dl = threadIdx.x;
+    if (dl < d.q && d.R - (dl != 0) >= 0) {
+        uint64_t c = 0;
+        uint32_t x = 0;
+        for (int j = 0; j < d.NR; j++) {
+            int cj = cov_nib(e, j) + dl;
+            if (cj >= d.q) cj -= d.q;
+            c = cov_setnib(c, j, cj);
+            x += (uint32_t)cj * d.pw[j];
+        }
+        C.cpk[dl] = c;
+        C.base[dl] = x;
+        if (p >= 0) {
+            int nv = v + dl;
+            if (nv >= d.q) nv -= d.q;
+            C.dv[dl] = (uint32_t)((nv - cov_nib(c, p)) * (int)d.pw[p]);
+        }
+    }
+}
+
+// one 32-bit word of the eight loaded as two uint4
+__device__ __forceinline__ uint32_t sym_pick8(const uint4 &lo, const uint4 &hi, int i)
+{
+    const uint4 &h = (i & 4) ? hi : lo;
+    return (i & 2) ? ((i & 1) ? h.w : h.z) : ((i & 1) ? h.y : h.x);
+}
+
+// Walk item r in [0, ipc) of a move of position p: its sub-move delta, one
+// subset of the other positions and values for all but the subset's last
+// position; the q-1 values of the last position are the inner loop.  Each
+// word a differs from the centre exactly on the subset; b is a with
+// position p moved (symsearch.c:177-205).  MODE 0: (cnt[a]==1) - (cnt[b]==0)
+// against the unchanged counters (read from the 2-bit shadow); MODE 1: the
+// move itself on the counters; MODE 2: refresh the shadow of a and b.
+// cpk/base/dv: the centres' packed digits, word indices and move offsets,
+// indexed by delta.
+template <int MODE>
+__device__ __forceinline__ long long sym_walk_item(const SymSlot &d, const uint64_t *cpk, const uint32_t *cbase,
+                                                   const uint32_t *cdv, int p, uint32_t r)
+{
+    int delta = 0;
+    uint32_t loc = r;
+    if (r >= d.witems[0]) {
+        const uint32_t k = sym_div64(r - d.witems[0], d.witems[1], d.inv_wit1);
+        delta = 1 + (int)k;
+        loc = r - d.witems[0] - k * d.witems[1];
+    }
+    const int t = delta ? 1 : 0, rad = d.R - t;
+    const uint64_t c = cpk[delta];
+    const uint32_t base = cbase[delta], dv = cdv[delta];
     long long du = 0;
-    if (rad == 0) {
-        const uint32_t a = base, b = base + dv;
-        if (MODE) {
+    auto visit = [&](uint32_t a) {
+        const uint32_t b = a + dv;
+        if (MODE == 1) {
             const int oa = sym_add(d, a, -1);
             if (oa == 0) sym_error(d, COV_EDRIFT);
             du += oa == 1;
             du -= sym_add(d, b, +1) == 0;
-        } else {
-            du += sym_cnt(d, a) == 1;
-            du -= sym_cnt(d, b) == 0;
+        } else if (MODE == 2) {
+            sym_fix(d, a);
+            sym_fix(d, b);
         }
+    };
+    if (rad == 0) {
+        if (MODE == 0) du += (long long)(sym_st(d, base) == 1) - (long long)(sym_st(d, base + dv) == 0);
+        else visit(base);
         return du;
     }
     const uint32_t pp = d.ppow[rad - 1];
-    const uint32_t kk = loc / pp;
+    const uint32_t kk = sym_div64(loc, pp, d.inv_pp[rad - 1]);
     uint32_t rem = loc - kk * pp;
     const uint8_t *ps = d.wsub[t] + ((size_t)p * d.wnc[t] + kk) * d.rs;
-    const int qm1 = q - 1;
+    const int qm1 = d.q - 1;
     uint32_t w = base;
     for (int k = rad - 2; k >= 0; --k) {
-        const int dig = (int)(rem % (uint32_t)qm1);
-        rem /= (uint32_t)qm1;
-        const int j = ps[k], c = sym_cdig(d, e, delta, j);
-        w += (uint32_t)((dig + (dig >= c) - c) * (int)d.pw[j]);
+        const uint32_t qt = sym_div_qm1(d, rem);
+        const int dig = (int)(rem - qt * (uint32_t)qm1);
+        rem = qt;
+        const int j = ps[k], cj = cov_nib(c, j);
+        w += (uint32_t)((dig + (dig >= cj) - cj) * (int)d.pw[j]);
     }
-    const int last = ps[rad - 1], cl = sym_cdig(d, e, delta, last);
+    const int last = ps[rad - 1], cl = cov_nib(c, last);
     const int pl = (int)d.pw[last];
-    for (int k = 0; k < qm1; k++) {
-        const uint32_t a = w + (uint32_t)((k + (k >= cl) - cl) * pl), b = a + dv;
-        if (MODE) {
-            const int oa = sym_add(d, a, -1);
-            if (oa == 0) sym_error(d, COV_EDRIFT);
-            du += oa == 1;
-            du -= sym_add(d, b, +1) == 0;
-        } else {
-            du += sym_cnt(d, a) == 1;
-            du -= sym_cnt(d, b) == 0;
+    if (MODE == 0) {
+        const uint32_t a0 = w - (uint32_t)(cl * pl);       // the word with digit 0 at `last`
+        if (d.q * pl <= 64) {
+            // the q words a0 + v pl lie in two aligned 16-byte windows of the
+            // shadow (64 words each); so do the b words
+            auto count = [&](uint32_t x0, int want) -> int {
+                const uint32_t w0 = x0 & ~63u;
+                const uint4 lo = __ldcg(reinterpret_cast<const uint4 *>(d.st2 + (w0 >> 4)));
+                uint4 hi = make_uint4(0, 0, 0, 0);
+                if (x0 + (uint32_t)(qm1 * pl) >= w0 + 64) hi = __ldcg(reinterpret_cast<const uint4 *>(d.st2 + (w0 >> 4) + 4));
+                int n = 0;
+                for (int v = 0; v <= qm1; v++) {
+                    if (v == cl) continue;
+                    const int x = (int)(x0 - w0) + v * pl;
+                    n += (int)((sym_pick8(lo, hi, x >> 4) >> (2 * (x & 15))) & 3u) == want;
+                }
+                return n;
+            };
+            return (long long)count(a0, 1) - (long long)count(a0 + dv, 0);
         }
+        // otherwise all 2(q-1) reads of the item are issued before any is used
+        int ca[COV_MAXQ - 1], cb[COV_MAXQ - 1];
+#pragma unroll
+        for (int k = 0; k < COV_MAXQ - 1; k++) {
+            if (k < qm1) {
+                const uint32_t a = w + (uint32_t)((k + (k >= cl) - cl) * pl);
+                ca[k] = sym_st(d, a);
+                cb[k] = sym_st(d, a + dv);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < COV_MAXQ - 1; k++)
+            if (k < qm1) du += (long long)(ca[k] == 1) - (long long)(cb[k] == 0);
+        return du;
     }
+    for (int k = 0; k < qm1; k++) visit(w + (uint32_t)((k + (k >= cl) - cl) * pl));
     return du;
 }
 
-// candidate item r in [0, ipc): its sub-move and the item within it
-__device__ __forceinline__ void sym_split(const SymSlot &d, uint32_t r, int &delta, uint32_t &loc)
+// Ball item r in [0, opi) of an orbit (centres in C): +1 / -1 on every word
+// it names (MODE 1, symsearch.c:135-174; returns the uncovered change) or
+// the refresh of their shadow (MODE 2)
+template <int MODE>
+__device__ __forceinline__ long long sym_ball_item(const SymSlot &d, const SymCentres &C, uint32_t r, int sign)
 {
-    if (r < d.witems[0]) { delta = 0; loc = r; return; }
-    r -= d.witems[0];
-    const uint32_t k = r / d.witems[1];
-    delta = 1 + (int)k;
-    loc = r - k * d.witems[1];
-}
-
-// Ball item r in [0, opi) of orbit e: +1 or -1 on every word it names
-// (symsearch.c:135-174); returns the uncovered change
-__device__ __forceinline__ long long sym_ball_item(const SymSlot &d, uint64_t e, uint32_t r, int sign)
-{
-    int delta;
-    uint32_t loc;
-    if (r < d.bitems[0]) { delta = 0; loc = r; }
-    else {
-        r -= d.bitems[0];
-        const uint32_t k = r / d.bitems[1];
+    int delta = 0;
+    uint32_t loc = r;
+    if (r >= d.bitems[0]) {
+        const uint32_t k = sym_div64(r - d.bitems[0], d.bitems[1], d.inv_bit1);
         delta = 1 + (int)k;
-        loc = r - k * d.bitems[1];
+        loc = r - d.bitems[0] - k * d.bitems[1];
     }
-    const int q = d.q, qm1 = q - 1;
-    const uint32_t base = sym_centre(d, e, delta);
+    const int qm1 = d.q - 1;
+    const uint64_t c = C.cpk[delta];
+    const uint32_t base = C.base[delta];
     long long du = 0;
     auto touch = [&](uint32_t w) {
+        if (MODE == 2) { sym_fix(d, w); return; }
         const int old = sym_add(d, w, sign);
         if (sign > 0) du -= old == 0;
         else {
@@ -293,33 +411,46 @@ __device__ __forceinline__ long long sym_ball_item(const SymSlot &d, uint64_t e,
     while (rr <= SYM_MAXR && loc >= d.bcum[rr + 1]) rr++;
     loc -= d.bcum[rr];
     const uint32_t pp = d.ppow[rr - 1];
-    const uint32_t kk = loc / pp;
+    const uint32_t kk = sym_div64(loc, pp, d.inv_pp[rr - 1]);
     uint32_t rem = loc - kk * pp;
     const uint8_t *ps = d.bsub + (size_t)(d.boff[rr] + (int)kk) * d.rs;
     uint32_t w = base;
     for (int k = rr - 2; k >= 0; --k) {
-        const int dig = (int)(rem % (uint32_t)qm1);
-        rem /= (uint32_t)qm1;
-        const int j = ps[k], c = sym_cdig(d, e, delta, j);
-        w += (uint32_t)((dig + (dig >= c) - c) * (int)d.pw[j]);
+        const uint32_t qt = sym_div_qm1(d, rem);
+        const int dig = (int)(rem - qt * (uint32_t)qm1);
+        rem = qt;
+        const int j = ps[k], cj = cov_nib(c, j);
+        w += (uint32_t)((dig + (dig >= cj) - cj) * (int)d.pw[j]);
     }
-    const int last = ps[rr - 1], cl = sym_cdig(d, e, delta, last);
+    const int last = ps[rr - 1], cl = cov_nib(c, last);
     const int pl = (int)d.pw[last];
     for (int k = 0; k < qm1; k++) touch(w + (uint32_t)((k + (k >= cl) - cl) * pl));
     return du;
 }
 
 // ----------------------------------------------------------------- ops ----
-__device__ void sym_op_orbit(const SymSlot &d, SymSmem &S, SymSmem *LS, int rank, int csize, int i, int sign)
+// The counters change first; after a cluster barrier the same words get
+// their shadow refreshed from the final counts (a word may be touched by
+// several threads, so the shadow is only written once its count is final).
+__device__ void sym_op_orbit(const SymSlot &d, SymSmem &S, SymSmem *LS, cg::cluster_group &cl, int rank,
+                             int csize, int i, int sign)
 {
-    const uint64_t e = cov_ldcg(&d.rep[i]);
+    sym_centres(d, S.ct, cov_ldcg(&d.rep[i]), -1, 0);
+    sym_bar();
     long long du = 0;
     const uint32_t stride = (uint32_t)csize * SNT;
-    for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.opi; r += stride) du += sym_ball_item(d, e, r, sign);
+    for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.opi; r += stride)
+        du += sym_ball_item<1>(d, S.ct, r, sign);
     du = sym_block_sum(S, du);
     if (threadIdx.x == 0 && du) atomicAdd(&LS->acc, (unsigned long long)du);
+    cl.sync();
+    for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.opi; r += stride) sym_ball_item<2>(d, S.ct, r, 0);
 }
 
+// Estimates of the sampled moves.  Flat: every CTA holds the centres of all
+// sampled candidates (take x q entries) and the cluster's threads run over
+// all (candidate, item) pairs at once.  Nested, for samples too large for
+// that table: candidate by candidate, the threads splitting its items.
 __device__ void sym_op_eval(const SymSlot &d, SymSmem &S, SymSmem *LS, int rank, int csize, int take)
 {
     const bool sm = take <= SYM_TS;
@@ -327,54 +458,100 @@ __device__ void sym_op_eval(const SymSlot &d, SymSmem &S, SymSmem *LS, int rank,
         for (int s = threadIdx.x; s < take; s += SNT) S.cand[s] = LS->cand[s];
         sym_bar();
     }
-    if (sm) {
-        for (int s = threadIdx.x; s < take; s += SNT) S.samp_pk[s] = cov_ldcg(&d.rep[S.cand[s] >> 8]);
+    const uint32_t stride = (uint32_t)csize * SNT;
+    const int q = d.q;
+    if (sm && take * q <= SYM_CT && (unsigned long long)take * d.ipc < (1ull << 32)) {
+        for (int x = threadIdx.x; x < take * q; x += SNT) {
+            const int s = x / q, dl = x - s * q;
+            if (d.R - (dl != 0) < 0) continue;
+            const uint32_t c = S.cand[s];
+            const uint64_t e = cov_ldcg(&d.rep[c >> 8]);
+            const int p = (int)((c >> 4) & 15u), v = (int)(c & 15u);
+            uint64_t pk = 0;
+            uint32_t xw = 0;
+            for (int j = 0; j < d.NR; j++) {
+                int cj = cov_nib(e, j) + dl;
+                if (cj >= q) cj -= q;
+                pk = cov_setnib(pk, j, cj);
+                xw += (uint32_t)cj * d.pw[j];
+            }
+            int nv = v + dl;
+            if (nv >= q) nv -= q;
+            S.tcpk[x] = pk;
+            S.tbase[x] = xw;
+            S.tdv[x] = (uint32_t)((nv - cov_nib(pk, p)) * (int)d.pw[p]);
+        }
+        sym_bar();
+        const uint32_t total = (uint32_t)take * d.ipc;
+        int cur = -1, p = 0;
+        long long acc = 0;
+        for (uint32_t t = (uint32_t)rank * SNT + threadIdx.x; t < total; t += stride) {
+            const int s2 = (int)sym_div64(t, d.ipc, d.inv_ipc);
+            const uint32_t r = t - (uint32_t)s2 * d.ipc;
+            if (s2 != cur) {
+                if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
+                cur = s2;
+                acc = 0;
+                p = (int)((S.cand[s2] >> 4) & 15u);
+            }
+            const int o = s2 * q;
+            acc += sym_walk_item<0>(d, S.tcpk + o, S.tbase + o, S.tdv + o, p, r);
+        }
+        if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
+        return;
+    }
+    for (int s = 0; s < take; s++) {
+        const uint32_t c = sm ? S.cand[s] : cov_ldcg(&d.cands[s]);
+        const int p = (int)((c >> 4) & 15u), v = (int)(c & 15u);
+        sym_centres(d, S.ct, cov_ldcg(&d.rep[c >> 8]), p, v);
+        sym_bar();
+        long long acc = 0;
+        for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.ipc; r += stride)
+            acc += sym_walk_item<0>(d, S.ct.cpk, S.ct.base, S.ct.dv, p, r);
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&d.cd[s], (int)acc);
         sym_bar();
     }
-    const unsigned long long total = (unsigned long long)take * d.ipc;
-    const unsigned long long stride = (unsigned long long)csize * SNT;
-    int cur = -1;
-    long long acc = 0;
-    uint64_t e = 0;
-    int p = 0, v = 0;
-    for (unsigned long long t = (unsigned long long)rank * SNT + threadIdx.x; t < total; t += stride) {
-        const int s = (int)(t / d.ipc);
-        const uint32_t r = (uint32_t)(t - (unsigned long long)s * d.ipc);
-        if (s != cur) {
-            if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
-            cur = s;
-            acc = 0;
-            const uint32_t c = sm ? S.cand[s] : cov_ldcg(&d.cands[s]);
-            e = sm ? S.samp_pk[s] : cov_ldcg(&d.rep[c >> 8]);
-            p = (int)((c >> 4) & 15u);
-            v = (int)(c & 15u);
-        }
-        int delta;
-        uint32_t loc;
-        sym_split(d, r, delta, loc);
-        acc += sym_walk_item<0>(d, e, p, v, delta, loc);
-    }
-    if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
 }
 
-__device__ void sym_op_commit(const SymSlot &d, SymSmem &S, SymSmem *LS, int rank, int csize, int i, int p,
-                              int v)
+__device__ void sym_op_commit(const SymSlot &d, SymSmem &S, SymSmem *LS, cg::cluster_group &cl, int rank,
+                              int csize, int i, int p, int v)
 {
-    const uint64_t e = cov_ldcg(&d.rep[i]);
+    sym_centres(d, S.ct, cov_ldcg(&d.rep[i]), p, v);
+    sym_bar();
     long long du = 0;
     const uint32_t stride = (uint32_t)csize * SNT;
-    for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.ipc; r += stride) {
-        int delta;
-        uint32_t loc;
-        sym_split(d, r, delta, loc);
-        du += sym_walk_item<1>(d, e, p, v, delta, loc);
-    }
+    for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.ipc; r += stride)
+        du += sym_walk_item<1>(d, S.ct.cpk, S.ct.base, S.ct.dv, p, r);
     du = sym_block_sum(S, du);
     if (threadIdx.x == 0 && du) atomicAdd(&LS->acc, (unsigned long long)du);
+    cl.sync();
+    for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.ipc; r += stride)
+        sym_walk_item<2>(d, S.ct.cpk, S.ct.base, S.ct.dv, p, r);
 }
 
 // ------------------------------------------------------ leader routines ----
 __device__ __forceinline__ uint64_t sym_draw(SymSmem &S) { return cov_rng_next(S.rng); }
+
+// x mod m through a reciprocal (one correction at most): the table for small
+// m, the slot's own for N
+__device__ __forceinline__ uint64_t sym_mod(const SymSmem &S, uint64_t x, uint64_t m)
+{
+    if (m <= SYM_INV) {
+        const uint64_t qe = __umul64hi(x, S.inv[m]);
+        uint64_t r = x - qe * m;
+        while (r >= m) r -= m;
+        return r;
+    }
+    return x % m;
+}
+__device__ __forceinline__ uint32_t sym_modN(const SymSlot &d, uint64_t x)
+{
+    const uint64_t qe = __umul64hi(x, d.inv_N);
+    uint64_t r = x - qe * (uint64_t)d.N;
+    while (r >= (uint64_t)d.N) r -= (uint64_t)d.N;
+    return (uint32_t)r;
+}
 
 // 64 uniform probes, then the first zero cyclically after a random start
 // (symsearch.c:268-280).  Probes are drawn in batches with the generator
@@ -387,13 +564,13 @@ __device__ long long sym_pick(const SymSlot &d, SymSmem &S)
         if (tid == 0) {
             CovRng r = S.rng;
             for (int k = 0; k < SYM_PB; k++) {
-                S.probe[k] = (uint32_t)(cov_rng_next(r) % (uint64_t)d.N);
+                S.probe[k] = sym_modN(d, cov_rng_next(r));
                 S.pstate[k] = r;
             }
         }
         sym_bar();
         int hit = 0x7fffffff;
-        if (tid < SYM_PB && sym_cnt(d, S.probe[tid]) == 0) hit = tid;
+        if (tid < SYM_PB && sym_st(d, S.probe[tid]) == 0) hit = tid;
         hit = sym_block_min(S, hit);
         if (hit != 0x7fffffff) {
             const long long w = S.probe[hit];
@@ -405,7 +582,7 @@ __device__ long long sym_pick(const SymSlot &d, SymSmem &S)
         if (tid == 0) S.rng = S.pstate[SYM_PB - 1];
         sym_bar();
     }
-    if (tid == 0) S.ibc[0] = (int)(sym_draw(S) % (uint64_t)d.N);
+    if (tid == 0) S.ibc[0] = (int)sym_modN(d, sym_draw(S));
     sym_bar();
     const uint32_t start = (uint32_t)S.ibc[0];
     sym_bar();
@@ -416,7 +593,7 @@ __device__ long long sym_pick(const SymSlot &d, SymSmem &S)
             if (o >= d.N) break;
             uint32_t w = start + o;
             if (w >= d.N) w -= d.N;
-            if (sym_cnt(d, w) == 0) { best = (int)(o - off); break; }
+            if (sym_st(d, w) == 0) { best = (int)(o - off); break; }
         }
         best = sym_block_min(S, best);
         if (best != 0x7fffffff) {
@@ -439,6 +616,7 @@ __device__ __forceinline__ void sym_emit(SymSmem &S, int op, int i, int p, int v
 {
     S.op = op; S.oi = i; S.opos = p; S.oval = v; S.osign = sign;
     S.acc = 0ull;
+    S.t_mark = sym_clock();
 }
 
 __device__ bool sym_should_stop(const SymSlot &d, SymSmem &S)
@@ -468,7 +646,9 @@ __device__ bool sym_plan_move(const SymSlot &d, SymSmem &S)
     }
     sym_bar();
     if (S.ibc[1]) return false;
+    long long tp = sym_clock();
     const long long uw = sym_pick(d, S);
+    if (tid == 0) { const long long t1 = sym_clock(); S.prof[0] += t1 - tp; tp = t1; }
     if (uw < 0) {
         if (tid == 0) { S.it--; S.status = COV_EDRIFT; }
         sym_bar();
@@ -522,15 +702,16 @@ __device__ bool sym_plan_move(const SymSlot &d, SymSmem &S)
         nc += tot;
     }
     sym_bar();
+    if (tid == 0) { const long long t1 = sym_clock(); S.prof[1] += t1 - tp; tp = t1; }
     // an oversized set is sampled in global memory: its head joins it there
     if (nc > SYM_TS)
         for (int k = tid; k < SYM_TS; k += SNT) d.cands[k] = S.cand[k];
     sym_bar();
     if (tid == 0) {
         if (nc == 0) {                                   // symsearch.c:419-424
-            const int i = (int)(sym_draw(S) % (uint64_t)norb);
-            const int p = (int)(sym_draw(S) % (uint64_t)NR);
-            const int v = (int)(sym_draw(S) % (uint64_t)q);
+            const int i = (int)(sym_mod(S, sym_draw(S), (uint64_t)norb));
+            const int p = (int)(sym_mod(S, sym_draw(S), (uint64_t)NR));
+            const int v = (int)(sym_mod(S, sym_draw(S), (uint64_t)q));
             const uint32_t c = ((uint32_t)i << 8) | ((uint32_t)p << 4) | (uint32_t)v;
             S.cand[0] = c;
             d.cands[0] = c;
@@ -541,7 +722,7 @@ __device__ bool sym_plan_move(const SymSlot &d, SymSmem &S)
         const bool sm = nc <= SYM_TS;
         uint32_t *arr = sm ? S.cand : d.cands;
         for (int s = 0; s < take; s++) {
-            const int j = s + (int)(sym_draw(S) % (uint64_t)(nc - s));
+            const int j = s + (int)sym_mod(S, sym_draw(S), (uint64_t)(nc - s));
             const uint32_t a = arr[s];
             arr[s] = arr[j];
             arr[j] = a;
@@ -560,7 +741,10 @@ __device__ bool sym_plan_move(const SymSlot &d, SymSmem &S)
         for (int s = tid; s < S.take; s += SNT) S.cand[s] = cov_ldcg(&d.cands[s]);
     }
     sym_bar();
-    if (tid == 0) sym_emit(S, SOP_EVAL, 0, 0, 0, 0);
+    if (tid == 0) {
+        S.prof[2] += sym_clock() - tp;
+        sym_emit(S, SOP_EVAL, 0, 0, 0, 0);
+    }
     sym_bar();
     return true;
 }
@@ -593,7 +777,7 @@ __device__ void sym_select(const SymSlot &d, SymSmem &S)
             if (cd < bestd) { bestd = cd; bs = s; nties = 1; }
             else if (cd == bestd) {
                 nties++;
-                if (sym_draw(S) % (uint64_t)nties == 0) bs = s;
+                if (sym_mod(S, sym_draw(S), (uint64_t)nties) == 0) bs = s;
             }
         }
         uint32_t c;
@@ -602,7 +786,7 @@ __device__ void sym_select(const SymSlot &d, SymSmem &S)
             c = sm ? S.cand[bs] : cov_ldcg(&d.cands[bs]);
             i = (int)(c >> 8); p = (int)((c >> 4) & 15u); v = (int)(c & 15u);
         } else {
-            bs = (int)(sym_draw(S) % (uint64_t)take);
+            bs = (int)(sym_mod(S, sym_draw(S), (uint64_t)take));
             c = sm ? S.cand[bs] : cov_ldcg(&d.cands[bs]);
             i = (int)(c >> 8); p = (int)((c >> 4) & 15u); v = (int)(c & 15u);
             if (v == cov_nib(cov_ldcg(&d.rep[i]), p)) v = (v + 1) % d.q;
@@ -628,6 +812,7 @@ __device__ void sym_finish_iter(const SymSlot &d, SymSmem &S)
         if (d.trace && S.trace_n < d.trace_cap) d.trace[S.trace_n] = S.rec;
         if (d.trace) S.trace_n++;
         S.moves_left--;
+        S.prof[8]++;
         if (S.best_unc == 0) S.finished = 1;
     }
 }
@@ -637,6 +822,11 @@ __device__ void sym_finish_iter(const SymSlot &d, SymSmem &S)
 __device__ void sym_leader(const SymSlot &d, SymSmem &S, int mode)
 {
     const int tid = threadIdx.x;
+    if (tid == 0 && S.op > 0) {
+        // the op just run, timed from its emission
+        const long long dt = sym_clock() - S.t_mark;
+        S.prof[S.op == SOP_EVAL ? 3 : S.op == SOP_COMMIT ? 5 : 6] += dt;
+    }
     for (;;) {
         const int ph = S.phase;
         if (ph == SPH_INIT) {
@@ -663,7 +853,7 @@ __device__ void sym_leader(const SymSlot &d, SymSmem &S, int mode)
             }
             long long w = sym_pick(d, S);
             if (tid == 0) {
-                if (w < 0) w = (long long)(sym_draw(S) % (uint64_t)d.N);
+                if (w < 0) w = (long long)sym_modN(d, sym_draw(S));
                 uint64_t pk;
                 sym_word(d, (uint32_t)w, pk);
                 cov_stcg(&d.rep[S.init_i], pk);
@@ -684,7 +874,9 @@ __device__ void sym_leader(const SymSlot &d, SymSmem &S, int mode)
             return;
         }
         if (ph == SPH_SELECT) {
+            const long long ts = sym_clock();
             sym_select(d, S);
+            if (tid == 0) S.prof[4] += sym_clock() - ts;
             if (tid == 0) S.phase = SPH_AFTER_COMMIT;
             sym_bar();
             return;
@@ -724,7 +916,7 @@ __device__ void sym_leader(const SymSlot &d, SymSmem &S, int mode)
         if (ph == SPH_KICK_DEL) {
             // kick: take an orbit off ... (symsearch.c:459-475)
             if (tid == 0) {
-                const int i = (int)(sym_draw(S) % (uint64_t)d.norb);
+                const int i = (int)(sym_mod(S, sym_draw(S), (uint64_t)d.norb));
                 sym_emit(S, SOP_ORBIT, i, 0, 0, -1);
                 S.phase = SPH_KICK_ADD;
             }
@@ -744,12 +936,12 @@ __device__ void sym_leader(const SymSlot &d, SymSmem &S, int mode)
                     for (int t2 = 0; t2 < d.R; t2++) {
                         // the value is drawn before the position, as gcc
                         // sequences symsearch.c:467
-                        const int val = (int)(sym_draw(S) % (uint64_t)d.q);
-                        const int pos = (int)(sym_draw(S) % (uint64_t)d.NR);
+                        const int val = (int)(sym_mod(S, sym_draw(S), (uint64_t)d.q));
+                        const int pos = (int)(sym_mod(S, sym_draw(S), (uint64_t)d.NR));
                         pk = cov_setnib(pk, pos, val);
                     }
                 } else {
-                    for (int j = 0; j < d.NR; j++) pk = cov_setnib(pk, j, (int)(sym_draw(S) % (uint64_t)d.q));
+                    for (int j = 0; j < d.NR; j++) pk = cov_setnib(pk, j, (int)(sym_mod(S, sym_draw(S), (uint64_t)d.q)));
                 }
                 cov_stcg(&d.rep[i], pk);
                 sym_emit(S, SOP_ORBIT, i, 0, 0, +1);
@@ -794,12 +986,15 @@ sym_kernel(const SymSlot *slots, const int *list, int mode, unsigned long long b
     sym_bar();
     const SymSlot &d = S.slot;
     SymSmem *LS = cl.map_shared_rank(&S, 0);
+    if (rank == 0)
+        for (int m = threadIdx.x + 1; m <= SYM_INV; m += SNT) S.inv[m] = ~0ull / (uint64_t)m;
     if (rank == 0 && threadIdx.x == 0) {
         const SymState &st = *d.st;
         for (int k = 0; k < 4; k++) S.rng.s[k] = st.rng[k];
         S.it = st.it; S.unc = st.unc; S.best_unc = st.best_unc; S.since_improve = st.since_improve;
         S.nkicks = st.nkicks; S.trace_n = st.trace_n; S.moves_left = st.moves_left; S.it_limit = st.it_limit;
         S.init_i = st.init_i; S.status = st.status; S.finished = st.finished;
+        for (int k = 0; k < 9; k++) S.prof[k] = st.prof[k];
         S.phase = S.init_i < d.norb ? SPH_INIT : SPH_MOVE;
         S.op = -1;
         S.guard = 0;
@@ -825,9 +1020,9 @@ sym_kernel(const SymSlot *slots, const int *list, int mode, unsigned long long b
         const int op = LS->op, oi = LS->oi, opos = LS->opos, oval = LS->oval, osign = LS->osign;
         const int take = LS->take;
         if (op == SOP_STOP) break;
-        if (op == SOP_ORBIT) sym_op_orbit(d, S, LS, rank, csize, oi, osign);
+        if (op == SOP_ORBIT) sym_op_orbit(d, S, LS, cl, rank, csize, oi, osign);
         else if (op == SOP_EVAL) sym_op_eval(d, S, LS, rank, csize, take);
-        else if (op == SOP_COMMIT) sym_op_commit(d, S, LS, rank, csize, oi, opos, oval);
+        else if (op == SOP_COMMIT) sym_op_commit(d, S, LS, cl, rank, csize, oi, opos, oval);
         cl.sync();
     }
     if (rank == 0 && threadIdx.x == 0) {
@@ -836,6 +1031,7 @@ sym_kernel(const SymSlot *slots, const int *list, int mode, unsigned long long b
         st.it = S.it; st.unc = S.unc; st.best_unc = S.best_unc; st.since_improve = S.since_improve;
         st.nkicks = S.nkicks; st.trace_n = S.trace_n; st.moves_left = S.moves_left;
         st.init_i = S.init_i;
+        for (int k = 0; k < 9; k++) st.prof[k] = S.prof[k];
         if (S.status) atomicCAS(&st.status, 0, S.status);
         st.finished = S.finished || S.unc <= 0;
     }
@@ -1039,6 +1235,7 @@ size_t cov_sym_slot_bytes(const cov_sym_params *prm)
     size_t b = 0;
     auto add = [&](size_t x) { b += (x + 255) / 256 * 256; };
     add((size_t)((N + 1) / 2) * 4);
+    add((size_t)((N + 63) / 64 + 2) * 16);
     add((size_t)norb * 8 * 2);
     add(((size_t)norb * q * NR + 8) * 4 * 2);
     add(sizeof(SymState));
@@ -1104,6 +1301,15 @@ int cov_sym_add(cov_sym *p, const cov_sym_params *prm, int32_t *slot)
         d.bitems[1] = R >= 1 ? 1 + d.bcum[R] : 0;
         d.opi = d.bitems[0] + (R >= 1 ? (uint32_t)(q - 1) * d.bitems[1] : 0u);
     }
+    // reciprocals for multiply-high division (exact: x < 2^24 for q-1,
+    // x < 2^32 for the 64-bit ones)
+    auto inv64 = [](uint64_t m) -> uint64_t { return m <= 1 ? 0 : ~0ull / m + 1; };
+    d.inv_qm1 = q > 2 ? (uint32_t)(0xffffffffull / (uint64_t)(q - 1) + 1) : 0u;
+    for (int k = 0; k <= SYM_MAXR; k++) d.inv_pp[k] = inv64(d.ppow[k]);
+    d.inv_wit1 = inv64(d.witems[1]);
+    d.inv_bit1 = inv64(d.bitems[1]);
+    d.inv_ipc = inv64(d.ipc);
+    d.inv_N = ~0ull / (uint64_t)d.N;
     const size_t ncap = (size_t)norb * q * NR + 8;
     const size_t need = cov_sym_slot_bytes(prm) + w0.size() + w1.size() + bs.size() + 1024;
     void *arena = nullptr;
@@ -1111,6 +1317,7 @@ int cov_sym_add(cov_sym *p, const cov_sym_params *prm, int32_t *slot)
     size_t off = 0;
     auto take_ = [&](size_t x) { void *q2 = (char *)arena + off; off += (x + 255) / 256 * 256; return q2; };
     d.cnt2 = (uint32_t *)take_((size_t)((d.N + 1) / 2) * 4);
+    d.st2 = (uint32_t *)take_((size_t)((d.N + 63) / 64 + 2) * 16);
     d.rep = (uint64_t *)take_((size_t)norb * 8);
     d.best = (uint64_t *)take_((size_t)norb * 8);
     d.cands = (uint32_t *)take_(ncap * 4);
@@ -1130,6 +1337,7 @@ int cov_sym_add(cov_sym *p, const cov_sym_params *prm, int32_t *slot)
     st.best_unc = d.N;
     st.it_limit = -1;
     cudaError_t e = cudaMemsetAsync(d.cnt2, 0, (size_t)((d.N + 1) / 2) * 4, p->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.st2, 0, (size_t)((d.N + 63) / 64 + 2) * 16, p->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dw0, w0.data(), w0.size(), cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dw1, w1.data(), w1.size(), cudaMemcpyHostToDevice, p->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dbs, bs.data(), bs.size(), cudaMemcpyHostToDevice, p->stream);
@@ -1255,6 +1463,16 @@ int cov_sym_get_trace(cov_sym *p, int32_t slot, cov_move_rec *out, int64_t cap, 
         SCK(cudaStreamSynchronize(p->stream));
     }
     *n_out = n > 0 ? n : 0;
+    return COV_OK;
+}
+
+int cov_sym_get_prof(cov_sym *p, int32_t slot, uint64_t *out)
+{
+    if (!p || !out || slot < 0 || slot >= p->max_slots || !p->slots[slot].used) return COV_EINVAL;
+    SymState st;
+    SCK(cudaMemcpyAsync(&st, p->slots[slot].d.st, sizeof st, cudaMemcpyDeviceToHost, p->stream));
+    SCK(cudaStreamSynchronize(p->stream));
+    for (int k = 0; k < 9; k++) out[k] = st.prof[k];
     return COV_OK;
 }
 

@@ -126,6 +126,7 @@ SIGNATURES = {
     "cov_sym_get_cnt": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint16)]),
     "cov_sym_get_trace": (ctypes.c_int, [_P, _I32, ctypes.POINTER(CovMoveRec), _I64, _PI64]),
     "cov_sym_get_rng": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64)]),
+    "cov_sym_get_prof": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64)]),
     "cov_lns_create": (ctypes.c_int, [_I32, _I32, _I32, ctypes.POINTER(_P)]),
     "cov_lns_destroy": (ctypes.c_int, [_P]),
     "cov_lns_recount": (ctypes.c_int, [_P, _PU32, _I32]),

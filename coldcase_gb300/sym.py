@@ -107,6 +107,15 @@ class SymPool:
                 "cov_sym_get_rng")
         return out
 
+    def prof(self, slot):
+        """Leader cycles per move by phase (diagnostics)."""
+        out = np.zeros(9, dtype=np.uint64)
+        L.check(self.lib.cov_sym_get_prof(self.h, int(slot), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))),
+                "cov_sym_get_prof")
+        moves = max(1, int(out[8]))
+        names = ("pick", "candidates", "sample", "estimate", "select", "commit", "orbit", "other")
+        return {k: float(out[i]) / moves for i, k in enumerate(names)}, int(out[8])
+
     def trace(self, slot):
         n = ctypes.c_int64(0)
         L.check(self.lib.cov_sym_get_trace(self.h, int(slot), None, 0, ctypes.byref(n)), "cov_sym_get_trace")

@@ -243,6 +243,9 @@ int cov_sym_get_cnt(cov_sym *pool, int32_t slot, uint16_t *out);  /* q^(n-1)    
 int cov_sym_get_trace(cov_sym *pool, int32_t slot, cov_move_rec *out, int64_t cap,
                       int64_t *n_out);
 int cov_sym_get_rng(cov_sym *pool, int32_t slot, uint64_t *out);  /* 4 words        */
+/* Diagnostics: leader cycles by phase (0 pick, 1 candidates, 2 sample,
+ * 3 estimate op, 4 selection, 5 commit op, 6 orbit ops) and 8 = moves. */
+int cov_sym_get_prof(cov_sym *pool, int32_t slot, uint64_t *out);   /* 9 words        */
 
 /* ------------------------------------------------------------------------
  * Transform-engine primitives for one cell (q, n, R): the GPU side of the
