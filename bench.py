@@ -191,6 +191,20 @@ def design_bytes_per_move(q, n, R, M, ul_n):
 
 
 # ------------------------------------------------------------------ GPU ----
+def sym_cpu_measure(moves):
+    """The quotient-search oracle (a scalar port of symsearch.c) on one host
+    core: K_8(9,4)@940 from its greedy start, `moves` moves timed."""
+    from oracle.pyoracle import SymOracle
+    o = SymOracle(8, 9, 4, 940, seed=1000)
+    o.init()
+    o.run(1)
+    t0 = time.perf_counter()
+    o.run(moves)
+    dt = time.perf_counter() - t0
+    return dict(value=moves / dt, unit="moves/s", cores=1, kind="port",
+                sample="K_8(9,4)@940 seed 1000: %d moves after init and one untimed move" % moves)
+
+
 def gpu_bench(args, rank, world, dist):
     import numpy as np
     import torch
@@ -427,9 +441,45 @@ def gpu_bench(args, rank, world, dist):
         served = dict(rep, lam_per_s=args.lam * world, unit="moves/s", value=rep["moves_per_s"], clusters=splan,
                       elastic=True)
 
+    # ---------------- quotient search (symsearch) on the big cell K_8(9,4)@940
+    quotient = None
+    if not args.no_sym:
+        from coldcase_gb300.sym import SymPool
+        qq, qn, qR, qM = 8, 9, 4, 940
+        one = None
+        if rank == 0:
+            with SymPool(1, cluster=16, budget_s=120.0) as sp:
+                s = sp.add(qq, qn, qR, qM, seed=1000)
+                sp.run(10)
+                t0 = time.perf_counter()
+                sp.run(args.sym_moves)
+                dt = time.perf_counter() - t0
+                st = sp.status(s)
+                if st["status"] != 0:
+                    raise RuntimeError("quotient search: engine status %d" % st["status"])
+                phases, _ = sp.prof(s)
+                one = dict(value=args.sym_moves / dt, unit="moves/s", cluster=16, moves=args.sym_moves,
+                           best_red_uncovered=int(st["best"]),
+                           us_per_move={k: round(v / 2070.0, 1) for k, v in phases.items() if v})
+        seeds = replicas.shard(list(range(1000, 1000 + args.sym_batch * world)), rank, world)
+        with SymPool(len(seeds), cluster=args.sym_cluster, budget_s=120.0) as sp:
+            slots = [sp.add(qq, qn, qR, qM, seed=sd) for sd in seeds]
+            sp.run(10)
+            if dist:
+                dist.barrier()
+            t0 = time.perf_counter()
+            sp.run(args.sym_batch_moves)
+            dt = time.perf_counter() - t0
+            bmoves = sum(sp.status(x)["it"] - 10 for x in slots)
+        dt_max, bmoves_all = replicas.combine(dist, dt, bmoves, device=dev)
+        quotient = dict(workload="quotient search K_8(9,4)@940 (117 orbits, 8^8 quotient counters), seeds from 1000",
+                        unit="moves/s", single=one,
+                        batch=dict(value=bmoves_all / dt_max, instances=len(seeds) * world,
+                                   cluster=args.sym_cluster, moves=args.sym_batch_moves))
+
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
                 plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work, hetero=hetero,
-                served=served, plain_cfgs=plain_cfgs)
+                served=served, plain_cfgs=plain_cfgs, quotient=quotient)
 
 
 def main():
@@ -461,6 +511,11 @@ def main():
     ap.add_argument("--requests", type=int, default=100, help="served requests per GPU")
     ap.add_argument("--lam", type=float, default=100.0, help="request arrival rate per GPU (1/s)")
     ap.add_argument("--serve-chunk", type=int, default=256)
+    ap.add_argument("--no-sym", action="store_true", help="skip the quotient-search leg")
+    ap.add_argument("--sym-moves", type=int, default=300)
+    ap.add_argument("--sym-batch", type=int, default=38, help="quotient-search instances per GPU")
+    ap.add_argument("--sym-cluster", type=int, default=4)
+    ap.add_argument("--sym-batch-moves", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -485,8 +540,11 @@ def main():
         return 0
 
     cpu = None
+    sym_cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_measure(1, args.cpu_steps, args.cpu_moves)   # before any GPU call
+        if not args.no_sym:
+            sym_cpu = sym_cpu_measure(4)
 
     import torch
     torch.cuda.set_device(local)
@@ -533,8 +591,11 @@ def main():
             served_over_plain=(r["served"]["value"] / r["plain"]["value"])
             if r["served"] and r["plain"] else None,
             coverage=r["cov"],
+            quotient=r["quotient"],
             finished_restarts=r["finished"],
         )
+        if r["quotient"] and sym_cpu:
+            line["quotient"]["cpu_baseline"] = sym_cpu
         if cpu:
             line["cpu_baseline"] = dict(value=cpu["value"], unit="moves/s", cores=cpu["cores"], kind="port",
                                         sample=cpu["sample"])
