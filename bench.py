@@ -325,9 +325,14 @@ def gpu_bench(args, rank, world, dist):
     if not args.no_plain and rank == 0:
         from coldcase_gb300 import workloads
         plain_cfgs = {}
+        loose = dict(name="plain q3 n11 R4 M81 tenure0", q=3, n=11, R=4, M=81, tabu=0)
+        loose_wide = dict(loose, name="plain q3 n11 R4 M81 tenure0 --wide", wide=True)
         for key, w, cl, mv in (("q6n9_M700", workloads.PLAIN_GPU, 16, 2000),
-                               ("q4n6_M420", workloads.PLAIN_CPU, 1, 2000)):
-            eng = Search(w["q"], w["n"], w["R"], w["M"], seed=1, tabu=w["tabu"], cluster=cl, budget_s=120.0)
+                               ("q4n6_M420", workloads.PLAIN_CPU, 1, 2000),
+                               ("q3n11_M81", loose, 4, 2000),
+                               ("q3n11_M81_wide", loose_wide, 4, 2000)):
+            eng = Search(w["q"], w["n"], w["R"], w["M"], seed=1, tabu=w["tabu"], cluster=cl, budget_s=120.0,
+                         wide=w.get("wide", False))
             eng.load(uniform_code(w["q"], w["n"], w["M"], 1))
             ps = torch.cuda.Stream(device=dev)
             eng.pool.set_stream(ps.cuda_stream)

@@ -95,3 +95,30 @@ def test_sym_big_quotient_parity(covlib):
         k, g1, o1 = first_diff(gtr, otr)
         assert len(gtr) == len(otr) and k == len(otr), (k, g1, o1)
         assert (pool.cnt(s) == o.cnt()).all()
+
+
+def test_sym_timeout_resume_keeps_trajectory(covlib, sym_golden):
+    """A launch deadline stops an instance between two moves (or between two
+    orbit placements of its initialisation) with COV_ETIMEOUT; after
+    resume the run continues on exactly the uninterrupted trajectory."""
+    r = [x for x in sym_golden if (x["q"], x["n"], x["R"], x["M"]) == (6, 8, 4, 168)][0]
+    moves = 120
+    o, otr = sym_oracle_run(r, moves=moves)
+    pool = SymPool(1, cluster=1, budget_s=0.002)
+    s = gpu_sym(pool, r, moves)
+    stops = 0
+    for _ in range(100000):
+        st = pool.status(s)
+        if st["status"] == -4:
+            stops += 1
+            pool.resume(s)
+            continue
+        assert st["status"] == 0, st
+        if st["it"] >= moves or st["finished"]:
+            break
+        pool.run(moves - st["it"])
+    assert stops > 0
+    gtr = pool.trace(s)
+    assert gtr.tobytes() == otr.tobytes()
+    assert (pool.cnt(s) == o.cnt()).all()
+    pool.close()
