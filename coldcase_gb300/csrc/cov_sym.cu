@@ -350,6 +350,16 @@ __device__ __forceinline__ long long sym_walk_item(const SymSlot &d, const uint6
                 const uint4 lo = __ldcg(reinterpret_cast<const uint4 *>(d.st2 + (w0 >> 4)));
                 uint4 hi = make_uint4(0, 0, 0, 0);
                 if (x0 + (uint32_t)(qm1 * pl) >= w0 + 64) hi = __ldcg(reinterpret_cast<const uint4 *>(d.st2 + (w0 >> 4) + 4));
+                if (pl == 1) {
+                    // q consecutive 2-bit fields: compare all at once
+                    const int off = (int)(x0 - w0), wi = off >> 4;
+                    const uint32_t ch = __funnelshift_r(sym_pick8(lo, hi, wi), sym_pick8(lo, hi, wi + 1),
+                                                        2 * (off & 15));
+                    const uint32_t fm = (d.q == 16 ? 0xffffffffu : ((1u << (2 * d.q)) - 1u)) & 0x55555555u &
+                                        ~(1u << (2 * cl));
+                    const uint32_t b0 = ch & fm, b1 = (ch >> 1) & fm;
+                    return __popc(want ? (b0 & ~b1) : (fm & ~b0 & ~b1));
+                }
                 int n = 0;
                 for (int v = 0; v <= qm1; v++) {
                     if (v == cl) continue;
