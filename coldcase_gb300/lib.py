@@ -110,6 +110,8 @@ SIGNATURES = {
     "cov_count_above_dev": (ctypes.c_int64, [_I32, _I32, _P, _I32, _P]),
     "cov_mindist_dev_static": (ctypes.c_int, [_I32, _I32, _P, _I32, _P, _P]),
     "cov_finish": (ctypes.c_int, [_I32, _I32, _I32, _I32, _PU8, _I32, _I32, _PU8, _PI32, _PI64]),
+    "cov_chain_run": (ctypes.c_int, [ctypes.c_int] * 5 + [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_int,
+                                                          _PU8, _PU8, _PI32, _PI32, _PI64]),
     "cov_sym_create": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_P)]),
     "cov_sym_destroy": (ctypes.c_int, [_P]),
     "cov_sym_set_budget": (ctypes.c_int, [_P, ctypes.c_double]),

@@ -115,6 +115,17 @@ int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value);
  * takes one iteration budget for all chains; covengine gives each chain its
  * own time budget (cov/engine/covengine:624-643). */
 int cov_pool_set_slot_param(cov_pool *pool, int32_t slot, const char *name, int64_t value);
+/* The reference's batched GPU entry with its exact arguments and buffers:
+ * chain_run (cov/gemm2/chainsolve.cu:370-375, bound by
+ * cov/gemm2/chain.py:30-57).  code_h and best_h hold nchains x M rows of 16
+ * digits (digits past n are 0 in best_h); best_u_h, solved_h and iters_h
+ * one entry per chain.  Each chain runs the p5b trajectory from its own
+ * start code with seed seed*1000003 + chain*7919 for at most `iters` moves;
+ * `threads` is accepted and unused.  Returns 0 or a COV_E* code. */
+int cov_chain_run(int q, int n, int R, int M, int nchains, long long iters,
+                  unsigned long long seed, int threads, const uint8_t *code_h,
+                  uint8_t *best_h, int32_t *best_u_h, int32_t *solved_h,
+                  long long *iters_h);
 /* Free and total bytes of the current device (cudaMemGetInfo), for
  * admitting instances by free HBM.  No counterpart in the reference, whose
  * solvers run as CPU processes. */

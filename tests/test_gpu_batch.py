@@ -142,3 +142,36 @@ def test_batch_segmented_elastic_bit_exact(covlib):
             o, tr = oracle_of(s["q"], s["n"], s["R"], s["M"], s["moves"], s["tabu"], s["seed"])
             assert res[i]["iters"] == o.iters() and res[i]["uncovered"] == o.best_uncovered(), (s, res[i])
             assert (b.best(i) == o.best()).all(), s
+
+
+def test_chain_run_equals_pool_chains(covlib):
+    """cov_chain_run (chain_run's arguments and buffers, rows of 16 digits)
+    gives each chain exactly the trajectory of a pool slot with seed
+    seed*1000003 + chain*7919."""
+    import ctypes
+    from coldcase_gb300 import lib as L
+    q, n, R, M, nchains, iters, seed = 4, 7, 2, 40, 5, 400, 3
+    rng = np.random.default_rng(11)
+    codes = np.zeros((nchains, M, 16), dtype=np.uint8)
+    codes[:, :, :n] = rng.integers(0, q, (nchains, M, n), dtype=np.uint8)
+    best = np.zeros_like(codes)
+    bu = np.zeros(nchains, np.int32)
+    sv = np.zeros(nchains, np.int32)
+    it = np.zeros(nchains, np.int64)
+    p8 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    rc = covlib.cov_chain_run(q, n, R, M, nchains, iters, seed, 256, p8(codes), p8(best),
+                              bu.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                              sv.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                              it.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    assert rc == 0
+    assert (best[:, :, n:] == 0).all()
+    for c in range(nchains):
+        pool = Pool(1, cluster=1)
+        s = pool.add(q, n, R, M, code=codes[c, :, :n], seed=seed * 1000003 + c * 7919)
+        pool.set_slot_param(s, "it_limit", iters)
+        pool.run(iters)
+        st = pool.status(s)
+        assert (st["best"], st["it"]) == (bu[c], it[c])
+        assert sv[c] == (st["best"] == 0)
+        assert (pool.best(s) == best[c, :, :n]).all()
+        pool.close()
