@@ -122,3 +122,24 @@ def test_sym_timeout_resume_keeps_trajectory(covlib, sym_golden):
     assert gtr.tobytes() == otr.tobytes()
     assert (pool.cnt(s) == o.cnt()).all()
     pool.close()
+
+
+@pytest.mark.parametrize("cell,cand,kick,stall", [((6, 8, 4, 168), 7, 0, 15), ((5, 6, 2, 100), 3, 1, 25),
+                                                  ((3, 9, 2, 150), 50, 4, 40)])
+def test_sym_sample_cap_and_kicks(covlib, cell, cand, kick, stall):
+    """A candidate cap below the candidate count (sampled subsets), no-op
+    kicks and kicks of several orbits, against the oracle move by move."""
+    from oracle.pyoracle import SymOracle
+    q, n, R, M = cell
+    moves = 400
+    o = SymOracle(q, n, R, M, seed=5, kick=kick, stall=stall, cand=cand)
+    o.init()
+    otr = o.run(moves, trace=True)
+    with SymPool(1, cluster=2) as pool:
+        s = pool.add(q, n, R, M, seed=5, kick=kick, stall=stall, cand=cand, trace=1, trace_cap=moves)
+        pool.run(moves)
+        gtr = pool.trace(s)
+        k, g1, o1 = first_diff(gtr, otr)
+        assert len(gtr) == len(otr) and k == len(otr), (k, g1, o1)
+        assert (pool.cnt(s) == o.cnt()).all() and (pool.best(s) == o.best()).all()
+        assert (pool.rng(s) == o.rng()).all()
