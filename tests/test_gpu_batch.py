@@ -31,9 +31,9 @@ CELLS = [  # q, n, R, M, moves, tabu
 ]
 
 
-def oracle_of(q, n, R, M, moves, tabu, seed):
+def oracle_of(q, n, R, M, moves, tabu, seed, wide=False):
     from oracle.pyoracle import Oracle
-    o = Oracle(q, n, R, M, seed=seed, tabu=tabu)
+    o = Oracle(q, n, R, M, seed=seed, tabu=tabu, wide=wide)
     o.init(uniform_code(q, n, M, seed))
     tr = o.run(moves, trace=True)
     return o, tr
@@ -110,6 +110,21 @@ def test_served_result_same_alone_and_in_mix(covlib):
         assert (a["best"] == best).all()
         o, _ = oracle_of(r["q"], r["n"], r["R"], r["M"], r["moves"], r["tabu"], r["seed"])
         assert res["uncovered"] == o.best_uncovered() and res["iters"] == o.iters()
+
+
+def test_wide_requests_in_a_mix(covlib):
+    """--wide and plain requests served together: each answer is the
+    oracle's for its own flag."""
+    reqs = [dict(r, wide=bool(i % 2), seed=900 + i) for i, r in enumerate(_requests())]
+    with Server(max_slots=5, chunk=131) as srv:
+        rep = srv.serve(reqs)
+        assert rep["requests"] == len(reqs)
+        done = {r["id"]: r for r in srv.done}
+    for r in reqs:
+        o, _ = oracle_of(r["q"], r["n"], r["R"], r["M"], r["moves"], r["tabu"], r["seed"], wide=r["wide"])
+        res = done[r["id"]]["result"]
+        assert res["uncovered"] == o.best_uncovered() and res["iters"] == o.iters(), (r, res)
+        assert (done[r["id"]]["best"] == o.best()).all(), r
 
 
 def test_admission_by_device_bytes(covlib):
