@@ -240,7 +240,13 @@ def sym_runs(binary):
              (8, 6, 2, 400, 0, 0.2), (6, 8, 4, 168, 0, 0.3), (3, 9, 2, 150, 0, 0.1), (4, 7, 1, 400, 0, 0.1),
              (3, 6, 0, 300, 0, 0.05), (6, 8, 4, 240, 20, 0.3), (4, 6, 1, 500, 0, 0.1), (7, 5, 2, 140, 0, 0.1),
              (4, 5, 1, 64, 0, 0.1), (3, 5, 1, 27, 0, 0.1)]
-    for (q, n, R, M, orbits, t) in cells:
+    # edge cells: q = 2 and 16, a one-digit quotient (n = 2), R = 0,
+    # R >= n - 1, and cells covered by the initial orbits
+    edge = [(2, 4, 1, 4, 0, 0.01), (2, 5, 1, 6, 0, 0.01), (3, 2, 0, 3, 0, 0.01), (3, 2, 1, 3, 0, 0.01),
+            (3, 3, 1, 3, 0, 0.01), (3, 3, 2, 6, 0, 0.01), (5, 3, 1, 5, 0, 0.01), (16, 3, 1, 48, 0, 0.02),
+            (16, 4, 1, 160, 0, 0.02), (9, 4, 2, 27, 0, 0.02), (4, 4, 3, 4, 0, 0.01), (2, 8, 3, 8, 0, 0.01),
+            (3, 4, 0, 30, 0, 0.01)]
+    for (q, n, R, M, orbits, t) in cells + edge:
         for s, stall, kick in ((1, 3000, 2), (2, 30, 2), (3, 20, 3)):
             args = ["-q", q, "-n", n, "-R", R, "-M", M, "-t", t, "-s", s, "--stall", stall, "--kick", kick,
                     "--threads", 1]
