@@ -453,19 +453,23 @@ def gpu_bench(args, rank, world, dist):
         qq, qn, qR, qM = 8, 9, 4, 940
         one = None
         if rank == 0:
-            with SymPool(1, cluster=16, budget_s=120.0) as sp:
-                s = sp.add(qq, qn, qR, qM, seed=1000)
-                sp.run(10)
-                t0 = time.perf_counter()
-                sp.run(args.sym_moves)
-                dt = time.perf_counter() - t0
-                st = sp.status(s)
-                if st["status"] != 0:
-                    raise RuntimeError("quotient search: engine status %d" % st["status"])
-                phases, _ = sp.prof(s)
-                one = dict(value=args.sym_moves / dt, unit="moves/s", cluster=16, moves=args.sym_moves,
-                           best_red_uncovered=int(st["best"]),
-                           us_per_move={k: round(v / 2070.0, 1) for k, v in phases.items() if v})
+            one = {}
+            for form, ge in (("cluster", False), ("grid", True)):
+                with SymPool(1, cluster=16, budget_s=120.0, grid_eval=ge) as sp:
+                    s = sp.add(qq, qn, qR, qM, seed=1000)
+                    sp.run(10)
+                    t0 = time.perf_counter()
+                    sp.run(args.sym_moves)
+                    dt = time.perf_counter() - t0
+                    st = sp.status(s)
+                    if st["status"] != 0:
+                        raise RuntimeError("quotient search: engine status %d" % st["status"])
+                    phases, _ = sp.prof(s)
+                    one[form] = dict(value=args.sym_moves / dt, unit="moves/s", cluster=16, moves=args.sym_moves,
+                                     best_red_uncovered=int(st["best"]))
+                    if not ge:
+                        one[form]["us_per_move"] = {k: round(v / 2070.0, 1) for k, v in phases.items() if v}
+            one["grid"]["note"] = "estimates by a grid-wide launch per move, the rest on the cluster"
         seeds = replicas.shard(list(range(1000, 1000 + args.sym_batch * world)), rank, world)
         with SymPool(len(seeds), cluster=args.sym_cluster, budget_s=120.0) as sp:
             slots = [sp.add(qq, qn, qR, qM, seed=sd) for sd in seeds]

@@ -44,7 +44,7 @@ namespace cg = cooperative_groups;
 
 enum { SOP_STOP = 0, SOP_ORBIT = 1, SOP_EVAL = 2, SOP_COMMIT = 3 };
 enum { SPH_INIT = 0, SPH_MOVE = 1, SPH_SELECT = 2, SPH_AFTER_COMMIT = 3, SPH_KICK_DEL = 4,
-       SPH_KICK_ADD = 5, SPH_KICK_NEXT = 6, SPH_DONE = 7 };
+       SPH_KICK_ADD = 5, SPH_KICK_NEXT = 6, SPH_DONE = 7, SPH_EVAL = 8 };
 enum { SMODE_INIT = 0, SMODE_RUN = 1 };
 
 struct SymState {
@@ -56,6 +56,11 @@ struct SymState {
     // candidates, 2 sample, 3 estimate op, 4 selection, 5 commit op, 6 orbit
     // ops, 7 the rest; 8 moves counted
     unsigned long long prof[9];
+    // a move planned up to its estimates, which a grid-wide launch computes
+    // (the sample is in cands[0..take)); the next leader launch goes on
+    // from the selection
+    int eval_pending, take;
+    cov_move_rec rec;
 };
 
 struct SymSlot {
@@ -108,6 +113,7 @@ struct SymSmem {
     CovRng rng;
     long long it, unc, best_unc, since_improve, nkicks, trace_n, moves_left, it_limit;
     int init_i, status, finished, phase, kick_t, cand_sm;
+    int split, eval_pending;     // estimates by a grid-wide launch; one is due
     unsigned long long deadline;
     long long guard, est;
     unsigned long long prof[9];
@@ -461,13 +467,12 @@ __device__ void sym_op_orbit(const SymSlot &d, SymSmem &S, SymSmem *LS, cg::clus
 // sampled candidates (take x q entries) and the cluster's threads run over
 // all (candidate, item) pairs at once.  Nested, for samples too large for
 // that table: candidate by candidate, the threads splitting its items.
-__device__ void sym_op_eval(const SymSlot &d, SymSmem &S, SymSmem *LS, int rank, int csize, int take)
+// (S.cand holds the sample when take <= SYM_TS; `rank` of `csize` CTAs;
+// GRID: the whole grid runs it, else one cluster)
+template <bool GRID>
+__device__ void sym_eval_items(const SymSlot &d, SymSmem &S, int rank, int csize, int take)
 {
     const bool sm = take <= SYM_TS;
-    if (sm && rank != 0) {
-        for (int s = threadIdx.x; s < take; s += SNT) S.cand[s] = LS->cand[s];
-        sym_bar();
-    }
     const uint32_t stride = (uint32_t)csize * SNT;
     const int q = d.q;
     if (sm && take * q <= SYM_CT && (unsigned long long)take * d.ipc < (1ull << 32)) {
@@ -493,21 +498,60 @@ __device__ void sym_op_eval(const SymSlot &d, SymSmem &S, SymSmem *LS, int rank,
         }
         sym_bar();
         const uint32_t total = (uint32_t)take * d.ipc;
+        if (!GRID) {
+            // one cluster: items strided over its threads
+            int cur = -1, p = 0;
+            long long acc = 0;
+            for (uint32_t t = (uint32_t)rank * SNT + threadIdx.x; t < total; t += stride) {
+                const int s2 = (int)sym_div64(t, d.ipc, d.inv_ipc);
+                const uint32_t r = t - (uint32_t)s2 * d.ipc;
+                if (s2 != cur) {
+                    if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
+                    cur = s2;
+                    acc = 0;
+                    p = (int)((S.cand[s2] >> 4) & 15u);
+                }
+                const int o = s2 * q;
+                acc += sym_walk_item<0>(d, S.tcpk + o, S.tbase + o, S.tdv + o, p, r);
+            }
+            if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
+            return;
+        }
+        // the whole grid: each warp takes a contiguous run of items, 32 at a
+        // time, so that a lane's sum stays on one candidate for long
+        // stretches (strided items would send an atomic per item to a few
+        // dozen estimates); sums reach the estimates when the candidate
+        // changes and, warp-reduced, at the end of the run
+        const int lane = threadIdx.x & 31;
+        const uint32_t nwarps = (uint32_t)csize * SNW;
+        const uint32_t gw = (uint32_t)rank * SNW + (threadIdx.x >> 5);
+        const uint32_t seg = ((total + nwarps - 1) / nwarps + 31u) & ~31u;
+        const uint32_t lo = (uint32_t)min((unsigned long long)total, (unsigned long long)gw * seg);
+        const uint32_t hi = (uint32_t)min((unsigned long long)total, (unsigned long long)lo + seg);
         int cur = -1, p = 0;
         long long acc = 0;
-        for (uint32_t t = (uint32_t)rank * SNT + threadIdx.x; t < total; t += stride) {
-            const int s2 = (int)sym_div64(t, d.ipc, d.inv_ipc);
-            const uint32_t r = t - (uint32_t)s2 * d.ipc;
-            if (s2 != cur) {
-                if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
-                cur = s2;
-                acc = 0;
-                p = (int)((S.cand[s2] >> 4) & 15u);
+        for (uint32_t t0 = lo; t0 < hi; t0 += 32) {
+            const uint32_t t = t0 + (uint32_t)lane;
+            if (t < hi) {
+                const int s2 = (int)sym_div64(t, d.ipc, d.inv_ipc);
+                const uint32_t r = t - (uint32_t)s2 * d.ipc;
+                if (s2 != cur) {
+                    if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
+                    cur = s2;
+                    acc = 0;
+                    p = (int)((S.cand[s2] >> 4) & 15u);
+                }
+                const int o = s2 * q;
+                acc += sym_walk_item<0>(d, S.tcpk + o, S.tbase + o, S.tdv + o, p, r);
             }
-            const int o = s2 * q;
-            acc += sym_walk_item<0>(d, S.tcpk + o, S.tbase + o, S.tdv + o, p, r);
         }
-        if (cur >= 0 && acc) atomicAdd(&d.cd[cur], (int)acc);
+        const int c0 = __shfl_sync(0xffffffffu, cur, 0);
+        if (__all_sync(0xffffffffu, cur == c0)) {
+            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0 && c0 >= 0 && acc) atomicAdd(&d.cd[c0], (int)acc);
+        } else if (cur >= 0 && acc) {
+            atomicAdd(&d.cd[cur], (int)acc);
+        }
         return;
     }
     for (int s = 0; s < take; s++) {
@@ -538,6 +582,15 @@ __device__ void sym_op_commit(const SymSlot &d, SymSmem &S, SymSmem *LS, cg::clu
     cl.sync();
     for (uint32_t r = (uint32_t)rank * SNT + threadIdx.x; r < d.ipc; r += stride)
         sym_walk_item<2>(d, S.ct.cpk, S.ct.base, S.ct.dv, p, r);
+}
+
+__device__ void sym_op_eval(const SymSlot &d, SymSmem &S, SymSmem *LS, int rank, int csize, int take)
+{
+    if (take <= SYM_TS && rank != 0) {
+        for (int s = threadIdx.x; s < take; s += SNT) S.cand[s] = LS->cand[s];
+        sym_bar();
+    }
+    sym_eval_items<false>(d, S, rank, csize, take);
 }
 
 // ------------------------------------------------------ leader routines ----
@@ -879,7 +932,28 @@ __device__ void sym_leader(const SymSlot &d, SymSmem &S, int mode)
                 sym_bar();
                 return;
             }
+            if (S.split) {
+                // the estimates run as a grid-wide launch: hand the sample
+                // over and end this launch
+                if (S.take <= SYM_TS)
+                    for (int x = tid; x < S.take; x += SNT) cov_stcg(&d.cands[x], S.cand[x]);
+                if (tid == 0) {
+                    S.phase = SPH_SELECT;
+                    S.eval_pending = 1;
+                    sym_emit(S, SOP_STOP, 0, 0, 0, 0);
+                }
+                sym_bar();
+                return;
+            }
             if (tid == 0) S.phase = SPH_SELECT;
+            sym_bar();
+            return;
+        }
+        if (ph == SPH_EVAL) {
+            // a move left planned for a grid-wide estimate, continued here
+            for (int x = tid; x < S.take; x += SNT) cov_stcg(&d.cd[x], 0);
+            sym_bar();
+            if (tid == 0) { sym_emit(S, SOP_EVAL, 0, 0, 0, 0); S.phase = SPH_SELECT; }
             sym_bar();
             return;
         }
@@ -984,7 +1058,8 @@ __device__ void sym_leader(const SymSlot &d, SymSmem &S, int mode)
 }
 
 __global__ void __launch_bounds__(SNT, 1)
-sym_kernel(const SymSlot *slots, const int *list, int mode, unsigned long long budget_ns, long long op_guard)
+sym_kernel(const SymSlot *slots, const int *list, int mode, unsigned long long budget_ns, long long op_guard,
+           int split)
 {
     extern __shared__ __align__(16) unsigned char sym_raw[];
     SymSmem &S = *reinterpret_cast<SymSmem *>(sym_raw);
@@ -1010,7 +1085,22 @@ sym_kernel(const SymSlot *slots, const int *list, int mode, unsigned long long b
         S.guard = 0;
         S.deadline = (unsigned long long)sym_clock() + budget_ns * SYM_CYCLES_PER_NS;
         if (S.status) S.phase = SPH_MOVE;
+        S.split = split;
+        S.eval_pending = st.eval_pending;
+        if (st.eval_pending) {
+            // the estimates of this move were left to a grid-wide launch
+            // (already run when this launch is split too)
+            S.take = st.take;
+            S.rec = st.rec;
+            S.phase = split ? SPH_SELECT : SPH_EVAL;
+            S.eval_pending = 0;
+        }
     }
+    sym_bar();
+    if (rank == 0 && S.phase == SPH_SELECT && S.take <= SYM_TS)
+        for (int x = threadIdx.x; x < S.take; x += SNT) S.cand[x] = cov_ldcg(&d.cands[x]);
+    if (rank == 0 && S.phase == SPH_EVAL && S.take <= SYM_TS)
+        for (int x = threadIdx.x; x < S.take; x += SNT) S.cand[x] = cov_ldcg(&d.cands[x]);
     sym_bar();
     for (;;) {
         if (rank == 0) {
@@ -1042,9 +1132,31 @@ sym_kernel(const SymSlot *slots, const int *list, int mode, unsigned long long b
         st.nkicks = S.nkicks; st.trace_n = S.trace_n; st.moves_left = S.moves_left;
         st.init_i = S.init_i;
         for (int k = 0; k < 9; k++) st.prof[k] = S.prof[k];
+        st.eval_pending = S.eval_pending;
+        st.take = S.take;
+        st.rec = S.rec;
         if (S.status) atomicCAS(&st.status, 0, S.status);
         st.finished = S.finished || S.unc <= 0;
     }
+}
+
+// The estimates of one instance's planned move over the whole grid
+// (symsearch.c:432-433 for every sampled candidate); the cluster kernel left
+// the sample in cands[0..take) and zeroed cd[0..take).
+__global__ void __launch_bounds__(SNT, 1) sym_eval_kernel(const SymSlot *slots, int slot)
+{
+    extern __shared__ __align__(16) unsigned char sym_raw[];
+    SymSmem &S = *reinterpret_cast<SymSmem *>(sym_raw);
+    if (threadIdx.x == 0) S.slot = slots[slot];
+    sym_bar();
+    const SymSlot &d = S.slot;
+    if (!cov_ldcg(&d.st->eval_pending) || cov_ldcg(&d.st->status)) return;
+    const int take = cov_ldcg(&d.st->take);
+    if (take <= SYM_TS) {
+        for (int x = threadIdx.x; x < take; x += SNT) S.cand[x] = cov_ldcg(&d.cands[x]);
+        sym_bar();
+    }
+    sym_eval_items<true>(d, S, (int)blockIdx.x, (int)gridDim.x, take);
 }
 
 __global__ void k_sym_budget(SymState *states, const int *list, int count, long long moves)
@@ -1111,6 +1223,7 @@ int sym_attrs()
     if (g_sym_attr) return 0;
     SCK(cudaFuncSetAttribute(sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SymSmem)));
     SCK(cudaFuncSetAttribute(sym_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    SCK(cudaFuncSetAttribute(sym_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SymSmem)));
     g_sym_attr = 1;
     return 0;
 }
@@ -1119,6 +1232,8 @@ int sym_attrs()
 
 struct cov_sym {
     int max_slots = 0, cluster = 1;
+    int grid_eval = 0;           // one live instance: estimates over the whole GPU
+    int sms = 0;
     double budget_s = 30.0;
     std::vector<SymHost> slots;
     SymSlot *d_slots = nullptr;
@@ -1168,9 +1283,25 @@ static int sym_launch(cov_sym *p, const std::vector<int> &slots, int mode, long 
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        SCK(cudaLaunchKernelEx(&cfg, sym_kernel, (const SymSlot *)p->d_slots, (const int *)p->d_list, mode,
-                               budget_ns, guard));
-        SCK(cudaGetLastError());
+        if (mode == SMODE_RUN && p->grid_eval && slots.size() == 1) {
+            // one instance: each move is a cluster launch up to the
+            // estimates and a grid-wide launch for them; moves + 1 cluster
+            // launches close the last move (a finished instance's extra
+            // launches return at once)
+            for (long long m = 0; m <= moves; m++) {
+                SCK(cudaLaunchKernelEx(&cfg, sym_kernel, (const SymSlot *)p->d_slots, (const int *)p->d_list,
+                                       mode, budget_ns, guard, 1));
+                if (m < moves) {
+                    sym_eval_kernel<<<(unsigned)p->sms, SNT, sizeof(SymSmem), p->stream>>>(
+                        (const SymSlot *)p->d_slots, slots[0]);
+                }
+                SCK(cudaGetLastError());
+            }
+        } else {
+            SCK(cudaLaunchKernelEx(&cfg, sym_kernel, (const SymSlot *)p->d_slots, (const int *)p->d_list, mode,
+                                   budget_ns, guard, 0));
+            SCK(cudaGetLastError());
+        }
         SCK(cudaStreamSynchronize(p->stream));
     }
     return 0;
@@ -1192,6 +1323,7 @@ int cov_sym_create(int32_t max_slots, int32_t cluster, cov_sym **out)
     p->max_slots = max_slots;
     p->cluster = cluster;
     p->slots.resize(max_slots);
+    SCK(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev));
     cudaError_t e = cudaMalloc(&p->d_slots, sizeof(SymSlot) * max_slots);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_states, sizeof(SymState) * max_slots);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_list, sizeof(int) * max_slots);
@@ -1221,6 +1353,21 @@ int cov_sym_set_budget(cov_sym *p, double seconds)
     if (!p || !(seconds > 0)) return COV_EINVAL;
     p->budget_s = seconds;
     return COV_OK;
+}
+
+// Pool setting: "grid_eval" 1 runs a pool with one live instance with its
+// estimates spread over the whole GPU (a launch per move for them), 0 (the
+// default) keeps every move inside the instance's cluster.  Neither
+// changes a trajectory.
+int cov_sym_set_param(cov_sym *p, const char *name, int64_t value)
+{
+    if (!p || !name) return COV_EINVAL;
+    if (!strcmp(name, "grid_eval")) {
+        if (value < 0 || value > 1) return COV_EINVAL;
+        p->grid_eval = (int)value;
+        return COV_OK;
+    }
+    return COV_EINVAL;
 }
 
 int cov_sym_orbits(const cov_sym_params *prm)

@@ -115,6 +115,7 @@ SIGNATURES = {
     "cov_sym_create": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_P)]),
     "cov_sym_destroy": (ctypes.c_int, [_P]),
     "cov_sym_set_budget": (ctypes.c_int, [_P, ctypes.c_double]),
+    "cov_sym_set_param": (ctypes.c_int, [_P, ctypes.c_char_p, _I64]),
     "cov_sym_orbits": (ctypes.c_int, [ctypes.POINTER(CovSymParams)]),
     "cov_sym_slot_bytes": (ctypes.c_size_t, [ctypes.POINTER(CovSymParams)]),
     "cov_sym_add": (ctypes.c_int, [_P, ctypes.POINTER(CovSymParams), _PI32]),

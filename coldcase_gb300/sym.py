@@ -46,7 +46,9 @@ def format_code(reps, q):
 class SymPool:
     """Quotient-search instances on one GPU (cov_sym_* in include/covgpu.h)."""
 
-    def __init__(self, max_slots=1, cluster=1, budget_s=30.0):
+    def __init__(self, max_slots=1, cluster=1, budget_s=30.0, grid_eval=False):
+        """grid_eval: with one live instance, spread each move's estimates over
+        the whole GPU instead of the instance's cluster."""
         self.lib = L.load()
         h = ctypes.c_void_p()
         L.check(self.lib.cov_sym_create(int(max_slots), int(cluster), ctypes.byref(h)), "cov_sym_create")
@@ -54,6 +56,8 @@ class SymPool:
         self.meta = {}
         if budget_s:
             L.check(self.lib.cov_sym_set_budget(self.h, float(budget_s)), "cov_sym_set_budget")
+        if grid_eval:
+            L.check(self.lib.cov_sym_set_param(self.h, b"grid_eval", 1), "cov_sym_set_param")
 
     def add(self, q, n, R, M, orbits=0, seed=12345, kick=2, stall=3000, cand=100000, trace=0, trace_cap=0):
         """Create an instance; its orbits are placed greedily on the device."""

@@ -86,7 +86,8 @@ def main(argv=None):
     N = q ** (n - 1)
     cluster = a["cluster"] or (16 if N >= 1 << 22 else 8 if N >= 1 << 18 else 2)
     try:
-        pool = sym.SymPool(1, cluster=cluster, budget_s=max(1.0, min(30.0, a["t"])))
+        # one instance: its estimates spread over the whole GPU
+        pool = sym.SymPool(1, cluster=cluster, budget_s=max(1.0, min(30.0, a["t"])), grid_eval=True)
         s = pool.add(q, n, R, M, orbits=a["orbits"], seed=a["s"], kick=a["kick"], stall=a["stall"], cand=a["cand"])
     except CovError as e:
         sys.stderr.write("symsearch_gpu: %s\n" % e)

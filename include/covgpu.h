@@ -231,6 +231,10 @@ typedef struct {
 int cov_sym_create(int32_t max_slots, int32_t cluster, cov_sym **out);
 int cov_sym_destroy(cov_sym *pool);
 int cov_sym_set_budget(cov_sym *pool, double seconds);   /* per-launch wall limit */
+/* "grid_eval": 1 spreads the estimates of a pool with one live instance over
+ * the whole GPU (one launch per move for them); 0, the default, keeps every
+ * move inside the instance's cluster.  Neither changes a trajectory. */
+int cov_sym_set_param(cov_sym *pool, const char *name, int64_t value);
 /* Orbit count of these parameters, or COV_EINVAL where symsearch exits 2
  * and COV_ERANGE where it exits 3 (symsearch.c:311-333). */
 int cov_sym_orbits(const cov_sym_params *prm);

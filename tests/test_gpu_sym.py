@@ -143,3 +143,25 @@ def test_sym_sample_cap_and_kicks(covlib, cell, cand, kick, stall):
         assert len(gtr) == len(otr) and k == len(otr), (k, g1, o1)
         assert (pool.cnt(s) == o.cnt()).all() and (pool.best(s) == o.best()).all()
         assert (pool.rng(s) == o.rng()).all()
+
+
+def test_sym_grid_eval_bit_exact(covlib, sym_golden):
+    """One instance with its estimates spread over the whole GPU (a launch
+    per move) follows the same trajectory, also across runs that switch the
+    mode in the middle."""
+    for r in [x for x in sym_golden if x["seed"] == 1][::3]:
+        moves = min(r["ref"]["iters"], 1500)
+        o, otr = sym_oracle_run(r, moves=moves)
+        pool = SymPool(1, cluster=4, grid_eval=True)
+        s = gpu_sym(pool, r, moves)
+        pool.set_slot_param(s, "it_limit", moves)
+        pool.run(moves // 2)
+        pool.lib.cov_sym_set_param(pool.h, b"grid_eval", 0)
+        pool.run(7)
+        pool.lib.cov_sym_set_param(pool.h, b"grid_eval", 1)
+        pool.run(moves)
+        gtr = pool.trace(s)
+        k, g1, o1 = first_diff(gtr, otr)
+        assert len(gtr) == len(otr) and k == len(otr), (r["q"], r["n"], r["R"], r["M"], k, g1, o1)
+        assert (pool.cnt(s) == o.cnt()).all()
+        pool.close()
