@@ -1353,7 +1353,8 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
         }
         best = block_min_u32(S, best);
         if (best != 0xffffffffu) {
-            uint32_t x = start + best;
+            // (start + best) may pass 2^32 when q^n > 2^31
+            unsigned long long x = (unsigned long long)start + best;
             if (x >= d.N) x -= d.N;
             return (long long)x;
         }
@@ -1367,13 +1368,13 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
         for (int k = 0; k < 4; k++) {
             uint32_t o2 = off + (uint32_t)tid * 4 + k;
             if (o2 >= d.N) break;
-            uint32_t x = start + o2;
+            unsigned long long x = (unsigned long long)start + o2;
             if (x >= d.N) x -= d.N;
             if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) { best = o2; break; }
         }
         best = block_min_u32(S, best);
         if (best != 0xffffffffu) {
-            uint32_t x = start + best;
+            unsigned long long x = (unsigned long long)start + best;
             if (x >= d.N) x -= d.N;
             return (long long)x;
         }

@@ -654,13 +654,14 @@ __device__ long long sym_pick(const SymSlot &d, SymSmem &S)
         for (int k = 0; k < 4; k++) {
             const uint32_t o = off + (uint32_t)k * SNT + (uint32_t)tid;
             if (o >= d.N) break;
-            uint32_t w = start + o;
+            // (start + o) may pass 2^32 when the quotient has over 2^31 words
+            unsigned long long w = (unsigned long long)start + o;
             if (w >= d.N) w -= d.N;
-            if (sym_st(d, w) == 0) { best = (int)(o - off); break; }
+            if (sym_st(d, (uint32_t)w) == 0) { best = (int)(o - off); break; }
         }
         best = sym_block_min(S, best);
         if (best != 0x7fffffff) {
-            uint32_t w = start + off + (uint32_t)best;
+            unsigned long long w = (unsigned long long)start + off + (uint32_t)best;
             if (w >= d.N) w -= d.N;
             return (long long)w;
         }
