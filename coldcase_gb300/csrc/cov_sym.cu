@@ -346,7 +346,7 @@ __device__ __forceinline__ long long sym_walk_item(const SymSlot &d, const uint6
     }
     const int last = ps[rad - 1], cl = cov_nib(c, last);
     const int pl = (int)d.pw[last];
-    if (MODE == 0) {
+    if constexpr (MODE == 0) {
         const uint32_t a0 = w - (uint32_t)(cl * pl);       // the word with digit 0 at `last`
         if (d.q * pl <= 64) {
             // the q words a0 + v pl lie in two aligned 16-byte windows of the
@@ -390,9 +390,10 @@ __device__ __forceinline__ long long sym_walk_item(const SymSlot &d, const uint6
         for (int k = 0; k < COV_MAXQ - 1; k++)
             if (k < qm1) du += (long long)(ca[k] == 1) - (long long)(cb[k] == 0);
         return du;
+    } else {
+        for (int k = 0; k < qm1; k++) visit(w + (uint32_t)((k + (k >= cl) - cl) * pl));
+        return du;
     }
-    for (int k = 0; k < qm1; k++) visit(w + (uint32_t)((k + (k >= cl) - cl) * pl));
-    return du;
 }
 
 // Ball item r in [0, opi) of an orbit (centres in C): +1 / -1 on every word
@@ -1402,6 +1403,8 @@ size_t cov_sym_slot_bytes(const cov_sym_params *prm)
     return b;
 }
 
+int cov_sym_remove(cov_sym *p, int32_t slot);
+
 int cov_sym_add(cov_sym *p, const cov_sym_params *prm, int32_t *slot)
 {
     if (!p || !prm || !slot) return COV_EINVAL;
@@ -1506,10 +1509,12 @@ int cov_sym_add(cov_sym *p, const cov_sym_params *prm, int32_t *slot)
     h.used = true;
     p->slots[s] = h;
     int rc = sym_push(p, s);
-    if (rc) return rc;
     // greedy initialisation on the device
-    rc = sym_launch(p, std::vector<int>{s}, SMODE_INIT, 0);
-    if (rc) return rc;
+    if (!rc) rc = sym_launch(p, std::vector<int>{s}, SMODE_INIT, 0);
+    if (rc) {
+        cov_sym_remove(p, s);
+        return rc;
+    }
     *slot = s;
     return COV_OK;
 }
