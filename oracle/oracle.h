@@ -101,6 +101,8 @@ long long sym_init(sym_oracle *o);
 /* up to max_moves iterations; trace (capacity max_moves) gets one
  * cov_move_rec per move, with ncw = the candidate sample size */
 long long sym_run(sym_oracle *o, long long max_moves, cov_move_rec *trace);
+/* OpenMP threads for the estimates (default 1; the trajectory is the same) */
+void sym_set_threads(sym_oracle *o, int threads);
 long long sym_uncovered(const sym_oracle *o);
 long long sym_best_uncovered(const sym_oracle *o);
 long long sym_iters(const sym_oracle *o);

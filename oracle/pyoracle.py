@@ -69,6 +69,7 @@ def load():
     for f in ("sym_uncovered", "sym_best_uncovered", "sym_iters", "sym_kicks"):
         getattr(lib, f).restype = ctypes.c_longlong
         getattr(lib, f).argtypes = [P]
+    lib.sym_set_threads.argtypes = [P, ctypes.c_int]
     lib.sym_orbits.restype = ctypes.c_int
     lib.sym_orbits.argtypes = [P]
     lib.sym_get_rep.argtypes = [P, u8p]
@@ -316,12 +317,14 @@ def finish(text, q, n, R, M, fast=False):
 class SymOracle:
     """One restated symsearch run (cov/engine/symsearch.c:282-491)."""
 
-    def __init__(self, q, n, R, M, orbits=0, seed=12345, kick=2, stall=3000, cand=100000):
+    def __init__(self, q, n, R, M, orbits=0, seed=12345, kick=2, stall=3000, cand=100000, threads=1):
         self.lib = load()
         self.q, self.n, self.R, self.M = q, n, R, M
         self.h = self.lib.sym_create(q, n, R, M, orbits, seed, kick, stall, cand)
         if not self.h:
             raise ValueError("symsearch oracle: bad parameters")
+        if threads > 1:
+            self.lib.sym_set_threads(self.h, int(threads))
         self.orbits = self.lib.sym_orbits(self.h)
 
     def init(self):

@@ -22,6 +22,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include "oracle.h"
 
 typedef struct { uint64_t s[4]; } srng;
@@ -58,6 +61,7 @@ static inline uint64_t s_mod(srng *r, uint64_t m) { return s_next(r) % m; }
 
 struct sym_oracle {
     int q, n, R, NR, norb, kick, cand;
+    int threads;                     /* OpenMP threads for the estimates */
     long long stall;
     long long N;                     /* q^(n-1) quotient words */
     long long pw[32];
@@ -257,6 +261,7 @@ sym_oracle *sym_create(int q, int n, int R, int M, int orbits, uint64_t seed, in
     if (!o) return NULL;
     o->q = q; o->n = n; o->R = R; o->NR = n - 1; o->norb = norb;
     o->kick = kick; o->stall = stall; o->cand = cand;
+    o->threads = 1;
     o->N = s_ipow(q, o->NR);
     if (o->N > 4000000000LL) { free(o); return NULL; }
     for (int p = 0; p < o->NR; p++) o->pw[p] = s_ipow(q, o->NR - 1 - p);
@@ -359,6 +364,9 @@ long long sym_run(sym_oracle *o, long long max_moves, cov_move_rec *trace)
             o->ci[s] = o->ci[j]; o->cp[s] = o->cp[j]; o->cv[s] = o->cv[j];
             o->ci[j] = a; o->cp[j] = b; o->cv[j] = c;
         }
+        /* the estimates only read the counters, so they run in parallel
+         * (symsearch.c:432-433); the trajectory does not depend on it */
+#pragma omp parallel for schedule(dynamic, 1) if (take > 3 && o->threads > 1) num_threads(o->threads)
         for (int s = 0; s < take; s++) o->cd[s] = s_move(o, o->ci[s], o->cp[s], o->cv[s], 0);
         /* reservoir selection (:436-445) */
         int bi = -1, bp = -1, bv = -1, nties = 0, bs = -1;
@@ -420,6 +428,7 @@ long long sym_run(sym_oracle *o, long long max_moves, cov_move_rec *trace)
     return done;
 }
 
+void sym_set_threads(sym_oracle *o, int threads) { o->threads = threads > 0 ? threads : 1; }
 long long sym_uncovered(const sym_oracle *o) { return o->unc; }
 long long sym_best_uncovered(const sym_oracle *o) { return o->best_unc; }
 long long sym_iters(const sym_oracle *o) { return o->it; }

@@ -85,3 +85,15 @@ def test_sym_runs_match_reference(sym_golden):
         if got != want or sym_text(o.best(), r["q"]) != ref["out"] or (ref["rc"] == 0) != (got[1] == 0):
             bad.append((r["q"], r["n"], r["R"], r["M"], r["seed"], got, want))
     assert not bad, bad
+
+
+def test_sym_threads_do_not_change_trajectory(sym_golden):
+    from oracle.pyoracle import SymOracle
+    for r in [x for x in sym_golden if x["q"] ** (x["n"] - 1) > 20000][:3]:
+        traces = []
+        for th in (1, 4):
+            o = SymOracle(r["q"], r["n"], r["R"], r["M"], orbits=r["orbits"], seed=r["seed"], kick=r["kick"],
+                          stall=r["stall"], threads=th)
+            o.init()
+            traces.append(o.run(min(300, r["ref"]["iters"]), trace=True))
+        assert traces[0].tobytes() == traces[1].tobytes()
