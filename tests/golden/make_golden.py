@@ -16,6 +16,9 @@ Runs in the build container only (it needs the reference checkout):
                           with duplicates, malformed lines, too few and too
                           many words: COUNT line, exit status and --out file,
                           with and without --fast.
+  * opt_runs.json      -- the reference engine on the configurations of the
+                          optimisation gate cov/opt/selftest.sh (p5b, with
+                          and without --wide): fingerprint and --out file.
   * sym_runs.json      -- the reference quotient search (oracle/_ref/symsearch,
                           compiled from cov/engine/symsearch.c) on a cell
                           list with plain, short-stall and kick-3 runs and
@@ -226,6 +229,32 @@ def finish_cases(binary):
     return cases
 
 
+def opt_runs(binary):
+    """The configurations of the reference optimisation gate
+    (cov/opt/selftest.sh:24-33 and :54-62) on the reference engine: p5b at
+    seeds 1-3, and at seed 7 with and without --wide."""
+    runs = []
+    cfgs = [(6, 6, 3, 41, 2000), (6, 8, 4, 169, 150), (7, 5, 2, 120, 400), (3, 7, 1, 34, 1500),
+            (5, 4, 0, 600, 300), (4, 5, 4, 3, 100), (2, 8, 2, 12, 800), (6, 5, 2, 66, 900)]
+    for (q, n, R, M, it) in cfgs:
+        for s in (1, 2, 3):
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=s, iters=it, tabu=0, stall=5000, kick=2,
+                             random_init=False, code=None, wide=False))
+    cfgs2 = [(6, 4, 2, 15, 4000), (7, 3, 1, 25, 4000), (2, 8, 2, 12, 4000), (6, 6, 3, 41, 3000),
+             (3, 4, 1, 9, 4000), (5, 4, 1, 125, 2000), (6, 5, 2, 60, 1500)]
+    for (q, n, R, M, it) in cfgs2:
+        for wide in (False, True):
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=7, iters=it, tabu=0, stall=5000, kick=2,
+                             random_init=False, code=None, wide=wide))
+    for r in runs:
+        args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
+                "--threads", 1]
+        if r["wide"]:
+            args.append("--wide")
+        r["ref"] = run_ref(binary, args, None)
+    return runs
+
+
 def sym_text(rep, q):
     """symsearch's --out file: orbit by orbit, its q words (j, e + j)."""
     return "".join(DIG[j] + "".join(DIG[(int(x) + j) % q] for x in e) + "\n" for e in rep for j in range(q))
@@ -284,6 +313,9 @@ def main():
     fc = finish_cases(os.path.join(REPO, "oracle", "_ref", "covcount"))
     with open(os.path.join(HERE, "finish_cases.json"), "w") as f:
         json.dump(fc, f)
+    orr = opt_runs(binary)
+    with open(os.path.join(HERE, "opt_runs.json"), "w") as f:
+        json.dump(orr, f)
     sr = sym_runs(os.path.join(REPO, "oracle", "_ref", "symsearch"))
     with open(os.path.join(HERE, "sym_runs.json"), "w") as f:
         json.dump(sr, f)

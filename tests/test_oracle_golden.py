@@ -97,3 +97,26 @@ def test_sym_threads_do_not_change_trajectory(sym_golden):
             o.init()
             traces.append(o.run(min(300, r["ref"]["iters"]), trace=True))
         assert traces[0].tobytes() == traces[1].tobytes()
+
+
+def test_opt_gate_runs_match_reference():
+    """The configurations of the reference's optimisation gate
+    (cov/opt/selftest.sh): the oracle's fingerprint and --out file equal the
+    reference engine's, with and without --wide, and the written file's
+    count from the verifier equals the reported one."""
+    import json
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    with open(os.path.join(here, "opt_runs.json")) as f:
+        runs = json.load(f)
+    bad = []
+    for r in runs:
+        o, _ = oracle_run(r)
+        ref = r["ref"]
+        got = (o.best_uncovered(), o.iters(), o.kicks())
+        want = (ref["uncovered"], ref["iters"], ref["kicks"])
+        out = codefile.format_code(codefile.distinct_code(o.best(), r["q"], r["n"], r["M"]), r["q"])
+        words = code_from_text(ref["out"], r["n"])
+        if got != want or out != ref["out"] or po.verify_pure(words, r["q"], r["n"], r["R"]) != ref["uncovered"]:
+            bad.append((r["q"], r["n"], r["R"], r["M"], r["seed"], r["wide"], got, want))
+    assert not bad, bad
