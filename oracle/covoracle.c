@@ -7,8 +7,8 @@
  *
  * The algorithm is that of cov/engine/covsearch2e.c run as
  * `--preset p5b` (opt_hoist=1, opt_st=2, opt_eval=2; covsearch2e.c:1090),
- * with or without --wide (orc_set_wide), without --fix0, --sa, --noise,
- * --ucache or --upick.  Each function
+ * with or without --wide (orc_set_wide) and --fix0 (orc_set_fix0), without
+ * --sa, --noise, --ucache or --upick.  Each function
  * names the reference lines it restates.  Everything that decides the search
  * trajectory -- RNG consumption order, candidate order, tie-breaking, tabu
  * arithmetic -- is reproduced exactly; what only affects speed (offset
@@ -82,6 +82,7 @@ struct cov_oracle {
     orng rng;
     int tenure, kick, cand, threads;
     int wide;                       /* --wide: all n(q-1) moves per codeword */
+    int fix0;                       /* --fix0: codeword 0 translated to 0^n and frozen */
     size_t cand_cap;                /* entries of ci/cp/cv/cd */
     long long stall;
     long long it, since_improve, nkicks;
@@ -541,6 +542,16 @@ long long orc_init(cov_oracle *o, const uint8_t *code, int m, int random_init)
                 o->code[(size_t)i * n + j] = (uint8_t)orng_mod(&o->rng, (uint64_t)o->q);
         rebuild(o);
     }
+    if (o->fix0) {
+        /* translate the code so that codeword 0 is 0^n (an isometry), then
+         * keep it there: covsearch2e.c:1241-1253 */
+        uint8_t t0v[16];
+        memcpy(t0v, o->code, n);
+        for (int i = 0; i < M; i++)
+            for (int j = 0; j < n; j++)
+                o->code[(size_t)i * n + j] = (uint8_t)((o->code[(size_t)i * n + j] + o->q - t0v[j]) % o->q);
+        rebuild(o);
+    }
     memcpy(o->best, o->code, (size_t)M * n);
     o->best_unc = o->unc;
     o->ul_valid = 0;                /* built lazily: covsearch2e.c:1139 */
@@ -575,7 +586,7 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
 
         /* candidates: covsearch2e.c:1339-1380 */
         int dmin = n + 1;
-        for (int i = 0; i < M; i++) {
+        for (int i = o->fix0; i < M; i++) {
             const uint8_t *c = o->code + (size_t)i * n;
             int d = 0;
             for (int j = 0; j < n; j++) d += (c[j] != u[j]);
@@ -589,7 +600,7 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
         const int wide_now = o->wide && o->ul_valid &&
                              ((long long)o->ul_n * n < (long long)(R + 1) * o->totpat);
         int ncand = 0;
-        for (int i = 0; i < M; i++) {
+        for (int i = o->fix0; i < M; i++) {
             if (o->dist[i] != dtar) continue;
             const uint8_t *c = o->code + (size_t)i * n;
             if (wide_now) {
@@ -606,7 +617,7 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
             }
         }
         if (ncand == 0) {
-            int i = (int)orng_mod(&o->rng, (uint64_t)M);
+            int i = o->fix0 + (int)orng_mod(&o->rng, (uint64_t)(M - o->fix0));
             int p = (int)orng_mod(&o->rng, (uint64_t)n);
             o->ci[0] = i; o->cp[0] = p; o->cv[0] = u[p]; ncand = 1;
         }
@@ -673,7 +684,7 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
         } else if (++o->since_improve > o->stall) {
             /* kick: covsearch2e.c:1553-1579 */
             for (int t = 0; t < o->kick; t++) {
-                int i = (int)orng_mod(&o->rng, (uint64_t)M);
+                int i = o->fix0 + (int)orng_mod(&o->rng, (uint64_t)(M - o->fix0));
                 uint8_t *c = o->code + (size_t)i * n;
                 ball_apply(o, c, o->cidx[i], -1);
                 long long w = pick_uncovered(o);
@@ -723,6 +734,14 @@ int orc_set_wide(cov_oracle *o, int wide)
         o->cand_cap = cap;
     }
     o->wide = wide ? 1 : 0;
+    return 0;
+}
+
+/* --fix0 (covsearch2e.c:1074, :1241-1253); set before orc_init */
+int orc_set_fix0(cov_oracle *o, int fix0)
+{
+    if (fix0 && o->M < 2) return -1;
+    o->fix0 = fix0 ? 1 : 0;
     return 0;
 }
 

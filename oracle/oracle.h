@@ -68,6 +68,9 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target,
  * valid and short, the candidates are all n(q-1) moves of each codeword at
  * the target distance.  Returns 0, or -1 when out of memory. */
 int orc_set_wide(cov_oracle *o, int wide);
+/* --fix0 (covsearch2e.c:1241-1253): before orc_init; codeword 0 is moved to
+ * 0^n by translating the whole code and never moves again.  -1 if M < 2. */
+int orc_set_fix0(cov_oracle *o, int fix0);
 /* the uncovered-word list: valid flag and length, stale entries included */
 void orc_ul_state(const cov_oracle *o, int *valid, int *n);
 

@@ -55,6 +55,8 @@ def load():
     lib.orc_get_tabu.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
     lib.orc_get_rng.argtypes = [P, ctypes.POINTER(ctypes.c_uint64)]
     lib.orc_eval_codeword.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+    lib.orc_set_fix0.restype = ctypes.c_int
+    lib.orc_set_fix0.argtypes = [P, ctypes.c_int]
     lib.orc_set_wide.restype = ctypes.c_int
     lib.orc_set_wide.argtypes = [P, ctypes.c_int]
     lib.orc_ul_state.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
@@ -98,7 +100,7 @@ class Oracle:
     """One restated covsearch2e p5b search (covsearch2e.c:1023-1621)."""
 
     def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000, threads=1,
-                 wide=False):
+                 wide=False, fix0=False):
         self.lib = load()
         self.q, self.n, self.R, self.M = q, n, R, M
         self.h = self.lib.orc_create(q, n, R, M, seed, tabu, kick, stall, cand, threads)
@@ -107,6 +109,9 @@ class Oracle:
         if wide and self.lib.orc_set_wide(self.h, 1) != 0:
             self.close()
             raise MemoryError("oracle: no memory for the wide candidate set")
+        if fix0 and self.lib.orc_set_fix0(self.h, 1) != 0:
+            self.close()
+            raise ValueError("oracle: --fix0 needs M >= 2")
 
     def init(self, code=None, random_init=False):
         a = np.zeros((0, self.n), dtype=np.uint8) if code is None else \

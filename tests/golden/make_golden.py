@@ -18,7 +18,8 @@ Runs in the build container only (it needs the reference checkout):
                           with and without --fast.
   * opt_runs.json      -- the reference engine on the configurations of the
                           optimisation gate cov/opt/selftest.sh (p5b, with
-                          and without --wide): fingerprint and --out file.
+                          and without --wide, and --fix0): fingerprint and
+                          --out file.
   * sym_runs.json      -- the reference quotient search (oracle/_ref/symsearch,
                           compiled from cov/engine/symsearch.c) on a cell
                           list with plain, short-stall and kick-3 runs and
@@ -246,12 +247,24 @@ def opt_runs(binary):
         for wide in (False, True):
             runs.append(dict(q=q, n=n, R=R, M=M, seed=7, iters=it, tabu=0, stall=5000, kick=2,
                              random_init=False, code=None, wide=wide))
+    # --fix0 (codeword 0 translated to 0^n and frozen), also with kicks and
+    # from a given code
+    for (q, n, R, M, it) in cfgs2[:5]:
+        runs.append(dict(q=q, n=n, R=R, M=M, seed=7, iters=it, tabu=0, stall=5000, kick=2,
+                         random_init=False, code=None, wide=False, fix0=True))
+        runs.append(dict(q=q, n=n, R=R, M=M, seed=8, iters=it, tabu=5, stall=40, kick=2,
+                         random_init=False, code=None, wide=False, fix0=True))
+    code = np.random.default_rng(55).integers(0, 6, (41, 6), dtype=np.uint8)
+    runs.append(dict(q=6, n=6, R=3, M=41, seed=9, iters=1500, tabu=7, stall=50, kick=2, random_init=False,
+                     code=code_text(code), wide=True, fix0=True))
     for r in runs:
         args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
-                "--threads", 1]
+                "--threads", 1, "--tabu", r["tabu"], "--stall", r["stall"], "--kick", r["kick"]]
         if r["wide"]:
             args.append("--wide")
-        r["ref"] = run_ref(binary, args, None)
+        if r.get("fix0"):
+            args.append("--fix0")
+        r["ref"] = run_ref(binary, args, r["code"])
     return runs
 
 

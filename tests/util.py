@@ -17,7 +17,8 @@ def oracle_run(run, threads=1):
     """Replay one golden run on the oracle; returns (oracle, trace)."""
     from oracle.pyoracle import Oracle
     o = Oracle(run["q"], run["n"], run["R"], run["M"], seed=run["seed"], tabu=run["tabu"],
-               kick=run["kick"], stall=run["stall"], threads=threads, wide=run.get("wide", False))
+               kick=run["kick"], stall=run["stall"], threads=threads, wide=run.get("wide", False),
+               fix0=run.get("fix0", False))
     code = code_from_text(run["code"], run["n"]) if run["code"] else None
     o.init(code, random_init=run["random_init"])
     tr = o.run(run["iters"], trace=True)
