@@ -53,16 +53,107 @@ def workload_name(restarts, moves):
 
 
 # ------------------------------------------------------------------ CPU ----
+REF_DIR = os.path.join(HERE, "baseline", "_ref")
+WARM_NPZ = os.path.join(HERE, "tests", "golden", "warm_q7n9.npz")
+WARM_JSON = os.path.join(HERE, "tests", "golden", "warm_q7n9.json")
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def ref_exe():
+    """The reference engine (cov/engine/covsearch2e.c, unchanged), built from
+    its copy under baseline/_ref by oracle/Makefile's refbin recipe; None
+    when this host has no copy."""
+    exe = os.path.join(REF_DIR, "bin", "covsearch2e")
+    if not os.path.exists(exe) and os.path.exists(os.path.join(REF_DIR, "cov", "engine", "covsearch2e.c")):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "oracle"), exe], capture_output=True)
+    return exe if os.path.exists(exe) else None
+
+
+def warm_state():
+    """The restarts' codes at the start of the timed window: the oracle's
+    codes of restarts 0..15 after `moves` moves (tests/golden/make_warm.py)."""
+    import numpy as np
+    d = np.load(WARM_NPZ)
+    with open(WARM_JSON) as f:
+        moves = json.load(f)["moves"]
+    return d["codes"], [int(x) for x in d["seeds"]], moves
+
+
+def _code_file(d, name, code, q):
+    from coldcase_gb300 import codefile
+    path = os.path.join(d, name)
+    with open(path, "w") as f:
+        f.write(codefile.format_code(code, q))
+    return path
+
+
+def ref_processes(exe, jobs, tlimit=600.0):
+    """Run one reference process per job concurrently (single-threaded, as
+    covengine runs its chains): job = (q, n, R, M, code file, seed, tabu,
+    iters).  Returns [(iters, seconds after init, wall seconds)], from each
+    process's own RESULT line (covsearch2e.c:1582-1589)."""
+    import re
+    rx = re.compile(r"RESULT .* iters=(\d+) .*time=([0-9.]+) ")
+    procs = []
+    for (q, n, R, M, path, seed, tabu, iters) in jobs:
+        cmd = [exe, "-q", str(q), "-n", str(n), "-R", str(R), "-M", str(M), "--preset", "p5b", "--in", path,
+               "-s", str(seed), "--tabu", str(tabu), "--iters", str(iters), "--threads", "1", "-t", str(tlimit),
+               "--quiet"]
+        procs.append((time.monotonic(), subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                                         text=True)))
+    out = []
+    for t0, p in procs:
+        txt, _ = p.communicate()
+        wall = time.monotonic() - t0
+        m = rx.search(txt or "")
+        if not m:
+            raise RuntimeError("reference engine printed no RESULT line (rc %s)" % p.returncode)
+        out.append((int(m.group(1)), float(m.group(2)), wall))
+    return out
+
+
+def ref_measure(warmup, steps, moves, cores=None):
+    """The reference engine on this host's cores: `cores` concurrent
+    single-thread processes, restart i started from its code at the start of
+    the GPU's timed window (warm_state), `moves` moves per step.  The rate of
+    a step is the sum of the processes' own rates (moves / seconds after
+    init); the value is the mean over the timed steps."""
+    exe = ref_exe()
+    if exe is None:
+        return None
+    codes, seeds, at = warm_state()
+    cores = min(cores or host_cores(), len(codes))
+    rates, walls = [], []
+    with tempfile.TemporaryDirectory() as d:
+        files = [_code_file(d, "w%02d.txt" % i, codes[i], Q) for i in range(cores)]
+        for k in range(warmup + steps):
+            t0 = time.monotonic()
+            res = ref_processes(exe, [(Q, N_, R_, M_, files[i], seeds[i] + k, TENURE, moves) for i in range(cores)])
+            if k >= warmup:
+                rates.append(sum(it / t for it, t, _ in res if t > 0))
+                walls.append(time.monotonic() - t0)
+    return dict(value=statistics.mean(rates), cores=cores, kind="reference", seconds=sum(walls),
+                sample="%d concurrent single-thread covsearch2e --preset p5b processes x %d moves x %d steps, "
+                       "restart i from its code after %d moves (the GPU's timed window), rate after init"
+                       % (cores, moves, steps, at))
+
+
 def _cpu_worker(args):
-    """One restart on the oracle (single thread): untimed init, then the
-    timed steps; each step starts at a shared barrier."""
+    """One restart on the oracle (single thread) from its warm code:
+    untimed init, then the timed steps; each step starts at a shared
+    barrier."""
     idx, steps, moves, barrier = args
     sys.path.insert(0, HERE)
     from oracle.pyoracle import Oracle
-    from coldcase_gb300.workloads import instance_seed, uniform_code
-    seed = instance_seed(BASE_SEED, idx)
-    o = Oracle(Q, N_, R_, M_, seed=seed, tabu=TENURE, threads=1)
-    o.init(uniform_code(Q, N_, M_, seed))
+    codes, seeds, _ = warm_state()
+    o = Oracle(Q, N_, R_, M_, seed=seeds[idx], tabu=TENURE, threads=1)
+    o.init(codes[idx])
     out = []
     for _ in range(steps):
         barrier.wait()
@@ -74,9 +165,10 @@ def _cpu_worker(args):
 
 
 def cpu_measure(warmup, steps, moves, cores=None):
-    """Aggregate moves/s of `cores` concurrent single-thread restarts."""
-    if cores is None:
-        cores = len(os.sched_getaffinity(0))
+    """The oracle port: aggregate moves/s of `cores` concurrent single-thread
+    restarts from the same warm codes as ref_measure."""
+    codes, _, at = warm_state()
+    cores = min(cores or host_cores(), len(codes))
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "oracle")], check=True)
     ctx = mp.get_context("spawn")
     mgr = ctx.Manager()
@@ -84,17 +176,89 @@ def cpu_measure(warmup, steps, moves, cores=None):
     with ctx.Pool(cores) as pool:
         res = pool.map(_cpu_worker, [(i, warmup + steps, moves, barrier) for i in range(cores)])
     mgr.shutdown()
-    rates = []
     total_m, total_t = 0, 0.0
     for k in range(warmup, warmup + steps):
-        m = sum(r[k][0] for r in res)
-        t = max(r[k][2] for r in res) - min(r[k][1] for r in res)
-        total_m += m
-        total_t += t
-        rates.append(m / t)
-    return dict(value=total_m / total_t, cores=cores, moves=total_m, seconds=total_t,
-                sample="%d concurrent restarts x %d moves x %d steps (after untimed init)"
-                       % (cores, moves, steps))
+        total_m += sum(r[k][0] for r in res)
+        total_t += max(r[k][2] for r in res) - min(r[k][1] for r in res)
+    return dict(value=total_m / total_t, cores=cores, moves=total_m, seconds=total_t, kind="port",
+                sample="%d concurrent oracle restarts x %d moves x %d steps from their codes after %d moves "
+                       "(after untimed init)" % (cores, moves, steps, at))
+
+
+def ref_cells_measure(cells, moves, tlimit=600.0, cores=None, min_s=0.3):
+    """CPU baseline of a set of independent cells (the uneven batch, the
+    served requests): every distinct (q, n, R, M) shape once on the
+    reference engine from a uniform code, up to `cores` processes at a time;
+    a shape is re-run with ten times the moves while its run took under
+    `min_s` seconds after init (and did not cover), so that its rate is
+    timed precisely.  Returns per shape (rate after init, init seconds) and
+    the batch's modelled CPU time: each cell costs init + its own move budget
+    / its shape's rate on one core, the cores share the cells perfectly."""
+    from coldcase_gb300.workloads import uniform_code
+    exe = ref_exe()
+    if exe is None:
+        return None
+    cores = cores or host_cores()
+    shapes = sorted({(c["q"], c["n"], c["R"], c["M"]) for c in cells})
+    rate = {}
+    iters = {sh: moves for sh in shapes}
+    with tempfile.TemporaryDirectory() as d:
+        files = {sh: _code_file(d, "c%d.txt" % j, uniform_code(sh[0], sh[1], sh[3], 4242 + j), sh[0])
+                 for j, sh in enumerate(shapes)}
+        pending = list(shapes)
+        for _ in range(4):
+            if not pending:
+                break
+            again = []
+            for b in range(0, len(pending), cores):
+                part = pending[b:b + cores]
+                jobs = [(q, n, R, M, files[(q, n, R, M)], 4242, 0, iters[(q, n, R, M)]) for (q, n, R, M) in part]
+                for sh, (it, t, wall) in zip(part, ref_processes(exe, jobs, tlimit)):
+                    rate[sh] = (it / t if t > 0 and it > 0 else None, max(0.0, wall - t))
+                    if t < min_s and it >= iters[sh]:
+                        iters[sh] *= 10
+                        again.append(sh)
+            pending = again
+    per_cell = []
+    for c in cells:
+        r, init = rate[(c["q"], c["n"], c["R"], c["M"])]
+        per_cell.append(init + (c["moves"] / r if r else 0.0))
+    total_moves = sum(c["moves"] for c in cells)
+    cpu_s = sum(per_cell) / cores
+    return dict(value=total_moves / cpu_s, unit="moves/s", cores=cores, kind="reference", per_cell_s=per_cell,
+                shapes=len(shapes),
+                sample="each of %d distinct (q,n,R,M) shapes on covsearch2e --preset p5b from a uniform code, "
+                       ">= %d moves (more until >= %.1f s after init); every cell costs init + its move budget "
+                       "at its shape's rate on one core, %d cores shared perfectly"
+                       % (len(shapes), moves, min_s, cores))
+
+
+
+def cells_cpu_measure(args, world):
+    """CPU baselines of the uneven-cells and served legs (one reference
+    process per cell or request, concurrent up to the host's cores),
+    sampled per distinct shape (ref_cells_measure)."""
+    import numpy as np
+    from coldcase_gb300 import workloads
+    out = {}
+    if not args.no_hetero:
+        cells = workloads.hetero_cells(count=args.cells * world)
+        for c in cells:
+            c["moves"] = args.cell_moves
+        r = ref_cells_measure(cells, args.cell_cpu_moves)
+        if r:
+            r.pop("per_cell_s")
+            out["hetero"] = r
+    if not args.no_serve:
+        reqs = workloads.serve_requests(args.requests * world, lam=args.lam * world, seed=2027)
+        r = ref_cells_measure(reqs, args.cell_cpu_moves)
+        if r:
+            svc = np.array(r.pop("per_cell_s"))
+            r["p50_s"] = float(np.percentile(svc, 50))
+            r["p99_s"] = float(np.percentile(svc, 99))
+            r["latency_note"] = "service time of each request alone on one core (init + budget / rate), no queueing"
+            out["served"] = r
+    return out
 
 
 # --------------------------------------------------------------- clocks ----
@@ -210,6 +374,285 @@ def sym_cpu_measure(moves):
                 sample="K_8(9,4)@940 seed 1000: %d moves after init and one untimed move" % moves)
 
 
+def dt_pass_bytes(q, n):
+    """HBM bytes the distance transform's kernels must move per launch: the
+    code bitmap read (N/8), the low-axes tile pass writing every word once
+    (N), and one read + write of every word per high-axes strip pass (the
+    same grouping of axes as cov_verify.cu's dt_run)."""
+    N = q ** n
+    q4 = (q + 3) // 4 * 4
+    k = 1
+    while k < n and q ** (k + 1) // q * q4 <= 65536:
+        k += 1
+    passes, j0 = 0, k
+    while j0 < n:
+        g = 0
+        while j0 + g < n and q ** (g + 1) * 32 <= 98304:
+            g += 1
+        j0 += g
+        passes += 1
+    return N // 8 + N + 2 * N * passes
+
+
+COVERAGE_CELLS = (   # (q, n, R, M): the headline cell and the reference's published transform sizes
+    (7, 9, 4, 1500),
+    (7, 10, 5, 163),     # M = ceil(1.3 q^n / |B|)
+    (8, 10, 4, 2549),
+)
+
+
+def coverage_bench(args, code79, dev):
+    """Words/s of the distance transform (cov_mindist_dev) and of the
+    coverage count (cov_count_dev) at 7^9 (the headline code) and at 7^10 /
+    8^10 (HBM-resident), each with its roofline, plus the CPU baselines at
+    7^9: the oracle's line-min transform on all host cores and the
+    reference's own verifiers (verify_cov.py --method numpy,
+    verify_independent.py --method dilate) as processes."""
+    import numpy as np
+    import torch
+    from coldcase_gb300 import lib as L
+    from coldcase_gb300.workloads import uniform_code
+    lib = L.load()
+    peak, kind = measured_peaks()
+    out = {}
+    for (q, n, R, M) in COVERAGE_CELLS:
+        code = code79 if (q, n, M) == (Q, N_, M_) else uniform_code(q, n, M, 77)
+        Nw = q ** n
+        code_d = torch.from_numpy(np.ascontiguousarray(code)).to(dev)
+        dist_d = torch.empty(Nw, dtype=torch.uint8, device=dev)
+        cnt_d = torch.empty(Nw + 1, dtype=torch.int16, device=dev)
+        st = torch.cuda.Stream(device=dev)
+        cs = st.cuda_stream
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st):
+            for _ in range(3):
+                L.check(lib.cov_mindist_dev(q, n, code_d.data_ptr(), M, dist_d.data_ptr(), cs))
+            reps = max(5, args.steps) if Nw < 1e8 else 5
+            a.record(st)
+            for _ in range(reps):
+                L.check(lib.cov_mindist_dev(q, n, code_d.data_ptr(), M, dist_d.data_ptr(), cs))
+            b.record(st)
+            st.synchronize()
+            dt_ms = a.elapsed_time(b) / reps
+            for _ in range(2):
+                L.check(lib.cov_count_dev(q, n, R, code_d.data_ptr(), M, cnt_d.data_ptr(), cs))
+            st.synchronize()
+            a.record(st)
+            for _ in range(3):
+                L.check(lib.cov_count_dev(q, n, R, code_d.data_ptr(), M, cnt_d.data_ptr(), cs))
+            b.record(st)
+            st.synchronize()
+            ct_ms = a.elapsed_time(b) / 3
+        unc_dt = int((dist_d > R).sum())
+        unc_ct = int((cnt_d[:Nw] == 0).sum())
+        if unc_dt != unc_ct:
+            raise RuntimeError("distance transform and count disagree at %d^%d: %d vs %d" % (q, n, unc_dt, unc_ct))
+        algo = 2 * n * Nw                       # n per-axis uint8 read+write sweeps
+        need = dt_pass_bytes(q, n)
+        cbytes = 2 * 2 * M * sum(math.comb(n, i) * (q - 1) ** i for i in range(R + 1))
+        key = "q%dn%d" % (q, n)
+        out[key] = dict(
+            q=q, n=n, R=R, M=M, words=Nw, uncovered=unc_dt,
+            l2="resident (%.0f MB uint8 array)" % (Nw / 1e6) if Nw < 1.2e8 else
+               "HBM-resident (%.0f MB uint8 array > L2)" % (Nw / 1e6),
+            dt=dict(ms=dt_ms, words_s=Nw / (dt_ms / 1e3),
+                    roofline=dict(bound="hbm", achieved=algo / (dt_ms / 1e3) / 1e9, peak=peak, unit="GB/s",
+                                  frac=algo / (dt_ms / 1e3) / 1e9 / peak, algorithmic_bytes=algo,
+                                  pass_bytes=need, pass_frac=need / (dt_ms / 1e3) / 1e9 / peak,
+                                  peak_source=kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                                  note="algorithmic bytes = 2 n N (n axis passes, uint8 read + write); "
+                                       "the kernels fuse the passes into %d HBM sweeps, pass_bytes" % (
+                                           1 + (need - Nw // 8 - Nw) // (2 * Nw)))),
+            count=dict(ms=ct_ms, words_s=Nw / (ct_ms / 1e3),
+                       roofline=dict(bound="hbm", achieved=cbytes / (ct_ms / 1e3) / 1e9, peak=peak, unit="GB/s",
+                                     frac=cbytes / (ct_ms / 1e3) / 1e9 / peak, algorithmic_bytes=cbytes,
+                                     written_bytes=2 * Nw,
+                                     note="algorithmic bytes = 2 b_c M V (ball marking RMW, b_c = 2); the "
+                                          "tiles mark in shared memory and write each count once (2 N)")))
+        del code_d, dist_d, cnt_d
+        torch.cuda.empty_cache()
+    # CPU baselines of the 7^9 transform / count
+    cpu = {}
+    try:
+        from oracle import pyoracle as po
+        cores = host_cores()
+        po.mindist(code79[:4], Q, N_, threads=cores)     # warm the library
+        t0 = time.perf_counter()
+        d_cpu = po.mindist(code79, Q, N_, threads=cores)
+        t1 = time.perf_counter()
+        cpu["line_min_port"] = dict(value=Q ** N_ / (t1 - t0), unit="words/s", seconds=t1 - t0, cores=cores,
+                                    kind="port", sample="the whole 7^9 transform, oracle/dtoracle.c")
+        if int((d_cpu > R_).sum()) != out["q7n9"]["uncovered"]:
+            raise RuntimeError("CPU and GPU transforms disagree")
+    except (OSError, ImportError) as e:
+        cpu["line_min_port"] = dict(unavailable=str(e))
+    vdir = os.path.join(REF_DIR, "cov")
+    if os.path.exists(os.path.join(vdir, "verify_cov.py")):
+        with tempfile.TemporaryDirectory() as d:
+            path = _code_file(d, "c.txt", code79, Q)
+            for name, cmd in (("verify_numpy", [sys.executable, os.path.join(vdir, "verify_cov.py"), path, "-q",
+                                                 str(Q), "-n", str(N_), "-R", str(R_), "--method", "numpy"]),
+                              ("dilate", [sys.executable, os.path.join(vdir, "verify_independent.py"), path, "-q",
+                                          str(Q), "-n", str(N_), "-R", str(R_), "--method", "dilate"])):
+                t0 = time.perf_counter()
+                p = subprocess.run(cmd, capture_output=True, text=True)
+                t1 = time.perf_counter()
+                cpu[name] = dict(value=Q ** N_ / (t1 - t0), unit="words/s", seconds=t1 - t0, cores=1,
+                                 kind="reference", rc=p.returncode,
+                                 sample="process wall time, the whole 7^9 verification of the headline code")
+    out["cpu_baseline"] = cpu
+    return out
+
+
+CHAIN_CELLS = (   # (label, q, n, R, M, iters per chain): the reference's idle benchmark cells
+    ("K6(6,3)@41", 6, 6, 3, 41, 2000),
+    ("K6(8,4)@169", 6, 8, 4, 169, 300),
+    ("K8(9,4)@2944", 8, 9, 4, 2944, 40),
+)
+DCT_CELLS = ((7, 9, 4, 1500), (7, 10, 5, 163))
+
+_REF_CHAIN = r"""
+import json, sys, time
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from chain import run, random_code
+q, n, R, M, chains, iters, seed = map(int, sys.argv[2:9])
+code = random_code(q, n, M, np.random.default_rng(seed))
+t0 = time.perf_counter()
+r = run(q, n, R, code, nchains=chains, iters=iters, seed=seed)
+dt = time.perf_counter() - t0
+print(json.dumps(dict(wall_s=dt, iters=int(r["iters"].sum()), best_u_median=float(np.median(r["best_u"])),
+                      solved=int(r["solved"].sum()))))
+"""
+
+_REF_DCT = r"""
+import json, sys, time
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from dctlib import DCT
+q, n, R, M, seed = map(int, sys.argv[2:7])
+code = np.random.default_rng(seed).integers(0, q, (M, n), dtype=np.uint8)
+e = DCT(q, n, R)
+idx = e.word_index(code)
+e.recount(idx)
+out = {}
+for name, fn in (("count", lambda: e.recount(idx)), ("gain_map", e.gain_map)):
+    fn()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        fn()
+    out[name + "_ms"] = (time.perf_counter() - t0) / 3 * 1e3
+e.recount(idx)
+out["uncovered"] = e.uncovered()
+e.close()
+print(json.dumps(out))
+"""
+
+
+def gpu_comparators(args, dev):
+    """The reference's own GPU kernels, rebuilt for sm_103a from their copy
+    and driven through their own ctypes drivers (cov/gemm2/chain.py,
+    cov/gemm2/dctlib.py) in a child process, beside this engine's entry
+    points on the same cells and inputs:
+      chain      chain_run (chainsolve.cu:370-375) vs cov_chain_run (the same
+                 C ABI), 256 chains from one uniform code, wall time of the
+                 whole call as the reference's idle benchmark takes it;
+      transform  dct_transform code -> cnt (dct.cu:360-411, OUT=2) and the
+                 gain map ([cnt==0] -> sum, OUT=1) vs cov_count_dev and
+                 cov_lns_map(0).
+    chain_kernel's 32-bit atomics on 16-bit counter pairs are misaligned for
+    a chain whose counter array starts at an odd word (odd q^n and odd chain
+    index), so it is only run on the reference's own even-q cells."""
+    import ctypes
+    import numpy as np
+    import torch
+    from coldcase_gb300 import lib as L
+    gem = os.path.join(REF_DIR, "cov", "gemm2")
+    libs = [os.path.join(gem, f) for f in ("libchain.so", "libdct.so")]
+    if not all(os.path.exists(x) for x in libs) and os.path.exists(os.path.join(gem, "chainsolve.cu")):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "oracle")] + libs, capture_output=True)
+    if not all(os.path.exists(x) for x in libs):
+        return dict(unavailable="the reference's GPU sources are not on this host (baseline/_ref)")
+    lib = L.load()
+    out = dict(chain={}, transform={}, chains=args.comp_chains,
+               note="reference kernels compiled here with nvcc -O3 -gencode arch=compute_103a,code=sm_103a")
+    for label, q, n, R, M, iters in CHAIN_CELLS:
+        seed = 23
+        p = subprocess.run([sys.executable, "-c", _REF_CHAIN, gem, str(q), str(n), str(R), str(M),
+                            str(args.comp_chains), str(iters), str(seed)], capture_output=True, text=True)
+        if p.returncode != 0:
+            out["chain"][label] = dict(error=(p.stderr or p.stdout)[-300:])
+            continue
+        ref = json.loads(p.stdout.strip().splitlines()[-1])
+        code = np.random.default_rng(seed).integers(0, q, size=(M, n), dtype=np.uint8)
+        rows = np.zeros((args.comp_chains, M, 16), dtype=np.uint8)
+        rows[:, :, :n] = code
+        best = np.zeros_like(rows)
+        bu = np.zeros(args.comp_chains, np.int32)
+        sv = np.zeros(args.comp_chains, np.int32)
+        io = np.zeros(args.comp_chains, np.int64)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = lib.cov_chain_run(q, n, R, M, args.comp_chains, ctypes.c_longlong(iters), ctypes.c_ulonglong(seed),
+                               256, L.u8ptr(rows), L.u8ptr(best), bu.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                               sv.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                               io.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+        dt = time.perf_counter() - t0
+        L.check(rc, "cov_chain_run")
+        ours = dict(wall_s=dt, iters=int(io.sum()), best_u_median=float(np.median(bu)), solved=int(sv.sum()))
+        out["chain"][label] = dict(
+            iters_per_chain=iters,
+            reference=dict(ref, agg_moves_s=ref["iters"] / ref["wall_s"]),
+            ours=dict(ours, agg_moves_s=ours["iters"] / ours["wall_s"]),
+            speedup=(ours["iters"] / ours["wall_s"]) / (ref["iters"] / ref["wall_s"]))
+    for (q, n, R, M) in DCT_CELLS:
+        seed = 91
+        p = subprocess.run([sys.executable, "-c", _REF_DCT, gem, str(q), str(n), str(R), str(M), str(seed)],
+                           capture_output=True, text=True)
+        key = "q%dn%dR%d" % (q, n, R)
+        if p.returncode != 0:
+            out["transform"][key] = dict(error=(p.stderr or p.stdout)[-300:])
+            continue
+        ref = json.loads(p.stdout.strip().splitlines()[-1])
+        code = np.random.default_rng(seed).integers(0, q, (M, n), dtype=np.uint8)
+        code_d = torch.from_numpy(code).to(dev)
+        cnt_d = torch.empty(q ** n + 1, dtype=torch.int16, device=dev)
+        st = torch.cuda.current_stream(dev).cuda_stream
+        L.check(lib.cov_count_dev(q, n, R, code_d.data_ptr(), M, cnt_d.data_ptr(), st))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            L.check(lib.cov_count_dev(q, n, R, code_d.data_ptr(), M, cnt_d.data_ptr(), st))
+        torch.cuda.synchronize()
+        c_ms = (time.perf_counter() - t0) / 3 * 1e3
+        unc = int((cnt_d[: q ** n] == 0).sum())
+        del cnt_d, code_d
+        from coldcase_gb300.lns import TransformEngine
+        te = TransformEngine(q, n, R)
+        te.recount(te.word_index(code))
+        te.gain_map()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            te.gain_map()
+        g_ms = (time.perf_counter() - t0) / 3 * 1e3
+        te.close()
+        torch.cuda.empty_cache()
+        out["transform"][key] = dict(
+            M=M, reference=ref, ours=dict(count_ms=c_ms, gain_map_ms=g_ms, uncovered=unc),
+            count_speedup=ref["count_ms"] / c_ms, gain_map_speedup=ref["gain_map_ms"] / g_ms,
+            note="wall time of each call after a warm-up; the reference's dct_transform ends in "
+                 "cudaDeviceSynchronize, cov_count_dev in a stream synchronize")
+        if ref["uncovered"] != unc:
+            out["transform"][key]["mismatch"] = "uncovered %d (reference) vs %d" % (ref["uncovered"], unc)
+    return out
+
+
+def ctypes_sizeof_status():
+    from coldcase_gb300 import lib as L
+    import ctypes
+    return ctypes.sizeof(L.CovStatus)
+
+
 def gpu_bench(args, rank, world, dist):
     import numpy as np
     import torch
@@ -270,15 +713,21 @@ def gpu_bench(args, rank, world, dist):
     work = dict(ncw=sum(b["sum_ncw"] - a["sum_ncw"] for a, b in zip(prof0, prof1)) / max(1, pm),
                 ul_n=sum(b["sum_ul_n"] - a["sum_ul_n"] for a, b in zip(prof0, prof1)) / max(1, pm))
 
-    # ---------------- e2e: host buffers through the public API
+    # ---------------- e2e: host buffers through the public API.  The host
+    # holds the search state between steps as a caller of the covsearch2e
+    # CLI does (its --in / --out codes): every step uploads each restart's
+    # code from pinned host memory, rebuilds its state on the device, runs
+    # --moves moves and reads the current code back (it seeds the next step)
+    # with the restarts' status.  The warm-up steps bring the codes to the
+    # same phase of the search as the device-timed window.
     e2e = None
     if not args.no_e2e:
-        pinned = [torch.from_numpy(c).pin_memory() for c in codes]
+        pinned = [torch.from_numpy(c.copy()).pin_memory() for c in codes]
         e_moves, e_t = 0, 0.0
         t_load = t_run = t_read = 0.0
         h2d = sum(int(c.numel()) for c in pinned)
-        d2h = args.restarts * M_ * N_
-        for k in range(args.e2e_steps):
+        d2h = args.restarts * M_ * N_ + args.restarts * ctypes_sizeof_status()
+        for k in range(args.warmup + args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.monotonic()
             for i, sl in enumerate(slots):
@@ -287,19 +736,21 @@ def gpu_bench(args, rank, world, dist):
             pool.run(S)
             t2 = time.monotonic()
             stt = pool.status_all(args.restarts)
-            for sl in slots:
-                pool.best(sl)
+            for i, sl in enumerate(slots):
+                pinned[i].numpy()[:] = pool.code(sl)
             t3 = time.monotonic()
+            if k < args.warmup:
+                continue
             e_t += t3 - t0
             t_load += t1 - t0
             t_run += t2 - t1
             t_read += t3 - t2
-            e_moves += sum(s["it"] for s in stt)
+            e_moves += sum(x["it"] for x in stt)
         e_t, e_moves = replicas.combine(dist, e_t, e_moves, device=dev)     # slowest rank, all moves
-        e2e = dict(value=e_moves / e_t, unit="moves/s", h2d_bytes_per_step=h2d,
-                   d2h_bytes_per_step=d2h + args.restarts * 72,
-                   note="per step: %d restarts re-seeded from pinned host codes (state build included), "
-                        "%d moves each from the fresh codes, every best code read back" % (args.restarts, S),
+        e2e = dict(value=e_moves / e_t, unit="moves/s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h,
+                   note="per step: %d restarts re-seeded from pinned host codes (state build included), %d moves "
+                        "each, every current code read back for the next step; %d untimed warm-up steps, then %d "
+                        "timed" % (args.restarts, S, args.warmup, args.e2e_steps),
                    ms_per_step=dict(load=1e3 * t_load / args.e2e_steps, run=1e3 * t_run / args.e2e_steps,
                                     read=1e3 * t_read / args.e2e_steps))
     pool.close()
@@ -357,44 +808,14 @@ def gpu_bench(args, rank, world, dist):
     # ---------------- coverage words/s: distance transform and count
     cov = None
     if rank == 0 and not args.no_cov:
-        lib = L.load()
-        code_d = torch.from_numpy(codes[0]).to(dev)
-        Nw = Q ** N_
-        dist_d = torch.empty(Nw, dtype=torch.uint8, device=dev)
-        cnt_d = torch.empty(Nw + 1, dtype=torch.int16, device=dev)
-        cs = torch.cuda.current_stream(dev).cuda_stream
-        for _ in range(3):
-            L.check(lib.cov_mindist_dev(Q, N_, code_d.data_ptr(), M_, dist_d.data_ptr(), cs))
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = max(5, args.steps)
-        a.record()
-        for _ in range(reps):
-            L.check(lib.cov_mindist_dev(Q, N_, code_d.data_ptr(), M_, dist_d.data_ptr(), cs))
-        b.record()
-        torch.cuda.synchronize()
-        dt_ms = a.elapsed_time(b) / reps
-        for _ in range(2):
-            L.check(lib.cov_count_dev(Q, N_, R_, code_d.data_ptr(), M_, cnt_d.data_ptr(), cs))
-        torch.cuda.synchronize()
-        a.record()
-        for _ in range(3):
-            L.check(lib.cov_count_dev(Q, N_, R_, code_d.data_ptr(), M_, cnt_d.data_ptr(), cs))
-        b.record()
-        torch.cuda.synchronize()
-        ct_ms = a.elapsed_time(b) / 3
-        unc_dt = int((dist_d > R_).sum())
-        unc_ct = int((cnt_d[:Nw] == 0).sum())
-        if unc_dt != unc_ct:
-            raise RuntimeError("distance transform and count disagree: %d vs %d" % (unc_dt, unc_ct))
-        cov = dict(dt_words_s=Nw / (dt_ms / 1e3), dt_ms=dt_ms, count_words_s=Nw / (ct_ms / 1e3), count_ms=ct_ms,
-                   dt_traffic_bytes=int(Nw * 3.25), uncovered=unc_dt)
+        cov = coverage_bench(args, codes[0], dev)
     # ---------------- heterogeneous cells: one tuned graph launch
     hetero = None
     if not args.no_hetero:
         from coldcase_gb300 import workloads
         from coldcase_gb300.batch import Batch, tune_batch
-        cells = replicas.shard(workloads.hetero_cells(count=args.cells * world), rank, world)
+        h_rej = []
+        cells = replicas.shard(workloads.hetero_cells(count=args.cells * world, rejected=h_rej), rank, world)
         for c in cells:
             c["moves"] = args.cell_moves
         t0 = time.monotonic()
@@ -422,6 +843,11 @@ def gpu_bench(args, rank, world, dist):
         hetero = dict(value=hmoves_all / (hms_max / 1e3), unit="moves/s", cells=len(cells) * world,
                       moves_per_cell=args.cell_moves, ms=hms_max, clusters=plan, plan_estimate_s=est,
                       tune_s=t_tune,
+                      outside_domain=dict(count=len(h_rej), cells=sorted({(c["q"], c["n"], c["R"], c["M"])
+                                                                           for c in h_rej}),
+                                          note="draws with M > 65535: outside the reference engine's domain "
+                                               "(covsearch2e.c:1117) and this engine's; redrawn, no CPU baseline "
+                                               "/ parity unpinned"),
                       launches=("launches of %d moves, clusters widened between them while SMs are spare"
                                 % args.cell_segment) if args.cell_segment else
                       "one graph: one persistent kernel per cluster size")
@@ -432,8 +858,9 @@ def gpu_bench(args, rank, world, dist):
         from coldcase_gb300 import workloads
         from coldcase_gb300.serve import Server
         from coldcase_gb300.batch import tune_batch
+        s_rej = []
         reqs = replicas.shard(workloads.serve_requests(args.requests * world, lam=args.lam * world,
-                                                       seed=2027), rank, world)
+                                                       seed=2027, rejected=s_rej), rank, world)
         splan, _, _ = tune_batch(reqs)
         with Server(max_slots=256, chunk=args.serve_chunk, clusters=splan) as srv:
             if dist:
@@ -449,7 +876,11 @@ def gpu_bench(args, rank, world, dist):
             rep = dict(rep, requests=len(lat), moves=int(moves), wall_s=wall, moves_per_s=moves / wall,
                        p50_s=float(np.percentile(lat, 50)), p99_s=float(np.percentile(lat, 99)))
         served = dict(rep, lam_per_s=args.lam * world, unit="moves/s", value=rep["moves_per_s"], clusters=splan,
-                      elastic=True)
+                      elastic=True,
+                      outside_domain=dict(count=len(s_rej), cells=sorted({(c["q"], c["n"], c["R"], c["M"])
+                                                                           for c in s_rej}),
+                                          note="requests with M > 65535: outside the reference engine's domain "
+                                               "and this engine's; redrawn, no CPU baseline / parity unpinned"))
 
     # ---------------- quotient search (symsearch) on the big cell K_8(9,4)@940
     quotient = None
@@ -491,7 +922,12 @@ def gpu_bench(args, rank, world, dist):
                         batch=dict(value=bmoves_all / dt_max, instances=len(seeds) * world,
                                    cluster=args.sym_cluster, moves=args.sym_batch_moves))
 
+    comparators = None
+    if rank == 0 and not args.no_comparators:
+        comparators = gpu_comparators(args, dev)
+
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
+                comparators=comparators,
                 plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work, hetero=hetero,
                 served=served, plain_cfgs=plain_cfgs, quotient=quotient)
 
@@ -508,8 +944,11 @@ def main():
     ap.add_argument("--plain-cluster", type=int, default=16)
     ap.add_argument("--plain-moves", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-moves", type=int, default=12)
-    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--ref-moves", type=int, default=100,
+                    help="moves per reference-engine process per step (CPU baselines and the reference arm)")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cell-cpu-moves", type=int, default=200,
+                    help="moves per shape of the uneven-cells / served CPU baselines")
     ap.add_argument("--no-graph", dest="graph", action="store_false",
                     help="launch each step directly instead of replaying its captured CUDA graph")
     ap.add_argument("--no-cpu", action="store_true")
@@ -526,6 +965,9 @@ def main():
     ap.add_argument("--lam", type=float, default=100.0, help="request arrival rate per GPU (1/s)")
     ap.add_argument("--serve-chunk", type=int, default=256)
     ap.add_argument("--no-sym", action="store_true", help="skip the quotient-search leg")
+    ap.add_argument("--no-comparators", action="store_true",
+                    help="skip timing the reference's own GPU kernels beside this engine")
+    ap.add_argument("--comp-chains", type=int, default=256, help="chains per comparator cell")
     ap.add_argument("--sym-moves", type=int, default=300)
     ap.add_argument("--sym-batch", type=int, default=38, help="quotient-search instances per GPU")
     ap.add_argument("--sym-cluster", type=int, default=4)
@@ -540,14 +982,19 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        r = cpu_measure(args.warmup, args.steps, args.cpu_moves)
+        r = ref_measure(args.warmup, args.steps, args.ref_moves)
+        if r is None:
+            r = cpu_measure(args.warmup, args.steps, args.ref_moves)
+            r["sample"] += "; the reference engine's sources are not on this host, so this is the oracle port"
+        _, _, at = warm_state()
         line = dict(metric=METRIC, value=r["value"], unit="moves/s", n_gpus=args.gpus, steps=args.steps,
                     warmup=args.warmup, ms_per_step=1e3 * r["seconds"] / args.steps, higher_is_better=True,
                     scaling="weak", vs_baseline=None, dtype="int64", data="synthetic: uniform random codes, seeded",
                     impl="reference",
                     config=dict(workload=workload_name(args.restarts, args.moves), q=Q, n=N_, R=R_, M=M_,
-                                tenure=TENURE, cpu_sample=r["sample"]),
-                    cpu_baseline=dict(value=r["value"], unit="moves/s", cores=r["cores"], kind="port",
+                                tenure=TENURE, window="moves %d.. of each restart (its code after %d moves)"
+                                                      % (at + 1, at), cpu_sample=r["sample"]),
+                    cpu_baseline=dict(value=r["value"], unit="moves/s", cores=r["cores"], kind=r["kind"],
                                       sample=r["sample"]),
                     e2e=dict(value=r["value"], unit="moves/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
         print(json.dumps(line))
@@ -555,10 +1002,19 @@ def main():
 
     cpu = None
     sym_cpu = None
+    cells_cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_measure(1, args.cpu_steps, args.cpu_moves)   # before any GPU call
+        # before any GPU call: the reference engine and the oracle port on
+        # this host's cores, both from the restarts' codes at the start of
+        # the timed window
+        cpu = ref_measure(1, args.cpu_steps, args.ref_moves)
+        port = cpu_measure(1, args.cpu_steps, args.ref_moves)
+        if cpu is None:
+            cpu = port
+        cpu["port"] = dict(value=port["value"], cores=port["cores"], sample=port["sample"])
         if not args.no_sym:
             sym_cpu = sym_cpu_measure(4)
+        cells_cpu = cells_cpu_measure(args, world)
 
     import torch
     torch.cuda.set_device(local)
@@ -606,13 +1062,19 @@ def main():
             if r["served"] and r["plain"] else None,
             coverage=r["cov"],
             quotient=r["quotient"],
+            gpu_comparators=r["comparators"],
             finished_restarts=r["finished"],
         )
         if r["quotient"] and sym_cpu:
             line["quotient"]["cpu_baseline"] = sym_cpu
+        if cells_cpu:
+            if line["hetero"] and "hetero" in cells_cpu:
+                line["hetero"]["cpu_baseline"] = cells_cpu["hetero"]
+            if line["served"] and "served" in cells_cpu:
+                line["served"]["cpu_baseline"] = cells_cpu["served"]
         if cpu:
-            line["cpu_baseline"] = dict(value=cpu["value"], unit="moves/s", cores=cpu["cores"], kind="port",
-                                        sample=cpu["sample"])
+            line["cpu_baseline"] = dict(value=cpu["value"], unit="moves/s", cores=cpu["cores"], kind=cpu["kind"],
+                                        sample=cpu["sample"], port=cpu.get("port"))
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

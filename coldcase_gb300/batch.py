@@ -29,7 +29,18 @@ from .engine import Pool
 from .workloads import uniform_code
 
 CLUSTERS = (1, 2, 4, 8, 16)
-RESIDENT_CTAS = 152          # one engine CTA per SM (its shared memory fills an SM)
+
+
+def resident_ctas():
+    """Engine CTAs resident at once: one per SM (an engine CTA's shared
+    memory fills an SM), so the current device's SM count."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return int(torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count)
+    except Exception:
+        pass
+    return 152      # GB300 (planning only; nothing runs without a device)
 
 
 def size_class(q, n, R, M):
@@ -120,9 +131,11 @@ class Tuner:
         return lat
 
     @staticmethod
-    def plan(classes, budget, resident=RESIDENT_CTAS):
+    def plan(classes, budget, resident=None):
         """classes: {key: (count, {cluster: seconds per move})}; budget: moves
         per instance.  Returns ({key: cluster}, estimated seconds)."""
+        if resident is None:
+            resident = resident_ctas()
         choice = {k: min(lat) for k, (cnt, lat) in classes.items()}
 
         def estimate(ch):
@@ -145,10 +158,12 @@ class Tuner:
         return choice, best
 
 
-def elastic_clusters(base, work, ctas=RESIDENT_CTAS):
+def elastic_clusters(base, work, ctas=None):
     """Cluster size per instance: its base size, doubled round by round for
     the instances with the most work per move while the total stays within
-    `ctas` resident CTAs (at most 16 per instance)."""
+    `ctas` resident CTAs (default: one per SM; at most 16 per instance)."""
+    if ctas is None:
+        ctas = resident_ctas()
     want = dict(base)
     used = sum(want.values())
     order = sorted(want, key=lambda s: -work[s])

@@ -9,10 +9,14 @@
 // candidate cap) with search seed seed * 1000003 + chain * 7919 (the
 // per-chain seed convention of cov/engine/covengine:557) and stops after
 // `iters` moves or when it covers.  `threads` (the reference's CTA size)
-// is accepted and not used: the pool sizes its own clusters.
+// is accepted and not used: the pool sizes its own clusters -- the widest
+// power of two (at most 16) with which every chain's cluster is resident at
+// once, one CTA per chain when there are more chains than SMs, and one CTA
+// for cells too small to share.
 #include <cstdio>
 #include <vector>
 #include <algorithm>
+#include "cov_common.cuh"
 #include "../../include/covgpu.h"
 
 #define CHAIN_ROW 16            // digits per code row, as chainsolve.cu's MAXN
@@ -27,7 +31,9 @@ extern "C" int cov_chain_run(int q, int n, int R, int M, int nchains, long long 
         return COV_EINVAL;
     long long N = 1;
     for (int j = 0; j < n; j++) N *= q;
-    const int cluster = N >= (1LL << 22) ? 4 : N >= (1LL << 16) ? 2 : 1;
+    int cluster = 1;
+    const int sms = std::max(1, cov_sm_count());
+    while (N >= (1LL << 16) && cluster < 16 && (long long)nchains * cluster * 2 <= sms) cluster *= 2;
     cov_pool *pool = nullptr;
     int rc = cov_pool_create(nchains, cluster, &pool);
     if (rc) return rc;

@@ -209,6 +209,38 @@ __device__ __forceinline__ void cov_item_word(const CovSlot &d, const CovItem &i
     pk = cov_setnib(it.pk, it.last, val);
 }
 
+// ------------------------------------------------------ per device, host --
+// Host-side facts that belong to one device: its SM count, and whether a
+// kernel's attributes (the dynamic shared-memory opt-in, which
+// cudaFuncSetAttribute sets for the current device only) were set on it.
+#define COV_MAX_DEVICES 64
+
+// SM count of the current device, cached per device (0 on error)
+static inline int cov_sm_count()
+{
+    static int cache[COV_MAX_DEVICES];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 0;
+    if (dev < COV_MAX_DEVICES && cache[dev]) return cache[dev];
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (dev < COV_MAX_DEVICES) cache[dev] = v;
+    return v;
+}
+
+// One bit per device: set once a set-up step ran with that device current.
+struct CovDeviceFlags {
+    unsigned long long bits = 0;
+    // true when the current device's bit is set; dev receives the device
+    bool done(int &dev) const
+    {
+        dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= COV_MAX_DEVICES) return false;
+        return (bits >> dev) & 1ull;
+    }
+    void set(int dev) { if (dev >= 0 && dev < COV_MAX_DEVICES) bits |= 1ull << dev; }
+};
+
 // L2-coherent global accessors: data written by other CTAs of the same
 // launch is read with ld.global.cg so that no stale L1 line is observed.
 template <class T>

@@ -2589,17 +2589,18 @@ struct cov_pool {
     cudaStream_t cur_stream() const { return use_ext ? ext : stream; }
 };
 
-static int g_attr_done = 0;
+static CovDeviceFlags g_attr_done;   // kernel attributes set, per device
 
 static int ensure_attrs()
 {
-    if (g_attr_done) return 0;
+    int dev = 0;
+    if (g_attr_done.done(dev)) return 0;
     CK(cudaFuncSetAttribute(cov_run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
     CK(cudaFuncSetAttribute(cov_run_kernel<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     CK(cudaFuncSetAttribute(cov_run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
     CK(cudaFuncSetAttribute(cov_run_kernel<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     CK(cudaFuncSetAttribute(k_build_state, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem_bytes(BT_MAX)));
-    g_attr_done = 1;
+    g_attr_done.set(dev);
     return 0;
 }
 
@@ -2998,7 +2999,7 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
         pk[i] = v;
     }
     int have = std::min(m, M);
-    const int grid = 152 * 8;
+    const int grid = std::max(1, cov_sm_count()) * 8;
     if (m > M) {
         // remove-and-repair descent (covsearch2e.c:1163-1192): cnt of all m
         // words, then repeatedly drop the first word with the fewest
@@ -3371,7 +3372,7 @@ int cov_pool_get_cnt(cov_pool *pool, int32_t slot, uint16_t *out)
     const CovSlot &d = pool->slots[slot].d;
     uint16_t *tmp = nullptr;
     CK(cudaMallocAsync(&tmp, (size_t)d.N * 2, pool->cur_stream()));
-    k_unpack_cnt<<<152 * 4, 256, 0, pool->cur_stream()>>>(d.cw, d.N, tmp);
+    k_unpack_cnt<<<std::max(1, cov_sm_count()) * 4, 256, 0, pool->cur_stream()>>>(d.cw, d.N, tmp);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, tmp, (size_t)d.N * 2, cudaMemcpyDeviceToHost, pool->cur_stream()));
     CK(cudaFreeAsync(tmp, pool->cur_stream()));

@@ -253,7 +253,10 @@ __global__ void k_lns_zero(const uint16_t *cnt, uint32_t N, int target, unsigned
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
-int grid_of(uint32_t N) { return (int)std::min<uint32_t>((N + LNS_NT - 1) / LNS_NT, 152u * 8); }
+int grid_of(uint32_t N)
+{
+    return (int)std::min<uint32_t>((N + LNS_NT - 1) / LNS_NT, (uint32_t)std::max(1, cov_sm_count()) * 8);
+}
 
 // the n axis passes over the layers; the last writes out or cnt16
 int lns_passes(cov_lns *h, int32_t *out, uint16_t *cnt16)

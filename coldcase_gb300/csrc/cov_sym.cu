@@ -1218,15 +1218,16 @@ struct SymHost {
     int cluster = 1;
 };
 
-int g_sym_attr = 0;
+CovDeviceFlags g_sym_attr;   // kernel attributes set, per device
 
 int sym_attrs()
 {
-    if (g_sym_attr) return 0;
+    int dev = 0;
+    if (g_sym_attr.done(dev)) return 0;
     SCK(cudaFuncSetAttribute(sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SymSmem)));
     SCK(cudaFuncSetAttribute(sym_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     SCK(cudaFuncSetAttribute(sym_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SymSmem)));
-    g_sym_attr = 1;
+    g_sym_attr.set(dev);
     return 0;
 }
 

@@ -417,17 +417,28 @@ int geom(int q, int n, DtGeom &g)
     return 0;
 }
 
-int g_dt_attr = 0;
-int g_ct_attr = 0;
+CovDeviceFlags g_dt_attr;   // shared-memory opt-in of the transform kernels, per device
+CovDeviceFlags g_ct_attr;   // the same for the tile count
+
+int ct_attrs()
+{
+    int dev = 0;
+    if (g_ct_attr.done(dev)) return 0;
+    CK(cudaFuncSetAttribute(k_count_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)bt_smem_bytes(BT_MAX)));
+    g_ct_attr.set(dev);
+    return 0;
+}
 
 // the transform on device buffers; hist (device, n+2 entries) may be null
 int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned long long *d_hist,
            uint32_t *d_bm, cudaStream_t st)
 {
-    if (!g_dt_attr) {
+    int dev = 0;
+    if (!g_dt_attr.done(dev)) {
         CK(cudaFuncSetAttribute(k_dt_low, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_TILE_MAX));
         CK(cudaFuncSetAttribute(k_dt_high, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_STRIP_MAX));
-        g_dt_attr = 1;
+        g_dt_attr.set(dev);
     }
     CK(cudaMemsetAsync(d_bm, 0, (size_t)((g.N + 31) / 32) * 4, st));
     if (M > 0) {
@@ -439,7 +450,7 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
     auto low_bytes = [&](int kk) { return (long long)g.pw[kk] / g.q * q4; };
     int k = 1;
     while (k < g.n && low_bytes(k + 1) <= DT_TILE_MAX) k++;
-    const int sms = 152;
+    const int sms = std::max(1, cov_sm_count());
     const uint32_t ntile = g.N / g.pw[k];
     {
         int grid = (int)std::min<uint32_t>(ntile, (uint32_t)sms * 4);
@@ -488,10 +499,9 @@ int cov_mindist_dev(int32_t q, int32_t n, const uint8_t *d_code, int32_t M, uint
 // whose device memory is entirely owned by another allocator (for example a
 // framework's caching allocator that has reserved the whole GPU), or code
 // that runs where an allocation would break the surrounding contract (inside
-// an out-of-memory handler, or while another component is capturing the
-// stream).  The one scratch buffer the transform needs -- the bitmap of
-// codeword positions -- lives in a file-scope device array instead of being
-// allocated per call.
+// an out-of-memory handler).  The one scratch buffer the transform needs --
+// the bitmap of codeword positions -- lives in a file-scope device array
+// instead of being allocated per call.
 //
 //  * Limit: q^n <= COV_DT_STATIC_MAX_WORDS (2^26 words, an 8 MiB bitmap that
 //    every GPU which loads the library keeps until the process exits).
@@ -539,7 +549,7 @@ int64_t cov_count_above_dev(int32_t q, int32_t n, const uint8_t *d_dist, int32_t
     unsigned long long *d_c = nullptr, h = 0;
     CK(cudaMallocAsync(&d_c, 8, st));
     CK(cudaMemsetAsync(d_c, 0, 8, st));
-    k_count_above<<<152 * 8, 256, 0, st>>>(d_dist, g.N, R, d_c);
+    k_count_above<<<std::max(1, cov_sm_count()) * 8, 256, 0, st>>>(d_dist, g.N, R, d_c);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&h, d_c, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaFreeAsync(d_c, st));
@@ -609,11 +619,8 @@ int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code, int32_
     if (R < 0 || M < 0 || M > 65535 || (M > 0 && !d_code) || !d_cnt) return COV_EINVAL;
     if (R > n) R = n;
     cudaStream_t st = (cudaStream_t)stream;
-    if (!g_ct_attr) {
-        CK(cudaFuncSetAttribute(k_count_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)bt_smem_bytes(BT_MAX)));
-        g_ct_attr = 1;
-    }
+    rc = ct_attrs();
+    if (rc) return rc;
     CountGeom g;
     memset(&g, 0, sizeof g);
     g.q = q; g.n = n; g.R = R; g.M = M;
@@ -687,11 +694,8 @@ int cov_finish(int32_t q, int32_t n, int32_t R, int32_t M, const uint8_t *code, 
         return COV_OK;
     }
     if (dg.N > 1200000000u) return COV_ERANGE;                        // covcount's limit without --fast
-    if (!g_ct_attr) {
-        CK(cudaFuncSetAttribute(k_count_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)bt_smem_bytes(BT_MAX)));
-        g_ct_attr = 1;
-    }
+    rc = ct_attrs();
+    if (rc) return rc;
     // tile count of the deduplicated words
     CountGeom g;
     memset(&g, 0, sizeof g);
@@ -740,7 +744,7 @@ int cov_finish(int32_t q, int32_t n, int32_t R, int32_t M, const uint8_t *code, 
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
-        k_count_zero16<<<152 * 4, 256>>>(d_cnt, dg.N, d_z);
+        k_count_zero16<<<std::max(1, cov_sm_count()) * 4, 256>>>(d_cnt, dg.N, d_z);
         e = cudaGetLastError();
     }
     std::vector<uint64_t> v((size_t)M);

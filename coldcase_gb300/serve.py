@@ -31,7 +31,7 @@ import time
 import numpy as np
 
 from . import verify
-from .batch import RESIDENT_CTAS, elastic_clusters, size_class
+from .batch import elastic_clusters, resident_ctas, size_class
 from .engine import Pool, device_memory, slot_bytes
 from .workloads import uniform_code
 
@@ -54,7 +54,7 @@ def _work_per_move(r):
 
 class Server:
     def __init__(self, max_slots=256, chunk=256, reserve_bytes=8 << 30, budget_bytes=None, clusters=None,
-                 verify_results=True, budget_s=120.0, elastic=True, ctas=RESIDENT_CTAS):
+                 verify_results=True, budget_s=120.0, elastic=True, ctas=None):
         self.pool = Pool(max_slots, cluster=1, budget_s=budget_s)
         self.max_slots = max_slots
         self.chunk = chunk
@@ -69,7 +69,7 @@ class Server:
         self.moves = 0
         self.steps = 0
         self.elastic = elastic
-        self.ctas = ctas
+        self.ctas = resident_ctas() if ctas is None else ctas
 
     def _cluster(self, r):
         if isinstance(self.clusters, dict):

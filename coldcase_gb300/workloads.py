@@ -28,10 +28,12 @@ BATCHED = dict(name="batched 64x q7 n9 R4 M1500 tenure20", q=7, n=9, R=4, M=1500
                moves=10 ** 5, restarts=64)
 
 
-def hetero_cells(count=256, seed=2026, max_words=43_000_000, max_m=65535):
+def hetero_cells(count=256, seed=2026, max_words=43_000_000, max_m=65535, rejected=None):
     """Uneven (q,n,R,M) cells: q in {5..8}, n in {6..9} with q^n <= 4.3e7,
-    R in {1..4}, M = ceil(1.3 q^n / |B(n,R)|).  Cells whose M exceeds the
-    reference engine's 65535 limit (covsearch2e.c:1117) are redrawn."""
+    R in {1..4}, M = ceil(1.3 q^n / |B(n,R)|).  Cells whose M exceeds 65535
+    lie outside the reference engine's domain (covsearch2e.c:1117) and this
+    engine's (16-bit coverer ids): they are redrawn, and each one drawn is
+    appended to `rejected` when a list is given."""
     rng = np.random.default_rng(seed)
     out = []
     while len(out) < count:
@@ -42,16 +44,20 @@ def hetero_cells(count=256, seed=2026, max_words=43_000_000, max_m=65535):
             continue
         M = math.ceil(1.3 * q ** n / ball_volume(q, n, R))
         if M > max_m:
+            if rejected is not None:
+                rejected.append(dict(q=q, n=n, R=R, M=M))
             continue
         out.append(dict(q=q, n=n, R=R, M=M, seed=instance_seed(seed, len(out))))
     return out
 
 
-def serve_requests(count=200, lam=100.0, seed=2027, max_words=60_500_000, max_m=65535):
+def serve_requests(count=200, lam=100.0, seed=2027, max_words=60_500_000, max_m=65535, rejected=None):
     """Open-loop Poisson stream of solve requests: q in {5,6,7}, n in
-    {6..10} with q^n <= 6.05e7, R in {1..4}, M = ceil(1.3 q^n / |B(n,R)|)
-    (redrawn above 65535), move budget log-uniform in [1e3, 1e5], arrivals
-    with exponential gaps of mean 1/lam seconds."""
+    {6..10} with q^n <= 6.05e7, R in {1..4}, M = ceil(1.3 q^n / |B(n,R)|),
+    move budget log-uniform in [1e3, 1e5], arrivals with exponential gaps of
+    mean 1/lam seconds.  Requests with M above 65535 (outside the reference
+    engine's domain and this engine's) are redrawn and, when a list is
+    given, appended to `rejected`."""
     rng = np.random.default_rng(seed)
     out = []
     t = 0.0
@@ -63,6 +69,8 @@ def serve_requests(count=200, lam=100.0, seed=2027, max_words=60_500_000, max_m=
             continue
         M = math.ceil(1.3 * q ** n / ball_volume(q, n, R))
         if M > max_m:
+            if rejected is not None:
+                rejected.append(dict(q=q, n=n, R=R, M=M))
             continue
         moves = int(round(10 ** rng.uniform(3, 5)))
         t += float(rng.exponential(1.0 / lam))

@@ -34,7 +34,8 @@ Runs in the build container only (it needs the reference checkout):
                           answer cases of cov/test_verify.py (whole space,
                           single word, perfect Hamming codes, direct sums).
 
-Usage: python3 tests/golden/make_golden.py [--ref /root/reference]
+Usage: python3 tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT]
+(default: $COLDCASE_REF, else /root/reference)
 """
 import argparse
 import contextlib
@@ -313,7 +314,7 @@ def sym_runs(binary):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("COLDCASE_REF", "/root/reference"))
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=%s" % a.ref], check=True)
     binary = os.path.join(REPO, "oracle", "_ref", "covsearch2e")
