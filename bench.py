@@ -97,9 +97,11 @@ def ref_processes(exe, jobs, tlimit=600.0):
     """Run one reference process per job concurrently (single-threaded, as
     covengine runs its chains): job = (q, n, R, M, code file, seed, tabu,
     iters).  Returns [(iters, seconds after init, wall seconds)], from each
-    process's own RESULT line (covsearch2e.c:1582-1589)."""
+    process's own RESULT line (covsearch2e.c:1582-1589); the seconds are its
+    CPU seconds (printed to the millisecond) when its wall time after init,
+    printed to 10 ms, is too short to be precise."""
     import re
-    rx = re.compile(r"RESULT .* iters=(\d+) .*time=([0-9.]+) ")
+    rx = re.compile(r"RESULT .* iters=(\d+) .*time=([0-9.]+) rate=\S+ cpu=([0-9.]+) ")
     procs = []
     for (q, n, R, M, path, seed, tabu, iters) in jobs:
         cmd = [exe, "-q", str(q), "-n", str(n), "-R", str(R), "-M", str(M), "--preset", "p5b", "--in", path,
@@ -114,7 +116,8 @@ def ref_processes(exe, jobs, tlimit=600.0):
         m = rx.search(txt or "")
         if not m:
             raise RuntimeError("reference engine printed no RESULT line (rc %s)" % p.returncode)
-        out.append((int(m.group(1)), float(m.group(2)), wall))
+        t, cpu = float(m.group(2)), float(m.group(3))
+        out.append((int(m.group(1)), t if t >= 0.5 else max(t, cpu), wall))
     return out
 
 
@@ -214,22 +217,27 @@ def ref_cells_measure(cells, moves, tlimit=600.0, cores=None, min_s=0.3):
                 part = pending[b:b + cores]
                 jobs = [(q, n, R, M, files[(q, n, R, M)], 4242, 0, iters[(q, n, R, M)]) for (q, n, R, M) in part]
                 for sh, (it, t, wall) in zip(part, ref_processes(exe, jobs, tlimit)):
-                    rate[sh] = (it / t if t > 0 and it > 0 else None, max(0.0, wall - t))
+                    # a run that stops short of its moves has covered: the cell's
+                    # search would stop there too
+                    rate[sh] = (it / t if t > 0 and it > 0 else None, max(0.0, wall - t),
+                                it if it < iters[sh] else None)
                     if t < min_s and it >= iters[sh]:
                         iters[sh] *= 10
                         again.append(sh)
             pending = again
-    per_cell = []
+    per_cell, total_moves = [], 0
     for c in cells:
-        r, init = rate[(c["q"], c["n"], c["R"], c["M"])]
-        per_cell.append(init + (c["moves"] / r if r else 0.0))
-    total_moves = sum(c["moves"] for c in cells)
+        r, init, cover = rate[(c["q"], c["n"], c["R"], c["M"])]
+        mv = c["moves"] if cover is None else min(c["moves"], cover)
+        per_cell.append(init + (mv / r if r else 0.0))
+        total_moves += mv
     cpu_s = sum(per_cell) / cores
     return dict(value=total_moves / cpu_s, unit="moves/s", cores=cores, kind="reference", per_cell_s=per_cell,
                 shapes=len(shapes),
                 sample="each of %d distinct (q,n,R,M) shapes on covsearch2e --preset p5b from a uniform code, "
                        ">= %d moves (more until >= %.1f s after init); every cell costs init + its move budget "
-                       "at its shape's rate on one core, %d cores shared perfectly"
+                       "(or the moves its shape's sample needed to cover) at its shape's rate on one core, %d "
+                       "cores shared perfectly"
                        % (len(shapes), moves, min_s, cores))
 
 
@@ -476,12 +484,13 @@ def coverage_bench(args, code79, dev):
     try:
         from oracle import pyoracle as po
         cores = host_cores()
-        po.mindist(code79[:4], Q, N_, threads=cores)     # warm the library
+        po.linemin(code79[:4], Q, N_, threads=cores)     # warm the library
         t0 = time.perf_counter()
-        d_cpu = po.mindist(code79, Q, N_, threads=cores)
+        d_cpu = po.linemin(code79, Q, N_, threads=cores)
         t1 = time.perf_counter()
         cpu["line_min_port"] = dict(value=Q ** N_ / (t1 - t0), unit="words/s", seconds=t1 - t0, cores=cores,
-                                    kind="port", sample="the whole 7^9 transform, oracle/dtoracle.c")
+                                    kind="port", sample="the whole 7^9 transform: n uint8 axis line-min passes "
+                                                        "(oracle/dtoracle.c orc_linemin), OpenMP over lines")
         if int((d_cpu > R_).sum()) != out["q7n9"]["uncovered"]:
             raise RuntimeError("CPU and GPU transforms disagree")
     except (OSError, ImportError) as e:

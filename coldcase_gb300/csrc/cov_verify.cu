@@ -24,7 +24,7 @@
 
 #define DT_TILE_MAX   65536    // bytes of the contiguous low-axes tile
 #define DT_STRIP_MAX  98304    // bytes of a high-axes strip
-#define DT_STRIP_W    32       // columns of a strip
+#define DT_STRIP_W    32       // narrowest strip (columns); strips widen while they fit
 #define DT_NT         512
 
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
@@ -120,15 +120,30 @@ k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__
             dt_pass4(dt_w, rows / q * wpr, q, inner, inner, inf4);
             __syncthreads();
         }
-        // out by rows: a thread writes the q words of its row
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const uint8_t *src = dt_b + r * (wpr * 4);
-            uint8_t *dst = D + x0 + (uint32_t)r * (uint32_t)q;
-            for (int a = 0; a < q; a++) {
-                const uint8_t v = src[a];
-                dst[a] = v;
-                if (last) dt_hist_add(sh, v);
+        // out: the tile is T contiguous bytes of D; the 4-byte-aligned
+        // interior goes out as whole words (byte b of the tile is row b / q,
+        // column b % q of the padded rows), the unaligned ends as bytes
+        const uint32_t head = min((4u - (uint32_t)(reinterpret_cast<uintptr_t>(D + x0) & 3u)) & 3u, T);
+        const uint32_t nw = (T - head) >> 2;
+        const int rb = wpr * 4;                   // padded row bytes
+        for (uint32_t e = threadIdx.x; e < head + ((T - head) & 3u); e += blockDim.x) {
+            const uint32_t b = e < head ? e : head + 4 * nw + (e - head);
+            const uint32_t r = b / (uint32_t)q;
+            const uint8_t v = dt_b[r * rb + (b - r * (uint32_t)q)];
+            D[x0 + b] = v;
+            if (last) dt_hist_add(sh, v);
+        }
+        for (uint32_t wi = threadIdx.x; wi < nw; wi += blockDim.x) {
+            const uint32_t b0 = head + 4 * wi;
+            uint32_t r = b0 / (uint32_t)q, a = b0 - r * (uint32_t)q, v = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const uint32_t byte = dt_b[r * rb + a];
+                v |= byte << (8 * k);
+                if (last) dt_hist_add(sh, (int)byte);
+                if (++a == (uint32_t)q) { a = 0; r++; }
             }
+            *reinterpret_cast<uint32_t *>(D + x0 + b0) = v;
         }
     }
     __syncthreads();
@@ -137,40 +152,44 @@ k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__
 }
 
 // Pass 2+: the axes of group [j0, j0+gsz) (in-word strides q^j0 .. ), for a
-// strip of up to DT_STRIP_W consecutive positions below the group: rows of
-// DT_STRIP_W bytes, DT_STRIP_W/4 words, so each pass moves whole words.
+// strip of W = 32 << lw consecutive positions below the group: rows of W
+// bytes, W/4 words, so each pass moves whole words.  W is as wide as the
+// shared memory allows for the group's q^gsz rows, so that a group of few
+// rows (the last axes of a long word) still moves long contiguous runs.
 __global__ void __launch_bounds__(DT_NT)
-k_dt_high(DtGeom g, int j0, int gsz, int last_, uint8_t *__restrict__ D, unsigned long long *hist)
+k_dt_high(DtGeom g, int j0, int gsz, int lw, int last_, uint8_t *__restrict__ D, unsigned long long *hist)
 {
     const bool last = last_ && hist != nullptr;
     extern __shared__ __align__(16) uint32_t dt_w[];
     __shared__ int sh[COV_MAXN + 2];
-    constexpr int WW = DT_STRIP_W / 4;           // words per row
+    const int lwb = lw + 5;                      // log2 of the strip width in bytes
+    const uint32_t W = 1u << lwb;
+    const int WW = (int)(W >> 2);                // words per row
     uint8_t *dt_b = reinterpret_cast<uint8_t *>(dt_w);
     const uint32_t inf4 = (uint32_t)g.inf * 0x01010101u;
     const uint32_t s = g.pw[j0];                 // stride of the lowest axis in the group
     const uint32_t rows = g.pw[gsz];
     const uint32_t span = rows * s;              // words spanned by one value of the outer digits
     const uint32_t outer = g.N / span;
-    const uint32_t nstrip = (s + DT_STRIP_W - 1) / DT_STRIP_W;
+    const uint32_t nstrip = (s + W - 1) >> lwb;
     const unsigned long long ntiles = (unsigned long long)outer * nstrip;
     if (threadIdx.x < COV_MAXN + 2) sh[threadIdx.x] = 0;
     for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint32_t o = (uint32_t)(tile / nstrip);
-        const uint32_t c0 = (uint32_t)(tile - (unsigned long long)o * nstrip) * DT_STRIP_W;
-        const int w = (int)min((uint32_t)DT_STRIP_W, s - c0);
+        const uint32_t c0 = (uint32_t)(tile - (unsigned long long)o * nstrip) << lwb;
+        const uint32_t w = min(W, s - c0);
         const uint32_t base = o * span + c0;
         __syncthreads();
         // element (row r, column c) at base + r*s + c, kept at byte r*W + c;
         // eight loads of a thread in flight before their stores
-        const uint32_t tot = rows * DT_STRIP_W;
+        const uint32_t tot = rows << lwb;
         for (uint32_t e0 = threadIdx.x; e0 < tot; e0 += 8 * blockDim.x) {
             uint8_t v[8];
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const uint32_t e = e0 + (uint32_t)u * blockDim.x;
-                const uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
-                v[u] = (e < tot && c < (uint32_t)w) ? D[base + r * s + c] : (uint8_t)g.inf;
+                const uint32_t r = e >> lwb, c = e & (W - 1);
+                v[u] = (e < tot && c < w) ? D[base + r * s + c] : (uint8_t)g.inf;
             }
 #pragma unroll
             for (int u = 0; u < 8; u++) {
@@ -184,9 +203,9 @@ k_dt_high(DtGeom g, int j0, int gsz, int last_, uint8_t *__restrict__ D, unsigne
             dt_pass4(dt_w, (int)(rows / (uint32_t)g.q) * WW, g.q, inner, inner, inf4);
             __syncthreads();
         }
-        for (uint32_t e = threadIdx.x; e < rows * DT_STRIP_W; e += blockDim.x) {
-            uint32_t r = e / DT_STRIP_W, c = e - r * DT_STRIP_W;
-            if (c < (uint32_t)w) {
+        for (uint32_t e = threadIdx.x; e < tot; e += blockDim.x) {
+            const uint32_t r = e >> lwb, c = e & (W - 1);
+            if (c < w) {
                 uint8_t v = dt_b[e];
                 D[base + r * s + c] = v;
                 if (last) dt_hist_add(sh, v);
@@ -465,9 +484,16 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
         if (gsz == 0) return COV_EINVAL;
         int last = (j0 + gsz == g.n);
         const uint32_t s = g.pw[j0];
-        const unsigned long long tiles = (unsigned long long)(g.N / (g.pw[gsz] * s)) * ((s + DT_STRIP_W - 1) / DT_STRIP_W);
+        // widest power-of-two strip (>= DT_STRIP_W bytes) the shared memory
+        // holds for these rows, but no wider than the group's stride needs
+        int lw = 0;
+        while ((long long)g.pw[gsz] * (DT_STRIP_W << (lw + 1)) <= DT_STRIP_MAX &&
+               (uint32_t)(DT_STRIP_W << lw) < s)
+            lw++;
+        const uint32_t W = (uint32_t)DT_STRIP_W << lw;
+        const unsigned long long tiles = (unsigned long long)(g.N / (g.pw[gsz] * s)) * ((s + W - 1) / W);
         int grid = (int)std::min<unsigned long long>(tiles, (unsigned long long)sms * 4);
-        k_dt_high<<<grid, DT_NT, (size_t)g.pw[gsz] * DT_STRIP_W, st>>>(g, j0, gsz, last, d_D, d_hist);
+        k_dt_high<<<grid, DT_NT, (size_t)g.pw[gsz] * W, st>>>(g, j0, gsz, lw, last, d_D, d_hist);
         CK(cudaGetLastError());
         j0 += gsz;
     }

@@ -126,6 +126,7 @@ long long orc_verify_pure(int q, int n, int R, const uint8_t *code, int M);
 int orc_mindist(int q, int n, const uint8_t *code, int M, uint8_t *dist,
                 int threads);
 /* run_dilate: 1 iff every word is within R of the code; covered[] optional */
+int orc_linemin(int q, int n, const uint8_t *code, int M, uint8_t *dist, int threads);
 int orc_dilate(int q, int n, int R, const uint8_t *code, int M,
                uint8_t *covered);
 

@@ -86,6 +86,8 @@ def load():
     lib.orc_verify_pure.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int]
     lib.orc_mindist.restype = ctypes.c_int
     lib.orc_mindist.argtypes = [ctypes.c_int, ctypes.c_int, u8p, ctypes.c_int, u8p, ctypes.c_int]
+    lib.orc_linemin.restype = ctypes.c_int
+    lib.orc_linemin.argtypes = [ctypes.c_int, ctypes.c_int, u8p, ctypes.c_int, u8p, ctypes.c_int]
     lib.orc_dilate.restype = ctypes.c_int
     lib.orc_dilate.argtypes = [ctypes.c_int] * 3 + [u8p, ctypes.c_int, u8p]
     _lib = lib
@@ -208,6 +210,15 @@ def mindist(code, q, n, threads=1):
     a = np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, n))
     out = np.zeros(q ** n, dtype=np.uint8)
     lib.orc_mindist(q, n, _u8(a) if a.size else None, a.shape[0], _u8(out), threads)
+    return out
+
+
+def linemin(code, q, n, threads=1):
+    """Per-word minimum distance by n axis line-min passes (orc_linemin)."""
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(code, dtype=np.uint8).reshape(-1, n))
+    out = np.zeros(q ** n, dtype=np.uint8)
+    lib.orc_linemin(q, n, _u8(a) if a.size else None, a.shape[0], _u8(out), threads)
     return out
 
 

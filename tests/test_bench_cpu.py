@@ -33,8 +33,8 @@ def test_cell_baseline_model():
     if not bench.ref_exe():
         import pytest
         pytest.skip("no copy of the reference engine on this host")
-    cells = [dict(q=4, n=6, R=1, M=420, moves=1000), dict(q=5, n=6, R=2, M=90, moves=500),
-             dict(q=4, n=6, R=1, M=420, moves=3000)]
+    cells = [dict(q=6, n=6, R=2, M=20, moves=100), dict(q=5, n=6, R=2, M=90, moves=500),
+             dict(q=6, n=6, R=2, M=20, moves=300)]
     r = bench.ref_cells_measure(cells, 20, cores=2)
     assert r["shapes"] == 2 and r["value"] > 0 and len(r["per_cell_s"]) == 3
     # the same shape costs in proportion to its budget (plus the same init)

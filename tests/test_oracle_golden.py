@@ -55,6 +55,9 @@ def test_verify_cases(golden):
             hist = np.bincount(d, minlength=n + 2)[: n + 2]
             assert hist.tolist() == c["hist"], c["src"]
             assert int(d.max()) == c["radius"]
+            # the line-min form (the CPU baseline of the transform) gives the
+            # same per-word distances as the direct minimum
+            assert (po.linemin(code, q, n, threads=4) == d).all(), c["src"]
             ok, cov = po.dilate(code, q, n, R)
             assert ok == c["covers"] and int((~cov).sum()) == c["uncovered"]
             cnt = po.cover_count(code, q, n, R)
