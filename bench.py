@@ -656,6 +656,44 @@ def gpu_comparators(args, dev):
     return out
 
 
+LNS_CELLS = ((7, 9, 4, 1500, 30), (8, 9, 4, 2944, 10))   # (q, n, R, M, rounds)
+
+
+def lns_bench(args):
+    """The transform-engine search (coldcase_gb300.lns) on the big cells:
+    a greedy fill from no codeword to M, then a fixed number of ruin-and-
+    recreate rounds; rounds/s, placements/s, the uncovered count, and the
+    best code checked by the GPU verifier (cov_verify)."""
+    import numpy as np
+    import torch
+    from coldcase_gb300 import verify
+    from coldcase_gb300.lns import LNS
+    out = {}
+    for (q, n, R, M, rounds) in LNS_CELLS:
+        rounds = args.lns_rounds if args.lns_rounds else rounds
+        with LNS(q, n, R, seed=1) as e:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e.load(np.zeros(0, dtype=np.int64))
+            e.recreate(M)
+            t1 = time.perf_counter()
+            fill = dict(e.stats)
+            unc0 = e.uncov
+            e.lns(M, budget_s=300.0, max_rounds=rounds)
+            t2 = time.perf_counter()
+            best = e.eng.index_word(e.best_code if e.best_code is not None else e.code)
+            unc_v, _ = verify.verify(best, n, q, R, want_witness=False)
+            st = e.stats
+            out["q%dn%dR%dM%d" % (q, n, R, M)] = dict(
+                fill_s=t1 - t0, fill_placements=fill["placements"], uncovered_after_fill=unc0,
+                rounds=st["rounds"], rounds_s=st["rounds"] / max(t2 - t1, 1e-9),
+                placements_s=st["placements"] / max(t2 - t0, 1e-9),
+                uncovered=int(e.best_uncov), verifier_uncovered=int(unc_v), verified=int(unc_v) == int(e.best_uncov),
+                accepted=st["accepted"], refreshes=st["refreshes"], exact_counts=st["exact_counts"],
+                seconds=t2 - t0)
+    return out
+
+
 def ctypes_sizeof_status():
     from coldcase_gb300 import lib as L
     import ctypes
@@ -931,12 +969,16 @@ def gpu_bench(args, rank, world, dist):
                         batch=dict(value=bmoves_all / dt_max, instances=len(seeds) * world,
                                    cluster=args.sym_cluster, moves=args.sym_batch_moves))
 
+    lns = None
+    if rank == 0 and not args.no_lns:
+        lns = lns_bench(args)
+
     comparators = None
     if rank == 0 and not args.no_comparators:
         comparators = gpu_comparators(args, dev)
 
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
-                comparators=comparators,
+                comparators=comparators, lns=lns,
                 plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work, hetero=hetero,
                 served=served, plain_cfgs=plain_cfgs, quotient=quotient)
 
@@ -977,6 +1019,8 @@ def main():
     ap.add_argument("--no-comparators", action="store_true",
                     help="skip timing the reference's own GPU kernels beside this engine")
     ap.add_argument("--comp-chains", type=int, default=256, help="chains per comparator cell")
+    ap.add_argument("--no-lns", action="store_true", help="skip the transform-engine search leg")
+    ap.add_argument("--lns-rounds", type=int, default=0, help="ruin-and-recreate rounds per LNS cell (0: default)")
     ap.add_argument("--sym-moves", type=int, default=300)
     ap.add_argument("--sym-batch", type=int, default=38, help="quotient-search instances per GPU")
     ap.add_argument("--sym-cluster", type=int, default=4)
@@ -1072,6 +1116,7 @@ def main():
             coverage=r["cov"],
             quotient=r["quotient"],
             gpu_comparators=r["comparators"],
+            lns=r["lns"],
             finished_restarts=r["finished"],
         )
         if r["quotient"] and sym_cpu:

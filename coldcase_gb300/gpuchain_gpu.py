@@ -5,7 +5,7 @@ Same flags as cov/gemm2/gpuchain.py (:412-457): -q -n -R -M -t -s --out
 (atomically, on improvement, at most once a second, and at the end) and one
 RESULT line reports M, uncovered, rounds, placements+removals per second,
 transforms and time.  A seed file with more than M words is first ruined
-down to M by lowest private coverage.
+down to M by the soft minimum of private coverage (lns.LNS.ruin).
 """
 import argparse
 import sys
@@ -39,7 +39,7 @@ def main(argv=None):
         if a.seed_code:
             e.load(codefile.read_code(a.seed_code, a.n))
             if len(e.code) > a.M:
-                e.ruin(len(e.code) - a.M, "low")
+                e.ruin(len(e.code) - a.M, "soft")
         else:
             e.load(np.zeros(0, dtype=np.int64))
         unc = e.lns(a.M, budget_s=deadline - time.time() - 5, kmin=a.kmin, kmax=a.kmax, max_rounds=a.rounds)

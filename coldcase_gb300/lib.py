@@ -140,6 +140,10 @@ SIGNATURES = {
     "cov_lns_map_read": (ctypes.c_int, [_P, _PU32, _I32, _PI32]),
     "cov_lns_ball": (ctypes.c_int, [_P, _PU32, _I32, _I32, _I32, _PI32]),
     "cov_lns_count": (ctypes.c_int, [_P, _I32, _PI64]),
+    "cov_lns_apply": (ctypes.c_int, [_P, _PU32, _I32, _I32, _PI64]),
+    "cov_lns_peel": (ctypes.c_int, [_P, _PU32, _I32, ctypes.POINTER(ctypes.c_uint8), _PI32, _PI64]),
+    "cov_lns_greedy": (ctypes.c_int, [_P, _I32, _I64, _PU32, _PI32, _PI64, _PI64]),
+    "cov_lns_uncovered": (ctypes.c_int, [_P, _I64, _PU32, _PI64]),
     "cov_lns_get_cnt": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint16)]),
     "cov_lns_get_map": (ctypes.c_int, [_P, _PI32]),
 }

@@ -1,30 +1,34 @@
-"""Transform-engine LNS: ruin-and-recreate over exact full-grid maps.
+"""Transform-engine search: ruin and recreate over exact maps of one cell.
 
-The GPU form of cov/gemm2/gpuchain.py (Engine, :94-410).  One cell is
-resident on the device (cov_lns_* in libcovgpu.so); every decision reads an
-exact map:
+Capability of cov/gemm2/gpuchain.py (its Engine, :94-410): a code of M words
+is improved by removing some codewords and placing new ones greedily, with
+every decision read off exact counts kept on the device (cov_lns_* in
+libcovgpu.so).  The search here is its own design:
 
-  * recreate (greedy_fill, gpuchain.py:193-279): lazy greedy placement.  A
-    gain map gives, for every word at once, how many uncovered words a
-    codeword there would cover.  Gains only fall as codewords are added, so
-    stale gains bound the true ones: candidates are popped best-first in
-    batches, re-evaluated exactly by ball gathers, and the best is placed
-    when it still beats the next bound.  The map is refreshed after a number
-    of placements, or when the bounds run out.
-  * ruin (:281-323): remove k codewords -- the lowest exact private coverage
-    (loss map) with exponential jitter, a random subset, a cluster around a
-    random codeword, or a cluster around a high-gain word (a hole).
-  * peel (:325-364): remove codewords of zero loss (a cover stays a cover),
-    pairwise far apart so that removals do not create private words for
-    each other.
-  * lns (:367-410): at fixed M, rounds of ruin + recreate; a round that
-    ends worse is undone with probability 0.9.
+  * recreate -- cov_lns_greedy: the lazy greedy placement runs on the device
+    (a persistent cluster kernel re-counts the best gain bound exactly until
+    it is current, then places it), so a placement costs no host round trip;
+    the host only asks for it.  Each placed word covers as many uncovered
+    words as any word can (ties to the lower index).
+  * ruin -- k codewords leave, chosen by one of four rules drawn with fixed
+    weights: a soft minimum of their exact losses (Gumbel top-k: codewords
+    that cover few words alone leave first, with randomness set by a
+    temperature), the codewords nearest a random uncovered word, the
+    codewords nearest a random codeword, or a uniform draw.  k follows a
+    truncated geometric law between kmin and kmax (small ruins are common).
+  * acceptance -- late acceptance (LAHC, Burke and Bykov): a round is kept
+    when its uncovered count is no worse than the current one or than the
+    count kept `history` rounds earlier; otherwise it is undone exactly by
+    the opposite balls of the words it placed and removed.
+  * peel -- cov_lns_peel: codewords in a random order leave while each
+    covers no word alone (one exact pass on the device is complete: a
+    removal never lowers another codeword's private count).
 
-Words are MSB-first indices (x = sum_j w_j q^(n-1-j)); extraction returns
-positions in index order, so a run is reproducible from its seed.
+Words are MSB-first indices (x = sum_j w_j q^(n-1-j)); every device result is
+deterministic, and the host draws come from one seeded generator, so a run
+is reproducible from its seed.
 """
 import ctypes
-import heapq
 import os
 import time
 
@@ -44,7 +48,6 @@ class TransformEngine:
         h = ctypes.c_void_p()
         L.check(self.lib.cov_lns_create(q, n, R, ctypes.byref(h)), "cov_lns_create")
         self.h = h
-        self.extract_cap = 1 << 22
 
     def close(self):
         if self.h:
@@ -112,10 +115,49 @@ class TransformEngine:
                     "cov_lns_ball")
         return out.astype(np.int64)
 
-    def ball_update(self, idx, delta):
+    def apply(self, idx, sign):
+        """Add sign (+1/-1) over the ball of each word in turn; returns the
+        uncovered count afterwards."""
         a, p = self._u32(idx)
-        if a.size:
-            L.check(self.lib.cov_lns_ball(self.h, p, int(a.size), 1, int(delta), None), "cov_lns_ball")
+        u = ctypes.c_int64(0)
+        L.check(self.lib.cov_lns_apply(self.h, p if a.size else None, int(a.size), int(sign), ctypes.byref(u)),
+                "cov_lns_apply")
+        return int(u.value)
+
+    def ball_update(self, idx, delta):
+        self.apply(idx, delta)
+
+    def greedy(self, room, cand_cap=1 << 16):
+        """Place up to `room` best words (device lazy greedy); returns
+        (placed indices in order, uncovered, refreshes, exact counts)."""
+        out = np.zeros(max(room, 1), dtype=np.uint32)
+        k = ctypes.c_int32(0)
+        u = ctypes.c_int64(0)
+        st = np.zeros(2, dtype=np.int64)
+        L.check(self.lib.cov_lns_greedy(self.h, int(room), int(cand_cap),
+                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(k),
+                                        ctypes.byref(u), st.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))),
+                "cov_lns_greedy")
+        return out[:k.value].astype(np.int64), int(u.value), int(st[0]), int(st[1])
+
+    def peel(self, order):
+        """Exact peel of the listed codewords in this order; returns (mask of
+        the removed, uncovered)."""
+        a, p = self._u32(order)
+        flags = np.zeros(max(a.size, 1), dtype=np.uint8)
+        k = ctypes.c_int32(0)
+        u = ctypes.c_int64(0)
+        L.check(self.lib.cov_lns_peel(self.h, p if a.size else None, int(a.size),
+                                      flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), ctypes.byref(k),
+                                      ctypes.byref(u)), "cov_lns_peel")
+        return flags[:a.size].astype(bool), int(u.value)
+
+    def uncovered_words(self, cap):
+        idx = np.zeros(max(cap, 1), dtype=np.uint32)
+        found = ctypes.c_int64(0)
+        L.check(self.lib.cov_lns_uncovered(self.h, int(cap), idx.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                           ctypes.byref(found)), "cov_lns_uncovered")
+        return idx[:min(cap, int(found.value))].astype(np.int64), int(found.value)
 
     def count(self, target=0):
         v = ctypes.c_int64(0)
@@ -144,25 +186,30 @@ def write_code_atomic(path, words):
 
 
 class LNS:
-    """Ruin-and-recreate search for one cell; codewords kept as sorted word
-    indices (distinct)."""
+    """Ruin-and-recreate search for one cell; the code is kept as a sorted
+    array of distinct word indices."""
 
-    RUIN_MODES = ("low", "hole", "hole", "cluster", "random")
+    RUIN_RULES = ("soft", "near_uncovered", "cluster", "random")
+    RUIN_WEIGHTS = (0.45, 0.30, 0.15, 0.10)
 
-    def __init__(self, q, n, R, seed=1, out=None, log=None, deadline=None, bound_cap=1 << 14):
+    def __init__(self, q, n, R, seed=1, out=None, log=None, deadline=None, cand_cap=1 << 16, history=16,
+                 temperature=0.25):
         self.q, self.n, self.R = q, n, R
-        self.bound_cap = bound_cap      # most stale bounds kept per refresh of the gain map
-        self.rng = np.random.default_rng(seed * 1000003 + 12345)
+        self.rng = np.random.default_rng([int(seed), q, n, R])
         self.out = out
         self.log = log or (lambda *a: None)
         self.deadline = deadline
+        self.cand_cap = cand_cap
+        self.history = history
+        self.temperature = temperature
         self.eng = TransformEngine(q, n, R)
         self.code = np.zeros(0, dtype=np.int64)
         self.uncov = None
         self.best_code = None
         self.best_uncov = None
         self._last_pub = 0.0
-        self.stats = dict(transforms=0, placements=0, removals=0, rounds=0, recounts=0)
+        self.stats = dict(transforms=0, placements=0, removals=0, rounds=0, recounts=0, refreshes=0,
+                          exact_counts=0, accepted=0)
 
     def close(self):
         self.eng.close()
@@ -181,20 +228,23 @@ class LNS:
         """Word indices (1-D) or digits (m, n); repeats are dropped."""
         a = np.asarray(code)
         if a.ndim == 2:
-            a = self.eng.word_index(a)
+            a = self.eng.word_index(a) if a.size else np.zeros(0, dtype=np.int64)
         self.code = np.unique(a.astype(np.int64)) if a.size else np.zeros(0, dtype=np.int64)
-        self._recount()
-        self._keep_best()
+        self.recount_from_scratch()
+        self.stats["recounts"] = 0
+        self._remember()
 
-    def _recount(self):
+    def recount_from_scratch(self):
         self.eng.recount(self.code)
         self.stats["transforms"] += 1
+        self.stats["recounts"] += 1
         self.uncov = self.eng.count(0)
+        return self.uncov
 
-    def _keep_best(self):
-        better = (self.best_uncov is None or self.uncov < self.best_uncov or
-                  (self.uncov == self.best_uncov and len(self.code) < len(self.best_code)))
-        if better:
+    def _remember(self):
+        """Keep the best code (fewest uncovered, then fewest words)."""
+        if (self.best_uncov is None or self.uncov < self.best_uncov or
+                (self.uncov == self.best_uncov and len(self.code) < len(self.best_code))):
             self.best_uncov = self.uncov
             self.best_code = self.code.copy()
             self.publish()
@@ -208,160 +258,92 @@ class LNS:
         self._last_pub = now
         write_code_atomic(self.out, self.eng.index_word(self.best_code))
 
-    def recount_from_scratch(self):
-        self._recount()
-        self.stats["recounts"] += 1
+    # ------------------------------------------------------------ moves
+    def recreate(self, M):
+        """Greedy placement up to M words; returns the placed words."""
+        room = M - len(self.code)
+        if room <= 0 or self.uncov == 0:
+            return np.zeros(0, dtype=np.int64)
+        placed, self.uncov, refr, ev = self.eng.greedy(room, self.cand_cap)
+        self.stats["refreshes"] += refr
+        self.stats["transforms"] += refr
+        self.stats["exact_counts"] += ev
+        self.stats["placements"] += len(placed)
+        if len(placed):
+            self.code = np.union1d(self.code, placed)
+        return placed
+
+    def greedy_fill(self, M):
+        self.recreate(M)
         return self.uncov
 
-    # ------------------------------------------------------------ recreate
-    def _refresh_bounds(self, codeset):
-        """Gain map -> heap of (-gain, word) above a threshold that keeps the
-        extraction bounded; returns (heap, threshold)."""
-        eng = self.eng
-        eng.gain_map()
-        self.stats["transforms"] += 1
-        top = eng.map_max()
-        if top <= 0:
-            return [], 0
-        cap = min(eng.extract_cap, self.bound_cap)
-        thr = 1
-        if top > 1:
-            hist = eng.map_hist(1024, top)
-            above = np.cumsum(hist[::-1])[::-1]           # words with gain in bin b or higher
-            ok = np.flatnonzero(above <= cap * 0.9)
-            b = int(ok[0]) if len(ok) else 1023
-            thr = max(1, b * top // 1024 + 1)
-        idx, val, found = eng.map_extract(thr, cap)
-        while found > cap and thr < top:
-            thr = min(top, thr + max(1, (top - thr) // 2))
-            idx, val, found = eng.map_extract(thr, cap)
-        heap = [(-int(v), int(i)) for v, i in zip(val.tolist(), idx.tolist()) if int(i) not in codeset]
-        heapq.heapify(heap)
-        return heap, thr
-
-    def greedy_fill(self, target_m, batch=64, refresh_every=512):
-        """Exact lazy greedy placement until covered, target_m codewords, or
-        the deadline; returns the uncovered count."""
-        eng = self.eng
-        codeset = set(self.code.tolist())
-        heap, thr = [], 1
-        since = refresh_every
-        while self.uncov > 0 and len(codeset) < target_m and self.time_left() >= 5:
-            if since >= refresh_every or not heap:
-                heap, thr = self._refresh_bounds(codeset)
-                since = 0
-                if not heap:
-                    if thr > 1:
-                        since = refresh_every
-                        continue
-                    break
-            cand = []
-            while heap and len(cand) < batch:
-                v, i = heapq.heappop(heap)
-                if i not in codeset:
-                    cand.append(i)
-            if not cand:
-                since = refresh_every
-                continue
-            exact = eng.ball_count(np.array(cand, dtype=np.int64), 0)
-            bi = int(np.argmax(exact))
-            best = int(exact[bi])
-            bound = -heap[0][0] if heap else 0
-            if best < 1:
-                since = refresh_every
-                continue
-            placed = None
-            if best >= bound and best >= thr:
-                placed = cand[bi]
-                eng.ball_update(np.array([placed], dtype=np.int64), +1)
-                codeset.add(placed)
-                self.uncov -= best
-                self.stats["placements"] += 1
-                since += 1
-            elif best < thr:
-                since = refresh_every              # below the extracted range: refresh to stay exact
-            for k, i in enumerate(cand):
-                if i != placed and exact[k] > 0:
-                    heapq.heappush(heap, (-int(exact[k]), i))
-        self.code = np.array(sorted(codeset), dtype=np.int64)
-        return self.uncov
-
-    # ------------------------------------------------------------ ruin
     def losses(self):
+        """Exact private coverage of every codeword (the loss map read at
+        the code)."""
         self.eng.loss_map()
         self.stats["transforms"] += 1
         return self.eng.map_read(self.code)
 
-    def _nearest(self, centre_digits, k):
-        digs = self.eng.index_word(self.code).astype(np.int16)
-        d = (digs != centre_digits[None, :]).sum(axis=1)
-        return np.argsort(d + self.rng.random(len(self.code)))[:k]
+    def _nearest(self, centre, k):
+        """Indices (into self.code) of the k codewords nearest `centre`
+        (digits), ties in random order."""
+        digs = self.eng.index_word(self.code)
+        d = (digs != centre[None, :]).sum(axis=1).astype(np.float64)
+        return np.argsort(d + self.rng.random(len(self.code)), kind="stable")[:k]
 
-    def ruin(self, k, mode="low"):
-        """Remove k codewords (mode: low, random, cluster, hole); returns them."""
+    def choose_ruin(self, k, rule):
+        m = len(self.code)
+        if rule == "random":
+            return self.rng.choice(m, size=k, replace=False)
+        if rule == "cluster":
+            return self._nearest(self.eng.index_word(self.code[self.rng.integers(m)])[0], k)
+        if rule == "near_uncovered":
+            words, found = self.eng.uncovered_words(4096)
+            if found == 0:
+                return self.choose_ruin(k, "soft")
+            u = words[self.rng.integers(len(words))]
+            return self._nearest(self.eng.index_word(np.array([u]))[0], k)
+        # soft minimum of the losses: Gumbel top-k of -loss / tau
+        loss = self.losses().astype(np.float64)
+        tau = max(1.0, self.temperature * float(loss.mean()))
+        g = -loss / tau + self.rng.gumbel(size=m)
+        return np.argsort(-g, kind="stable")[:k]
+
+    def ruin(self, k, rule="soft"):
+        """Remove k codewords chosen by `rule`; returns them."""
         m = len(self.code)
         k = min(k, m - 1)
         if k <= 0:
             return np.zeros(0, dtype=np.int64)
-        if mode == "random":
-            pick = self.rng.choice(m, size=k, replace=False)
-        elif mode == "cluster":
-            centre = self.eng.index_word(self.code[self.rng.integers(m)])[0].astype(np.int16)
-            pick = self._nearest(centre, k)
-        elif mode == "hole":
-            self.eng.gain_map()
-            self.stats["transforms"] += 1
-            top = self.eng.map_max()
-            if top <= 0:
-                return self.ruin(k, "low")
-            hi, _, _ = self.eng.map_extract(max(1, top // 2), 4096)
-            if not len(hi):
-                return self.ruin(k, "low")
-            centre = self.eng.index_word(np.array([int(hi[self.rng.integers(len(hi))])]))[0].astype(np.int16)
-            pick = self._nearest(centre, k)
-        else:
-            lo = self.losses().astype(np.float64)
-            jitter = self.rng.exponential(scale=max(1.0, lo.mean() * 0.15), size=m)
-            pick = np.argsort(lo + jitter)[:k]
+        pick = self.choose_ruin(k, rule)
         removed = self.code[pick]
-        self.eng.ball_update(removed, -1)
+        self.uncov = self.eng.apply(removed, -1)
         self.code = np.delete(self.code, pick)
-        self.uncov = self.eng.count(0)
         self.stats["removals"] += int(k)
         return removed
 
-    # ------------------------------------------------------------ peel
     def peel(self):
-        """Remove zero-loss codewords until none is left; returns how many."""
-        total = 0
-        while self.time_left() >= 5:
-            zeros = np.flatnonzero(self.losses() == 0)
-            if not len(zeros):
-                break
-            zeros = zeros[self.eng.ball_count(self.code[zeros], 1) == 0]
-            if not len(zeros):
-                break
-            self.rng.shuffle(zeros)
-            if 2 * self.R < self.n:
-                digs = self.eng.index_word(self.code[zeros]).astype(np.int16)
-                keep = []
-                for i in range(len(zeros)):
-                    if all((digs[j] != digs[i]).sum() > 2 * self.R for j in keep):
-                        keep.append(i)
-                pick = zeros[np.array(keep)]
-            else:
-                pick = zeros[:1]
-            self.eng.ball_update(self.code[pick], -1)
-            mask = np.ones(len(self.code), dtype=bool)
-            mask[pick] = False
-            self.code = self.code[mask]
-            total += len(pick)
-            self.stats["removals"] += len(pick)
-        if total:
-            self.uncov = self.eng.count(0)
-        return total
+        """Remove, in a random order, every codeword that covers no word
+        alone; returns how many left."""
+        if not len(self.code):
+            return 0
+        order = self.code[self.rng.permutation(len(self.code))]
+        gone, self.uncov = self.eng.peel(order)
+        keep = np.setdiff1d(self.code, order[gone])
+        removed = len(self.code) - len(keep)
+        self.code = keep
+        self.stats["removals"] += removed
+        return removed
 
-    # ------------------------------------------------------------ LNS
+    def _k(self, kmin, kmax):
+        """Ruin size: kmin plus a geometric draw of mean (kmax - kmin) / 4,
+        truncated at kmax."""
+        if kmax <= kmin:
+            return kmin
+        p = 1.0 / (1.0 + (kmax - kmin) / 4.0)
+        return int(min(kmax, kmin + self.rng.geometric(p) - 1))
+
+    # ------------------------------------------------------------ search
     def lns(self, M, budget_s, kmin=8, kmax=None, log_every=20, max_rounds=None):
         """Rounds of ruin + recreate at M codewords until covered, the
         budget or max_rounds; returns the uncovered count of the best code."""
@@ -370,36 +352,36 @@ class LNS:
         self.best_uncov = None
         self.best_code = None
         if len(self.code) < M:
-            self.greedy_fill(M)
-        self._keep_best()
+            self.recreate(M)
+        self._remember()
+        hist = [self.uncov] * max(1, self.history)
         r = 0
         while self.uncov > 0:
-            if time.time() - t0 > budget_s or self.time_left() < 10:
+            if time.time() - t0 > budget_s or self.time_left() < 5:
                 break
             if max_rounds is not None and r >= max_rounds:
                 break
             before = self.uncov
-            k = int(self.rng.integers(kmin, kmax + 1))
-            mode = self.RUIN_MODES[int(self.rng.integers(len(self.RUIN_MODES)))]
-            self.ruin(k, mode)
-            self.greedy_fill(M)
+            rule = self.RUIN_RULES[int(self.rng.choice(len(self.RUIN_RULES), p=self.RUIN_WEIGHTS))]
+            removed = self.ruin(self._k(kmin, kmax), rule)
+            placed = self.recreate(M)
             self.stats["rounds"] += 1
+            v = r % len(hist)
             r += 1
-            if self.uncov > before and self.rng.random() > 0.10:
-                self.code = self.best_code.copy()
-                self._recount()
+            if self.uncov <= before or self.uncov <= hist[v]:
+                self.stats["accepted"] += 1
+                self._remember()
             else:
-                self._keep_best()
+                # undo exactly: the placed words leave, the removed return
+                self.eng.apply(placed, -1)
+                self.uncov = self.eng.apply(removed, +1)
+                self.code = np.union1d(np.setdiff1d(self.code, placed), removed)
+            hist[v] = self.uncov
             if r % log_every == 0:
-                self.log("  lns M=%d round=%d uncov=%d best=%d k=%d (%.0fs)"
-                         % (M, r, self.uncov, self.best_uncov, k, time.time() - t0))
-            if r % 50 == 0:
-                inc = self.uncov
-                if self.recount_from_scratch() != inc:
-                    self.log("  drift: incremental %d, recount %d" % (inc, self.uncov))
-        if self.uncov == 0:
-            self._keep_best()
-        elif self.best_code is not None and self.best_uncov < self.uncov:
+                self.log("  lns M=%d round=%d uncov=%d best=%d (%.1fs)" % (M, r, self.uncov, self.best_uncov,
+                                                                          time.time() - t0))
+        if self.best_code is not None and (self.uncov > self.best_uncov or
+                                           (self.uncov == self.best_uncov and len(self.code) > len(self.best_code))):
             self.code = self.best_code.copy()
-            self._recount()
+            self.recount_from_scratch()
         return self.uncov

@@ -285,8 +285,31 @@ int cov_lns_map_hist(cov_lns *h, int32_t nbins, int32_t vmax, int64_t *hist);
 int cov_lns_map_extract(cov_lns *h, int32_t thr, int64_t cap, uint32_t *idx, int32_t *val, int64_t *found);
 int cov_lns_map_read(cov_lns *h, const uint32_t *idx, int32_t k, int32_t *out);
 /* op 0: out[i] = #{y in the ball of idx[i] : cnt[y] == arg};
- * op 1: add arg to cnt over the ball of every idx[i], one after another */
+ * op 1: add arg (+1 or -1) to cnt over the ball of every idx[i], one after
+ * another (cov_lns_apply) */
 int cov_lns_ball(cov_lns *h, const uint32_t *idx, int32_t k, int32_t op, int32_t arg, int32_t *out);
+/* Add sign (+1 or -1) to cnt over the ball of every listed word, one word
+ * after another; *uncovered receives #{x : cnt[x] == 0} afterwards. */
+int cov_lns_apply(cov_lns *h, const uint32_t *idx, int32_t k, int32_t sign, int64_t *uncovered);
+/* Exact peel in the given order (the peel of cov/gemm2/gpuchain.py:325-364,
+ * here sequential and exact): a listed codeword is removed (its ball -1)
+ * when, at its turn, no word of its ball is covered by it alone; removed[i]
+ * = 1 for those.  The uncovered count never changes. */
+int cov_lns_peel(cov_lns *h, const uint32_t *idx, int32_t k, uint8_t *removed, int32_t *nremoved,
+                 int64_t *uncovered);
+/* Lazy greedy placement (the recreate of cov/gemm2/gpuchain.py:193-279):
+ * up to `room` words, each one of maximal exact gain (#uncovered words it
+ * covers; ties to the lower index), until everything is covered or no word
+ * gains.  Bounds come from the gain map: at most cand_cap candidates above a
+ * threshold stay on the device, and a persistent cluster kernel re-counts
+ * the best bound exactly until it is current, then places it; the host only
+ * refreshes the map when the threshold is reached.  placed[] receives the
+ * words in order; stats (may be null): refreshes, exact counts. */
+int cov_lns_greedy(cov_lns *h, int32_t room, int64_t cand_cap, uint32_t *placed, int32_t *nplaced,
+                   int64_t *uncovered, int64_t *stats);
+/* The uncovered words (cnt == 0) in increasing index order, at most cap of
+ * them, and how many there are (overwrites the map). */
+int cov_lns_uncovered(cov_lns *h, int64_t cap, uint32_t *idx, int64_t *found);
 /* #{x : cnt[x] == target} */
 int cov_lns_count(cov_lns *h, int32_t target, int64_t *out);
 int cov_lns_get_cnt(cov_lns *h, uint16_t *out);
