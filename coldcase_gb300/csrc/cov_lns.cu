@@ -382,6 +382,8 @@ struct SeqArgs {
     int32_t *bound;
     int32_t *fresh;
     int ncand, thr, room;          // room: words still to place
+    int eval_cap;                  // exact counts since the last placement after which a
+                                   // fresh map is cheaper (the host refreshes)
     long long max_steps;           // bound on the steps of one launch
     // peel / apply: the listed words in order
     uint32_t *list;
@@ -443,7 +445,7 @@ __global__ void __cluster_dims__(SEQ_CL, 1, 1) __launch_bounds__(SEQ_NT) k_lns_s
     __shared__ SeqShared sh;
     __shared__ unsigned long long s_wmax[SEQ_NT / 32];
     __shared__ long long s_uncov, s_evals, s_steps;
-    __shared__ int s_epoch, s_placed, s_removed, s_i;
+    __shared__ int s_epoch, s_placed, s_removed, s_i, s_since;
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     SeqShared *lead = cl.map_shared_rank(&sh, 0);
@@ -452,7 +454,7 @@ __global__ void __cluster_dims__(SEQ_CL, 1, 1) __launch_bounds__(SEQ_NT) k_lns_s
         sh.sum = 0; sh.act = ACT_NEXT; sh.stop = 0; sh.pos = 0; sh.word = 0;
         if (rank == 0) {
             s_uncov = a.st->uncov; s_evals = 0; s_steps = 0;
-            s_epoch = 1; s_placed = 0; s_removed = 0; s_i = 0;
+            s_epoch = 1; s_placed = 0; s_removed = 0; s_i = 0; s_since = 0;
         }
     }
     __syncthreads();
@@ -485,6 +487,8 @@ __global__ void __cluster_dims__(SEQ_CL, 1, 1) __launch_bounds__(SEQ_NT) k_lns_s
                 // or beat the best: the host refreshes the bounds (and stops
                 // when the fresh map has no positive gain)
                 else if (pos < 0 || bnd < a.thr) st = SEQ_REFRESH;
+                // so many bounds went stale that a fresh map is cheaper
+                else if (s_since >= a.eval_cap && __ldcg(&a.fresh[pos]) != s_epoch) st = SEQ_REFRESH;
                 if (st >= 0) {
                     sh.act = ACT_STOP;
                     a.st->status = st;
@@ -527,6 +531,7 @@ __global__ void __cluster_dims__(SEQ_CL, 1, 1) __launch_bounds__(SEQ_NT) k_lns_s
                 if (a.mode == MODE_GREEDY) {
                     __stcg(&a.bound[pos], (int32_t)sh.sum);
                     __stcg(&a.fresh[pos], s_epoch);
+                    s_since++;
                     sh.act = ACT_NEXT;
                 } else {
                     sh.act = sh.sum == 0 ? ACT_PLACE : ACT_NEXT;    // peel: remove if it covers nothing alone
@@ -548,6 +553,7 @@ __global__ void __cluster_dims__(SEQ_CL, 1, 1) __launch_bounds__(SEQ_NT) k_lns_s
                 a.list[s_placed++] = word;
                 __stcg(&a.bound[pos], 0);         // a codeword now: its ball is covered
                 s_epoch++;
+                s_since = 0;
             } else {
                 if (a.mode == MODE_PEEL) { a.flag[s_i] = 1; s_removed++; }
                 s_i++;
@@ -720,6 +726,17 @@ BallGeom ball_geom(const cov_lns *h)
     for (int j = 0; j < h->n; j++) b.pw[j] = h->pw[j];
     b.items = h->ball; b.last = h->ball_last; b.ngroups = h->ngroups;
     return b;
+}
+
+// words in one ball of the cell
+long long ball_words(const cov_lns *h)
+{
+    long long v = 0, c = 1;
+    for (int i = 0; i <= h->R; i++) {
+        v += c;
+        c = c * (h->n - i) / (i + 1) * (h->q - 1);
+    }
+    return std::max(1LL, v);
 }
 
 // one sequence launch; st in/out through h->seq
@@ -1026,8 +1043,9 @@ int cov_lns_greedy(cov_lns *h, int32_t room, int64_t cand_cap, uint32_t *placed,
     if (st.uncov < 0) return -100;
     int total = 0;
     long long refreshes = 0, evals = 0;
-    // every refresh that finds a positive gain places at least one word
-    for (int guard = 0; total < room && st.uncov > 0 && guard <= room + 1; guard++) {
+    // every refresh that finds a positive gain places at least one word (the
+    // first placement of a launch needs no exact count: all bounds are fresh)
+    for (int guard = 0; total < room && st.uncov > 0 && guard <= 2 * room + 2; guard++) {
         // bounds: the exact gain map, extracted above a threshold that keeps
         // at most cand_cap candidates
         rc = cov_lns_map(h, 0);
@@ -1059,6 +1077,9 @@ int cov_lns_greedy(cov_lns *h, int32_t room, int64_t cand_cap, uint32_t *placed,
         a.thr = thr;
         a.room = room - total;
         a.list = h->list + total;
+        // a map costs about as much as N / (2 |ball|) exact counts: past
+        // that many counts for one placement, refresh instead
+        a.eval_cap = (int)std::max<long long>(8, std::min<long long>(4096, (long long)h->N / (2LL * ball_words(h))));
         a.max_steps = 64LL * (room - total) + 4LL * ncand + 64;
         rc = seq_run(h, a, &st);
         if (rc) return rc;
