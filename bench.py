@@ -704,6 +704,53 @@ def lns_bench(args):
     return out
 
 
+def portfolio_bench(args):
+    """A portfolio of N chains two ways, on the q6 n9 R4 M700 cell with the
+    flags campaign.py passes: N covsearch_gpu processes started together
+    (each its own CUDA context, taking turns on the GPU; the sum of their
+    own RESULT rates), and the same N chains as one Pool in this process
+    (the seeds campaign would give them)."""
+    import re
+    import torch
+    from coldcase_gb300.engine import Pool
+    from coldcase_gb300.workloads import uniform_code
+    q, n, R, M, N, T = 6, 9, 4, 700, args.portfolio_chains, args.portfolio_s
+    cli = os.path.join(HERE, "coldcase_gb300", "bin", "covsearch_gpu")
+    rx = re.compile(r"RESULT .* iters=(\d+) .*time=([0-9.]+) ")
+    with tempfile.TemporaryDirectory() as d:
+        code = uniform_code(q, n, M, 5)
+        path = _code_file(d, "seed.txt", code, q)
+        procs = [subprocess.Popen([sys.executable, cli, "-q", str(q), "-n", str(n), "-R", str(R), "-M", str(M),
+                                   "-t", str(T), "-s", str(1 + w), "--threads", "1", "--in", path,
+                                   "--out", os.path.join(d, "w%d.txt" % w), "--quiet"],
+                                  stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True) for w in range(N)]
+        rates, iters = [], 0
+        for p in procs:
+            txt, _ = p.communicate()
+            m = rx.search(txt or "")
+            if m and float(m.group(2)) > 0:
+                rates.append(int(m.group(1)) / float(m.group(2)))
+                iters += int(m.group(1))
+    pool = Pool(N, cluster=8, budget_s=120.0)
+    slots = [pool.add(q, n, R, M, code=code, seed=1 + w) for w in range(N)]
+    pool.run(50)
+    it0 = sum(pool.status(s)["it"] for s in slots)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < min(T, 5.0):
+        pool.run(200)
+    dt = time.perf_counter() - t0
+    moves = sum(pool.status(s)["it"] for s in slots) - it0
+    pool.close()
+    one = moves / dt
+    procs_rate = sum(rates)
+    return dict(cell="q6 n9 R4 M700, campaign's flags, one seed code", chains=N,
+                processes=dict(moves_s=procs_rate, finished=len(rates), seconds=T,
+                               note="sum of each process's RESULT rate (its moves after init / its search time)"),
+                one_pool=dict(moves_s=one, cluster=8, seconds=dt),
+                pool_over_processes=one / procs_rate if procs_rate else None)
+
+
 def ctypes_sizeof_status():
     from coldcase_gb300 import lib as L
     import ctypes
@@ -979,6 +1026,10 @@ def gpu_bench(args, rank, world, dist):
                         batch=dict(value=bmoves_all / dt_max, instances=len(seeds) * world,
                                    cluster=args.sym_cluster, moves=args.sym_batch_moves))
 
+    portfolio = None
+    if rank == 0 and not args.no_portfolio:
+        portfolio = portfolio_bench(args)
+
     lns = None
     if rank == 0 and not args.no_lns:
         lns = lns_bench(args)
@@ -988,7 +1039,7 @@ def gpu_bench(args, rank, world, dist):
         comparators = gpu_comparators(args, dev)
 
     return dict(value=value, ms=ms_max, step_ms=step_ms, moves=moves_all, clocks=clocks, e2e=e2e,
-                comparators=comparators, lns=lns,
+                comparators=comparators, lns=lns, portfolio=portfolio,
                 plain=plain, cov=cov, finished=finished, best_unc=best_unc, work=work, hetero=hetero,
                 served=served, plain_cfgs=plain_cfgs, quotient=quotient)
 
@@ -1030,6 +1081,9 @@ def main():
                     help="skip timing the reference's own GPU kernels beside this engine")
     ap.add_argument("--comp-chains", type=int, default=256, help="chains per comparator cell")
     ap.add_argument("--no-lns", action="store_true", help="skip the transform-engine search leg")
+    ap.add_argument("--no-portfolio", action="store_true", help="skip the N-processes-vs-one-pool leg")
+    ap.add_argument("--portfolio-chains", type=int, default=8)
+    ap.add_argument("--portfolio-s", type=float, default=10.0, help="seconds per portfolio process")
     ap.add_argument("--lns-rounds", type=int, default=0, help="ruin-and-recreate rounds per LNS cell (0: default)")
     ap.add_argument("--sym-moves", type=int, default=300)
     ap.add_argument("--sym-batch", type=int, default=38, help="quotient-search instances per GPU")
@@ -1127,6 +1181,7 @@ def main():
             quotient=r["quotient"],
             gpu_comparators=r["comparators"],
             lns=r["lns"],
+            portfolio=r["portfolio"],
             finished_restarts=r["finished"],
         )
         if r["quotient"] and sym_cpu:
