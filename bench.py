@@ -389,16 +389,23 @@ def dt_pass_bytes(q, n):
     same grouping of axes as cov_verify.cu's dt_run)."""
     N = q ** n
     q4 = (q + 3) // 4 * 4
-    k = 1
-    while k < n and q ** (k + 1) // q * q4 <= 65536:
-        k += 1
-    passes, j0 = 0, k
-    while j0 < n:
-        g = 0
-        while j0 + g < n and q ** (g + 1) * 32 <= 98304:
-            g += 1
-        j0 += g
-        passes += 1
+
+    def sweeps(k):
+        passes, j0 = 0, k
+        while j0 < n:
+            g = 0
+            while j0 + g < n and q ** (g + 1) * 32 <= 98304:
+                g += 1
+            j0 += max(g, 1)
+            passes += 1
+        return passes
+
+    def low(cap):
+        k = 1
+        while k < n and q ** (k + 1) // q * q4 <= cap:
+            k += 1
+        return k
+    passes = min(sweeps(low(65536)), sweeps(low(200 * 1024)))
     return N // 8 + N + 2 * N * passes
 
 

@@ -22,7 +22,9 @@
 #include "cov_tiles.cuh"
 #include "../../include/covgpu.h"
 
-#define DT_TILE_MAX   65536    // bytes of the contiguous low-axes tile
+#define DT_TILE_MAX   65536    // bytes of the contiguous low-axes tile (several CTAs per SM)
+#define DT_TILE_BIG   (200 * 1024)  // a tile of one CTA per SM, used when it saves a sweep
+#define DT_NT_BIG     1024     // threads of a big-tile CTA
 #define DT_STRIP_MAX  98304    // bytes of a high-axes strip
 #define DT_STRIP_W    32       // narrowest strip (columns); strips widen while they fit
 #define DT_NT         512
@@ -62,13 +64,22 @@ __device__ __forceinline__ void dt_hist_add(int *sh, int v)
 // so one __vminu4 serves four of them.
 __device__ __forceinline__ void dt_pass4(uint32_t *w, int nfib, int q, int stride, int inner, uint32_t inf4)
 {
+    // f / inner by a float reciprocal: f < 2^24, so the estimate is off by
+    // at most one and one correction makes it exact
+    const float rinv = 1.0f / (float)inner;
     for (int f = threadIdx.x; f < nfib; f += blockDim.x) {
-        const int o = f / inner, i = f - o * inner;
+        int o = (int)((float)f * rinv);
+        int i = f - o * inner;
+        if (i < 0) { o--; i += inner; } else if (i >= inner) { o++; i -= inner; }
         uint32_t *b = w + o * q * stride + i;
-        uint32_t m = inf4;
-        for (int a = 0; a < q; a++) m = __vminu4(m, b[a * stride]);
+        uint32_t m = inf4, v[COV_MAXQ];
+#pragma unroll
+        for (int a = 0; a < COV_MAXQ; a++)
+            if (a < q) { v[a] = b[a * stride]; m = __vminu4(m, v[a]); }
         const uint32_t c = __vminu4(__vadd4(m, 0x01010101u), inf4);
-        for (int a = 0; a < q; a++) b[a * stride] = __vminu4(b[a * stride], c);
+#pragma unroll
+        for (int a = 0; a < COV_MAXQ; a++)
+            if (a < q) b[a * stride] = __vminu4(v[a], c);
     }
 }
 
@@ -79,7 +90,7 @@ __device__ __forceinline__ void dt_pass4(uint32_t *w, int nfib, int q, int strid
 // while loading: a word is 0 on the code, 1 if its line holds a codeword,
 // else n+1.  When k == n this is the whole transform and the histogram is
 // taken here.
-__global__ void __launch_bounds__(DT_NT)
+__global__ void __launch_bounds__(DT_NT_BIG)
 k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__ D,
          unsigned long long *hist)
 {
@@ -455,7 +466,7 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
 {
     int dev = 0;
     if (!g_dt_attr.done(dev)) {
-        CK(cudaFuncSetAttribute(k_dt_low, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_TILE_MAX));
+        CK(cudaFuncSetAttribute(k_dt_low, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_TILE_BIG));
         CK(cudaFuncSetAttribute(k_dt_high, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_STRIP_MAX));
         g_dt_attr.set(dev);
     }
@@ -467,13 +478,29 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
     // low group: as many axes as fit a tile
     const long long q4 = (g.q + 3) / 4 * 4;      // padded bytes of one lowest-axis line
     auto low_bytes = [&](int kk) { return (long long)g.pw[kk] / g.q * q4; };
+    // HBM sweeps of the strip passes after a low tile of kk axes
+    auto strip_sweeps = [&](int kk) {
+        int sw = 0, j = kk;
+        while (j < g.n) {
+            int gz = 0;
+            while (j + gz < g.n && (long long)g.pw[gz + 1] * DT_STRIP_W <= DT_STRIP_MAX) gz++;
+            j += std::max(gz, 1);
+            sw++;
+        }
+        return sw;
+    };
     int k = 1;
     while (k < g.n && low_bytes(k + 1) <= DT_TILE_MAX) k++;
+    // a bigger tile (one CTA per SM, twice the threads) only where it saves a sweep
+    int kb = k;
+    while (kb < g.n && low_bytes(kb + 1) <= DT_TILE_BIG) kb++;
+    const bool big = strip_sweeps(kb) < strip_sweeps(k);
+    if (big) k = kb;
     const int sms = std::max(1, cov_sm_count());
     const uint32_t ntile = g.N / g.pw[k];
     {
-        int grid = (int)std::min<uint32_t>(ntile, (uint32_t)sms * 4);
-        k_dt_low<<<grid, DT_NT, (size_t)low_bytes(k), st>>>(g, k, d_bm, d_D, d_hist);
+        int grid = (int)std::min<uint32_t>(ntile, (uint32_t)sms * (big ? 1 : 4));
+        k_dt_low<<<grid, big ? DT_NT_BIG : DT_NT, (size_t)low_bytes(k), st>>>(g, k, d_bm, d_D, d_hist);
         CK(cudaGetLastError());
     }
     // high groups
