@@ -9,12 +9,13 @@ exit status (0 iff the best code covers, 1 otherwise, 2 on bad arguments).
 
 The search is the p5b trajectory, with or without --wide (every
 single-coordinate move of each candidate codeword while the uncovered list
-is short, covsearch2e.c:1353-1376).  Presets base/p1..p5/p5b/best and the
-speed-only switches (--st --eval --walk --hoist --early --pf --huge
---threads) leave the trajectory unchanged in the reference
-(cov/opt/METHODS.md:395-409) and are accepted; the other switches that
-change the trajectory (--sa --noise --fix0 --ucache --upick) are rejected
-with exit status 2.
+is short, covsearch2e.c:1353-1376) and --fix0 (the initial code translated
+so that codeword 0 is 0^n, which then never moves, :1241-1253, :1343,
+:1560).  Presets base/p1..p5/p5b/best and the speed-only switches (--st
+--eval --walk --hoist --early --pf --huge --threads) leave the trajectory
+unchanged in the reference (cov/opt/METHODS.md:395-409) and are accepted;
+the other switches that change the trajectory (--sa --noise --ucache
+--upick) are rejected with exit status 2.
 """
 import os
 import sys
@@ -29,7 +30,7 @@ from .lib import CovError
 USAGE = ("usage: covsearch -q Q -n N -R R -M M [-t sec] [-s seed] [--in f] [--out f]\n"
          "                 [--cand K] [--tabu T] [--kick K] [--noise PERMILLE] [--iters I]\n"
          "                 [--stall S] [--sa --t0 T0 --cool C --tmin TMIN]\n"
-         "                 [--random-init] [--wide]\n"
+         "                 [--random-init] [--wide] [--fix0]\n"
          "                 [--threads T] [--quiet]\n")
 
 PRESETS = {"base", "p1", "p2", "p2b", "p3", "p4", "p5", "best", "p5b"}
@@ -37,13 +38,13 @@ VALUE_FLAGS = {"-q", "-n", "-R", "-M", "-t", "-s", "--in", "--out", "--cand", "-
                "--noise", "--iters", "--stall", "--threads", "--t0", "--cool", "--tmin", "--st",
                "--eval", "--walk", "--target", "--cpu", "--preset", "--cluster", "--chunk"}
 SPEED_SWITCHES = {"--hoist", "--early", "--pf", "--huge"}
-TRAJECTORY_SWITCHES = {"--sa", "--fix0", "--ucache", "--upick"}
+TRAJECTORY_SWITCHES = {"--sa", "--ucache", "--upick"}
 
 
 def parse(argv):
     a = dict(q=0, n=0, R=-1, M=0, t=60.0, s=12345, inp=None, out=None, cand=100000, tabu=0,
              kick=2, noise=0, iters=-1, stall=5000, random_init=False, quiet=False, target=-1,
-             cluster=None, chunk=0, wide=False)
+             cluster=None, chunk=0, wide=False, fix0=False)
     i = 0
     while i < len(argv):
         f = argv[i]
@@ -75,6 +76,8 @@ def parse(argv):
             a["random_init"] = True
         elif f == "--wide":
             a["wide"] = True
+        elif f == "--fix0":
+            a["fix0"] = True
         elif f == "--quiet":
             a["quiet"] = True
         elif f in SPEED_SWITCHES:
@@ -131,7 +134,7 @@ def main(argv=None):
     cluster = a["cluster"] or (8 if N >= 1 << 20 else 2)
     try:
         eng = Search(q, n, R, M, seed=a["s"], tabu=a["tabu"], kick=a["kick"], stall=a["stall"],
-                     cand=a["cand"], cluster=cluster, wide=a["wide"])
+                     cand=a["cand"], cluster=cluster, wide=a["wide"], fix0=a["fix0"])
         unc0 = eng.load(code, random_init=a["random_init"])
     except CovError as e:
         sys.stderr.write("covsearch_gpu: %s\n" % e)

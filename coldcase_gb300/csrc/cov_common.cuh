@@ -97,6 +97,7 @@ struct CovSlot {
     int wide;                    // --wide: every single-coordinate move of a candidate codeword
                                  // while the list is valid and U_n n < (R+1) S'
     int wide_sliced;             // its list pass finds hits by bit-sliced counts (<= 64 candidates)
+    int fix0;                    // --fix0: codeword 0 translated to 0^n and never moved (0 or 1)
     // device arrays
     uint32_t *cw;                // [N]  cnt (bits 0-15) | sum of covering ids mod 2^16 (16-31)
     uint64_t *code;              // [M]  packed codewords

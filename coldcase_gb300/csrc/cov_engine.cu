@@ -1572,7 +1572,9 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
     // distances to all codewords and the target distance (covsearch2e.c:1342-1351)
     const bool csm = M <= CODE_SM;
     unsigned dm = 0xffffffffu;
+    // (with --fix0 codeword 0 is not a candidate, covsearch2e.c:1343)
     for (int i = tid; i < M; i += NT) {
+        if (i < d.fix0) { if (csm) S.dist8[i] = 0xff; continue; }
         int dd = cov_dist(leader_code(d, S, i), pu);
         if (csm) S.dist8[i] = (uint8_t)dd;
         dm = min(dm, (unsigned)dd);
@@ -1589,7 +1591,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         int i = c0 + tid;
         uint64_t pk = 0;
         int f = 0;
-        if (i < M) {
+        if (i < M && i >= d.fix0) {
             pk = leader_code(d, S, i);
             f = (csm ? (int)S.dist8[i] : cov_dist(pk, pu)) == dtar;
         }
@@ -2071,7 +2073,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                     const int cnt = cov_ldcg(&d.st->ul_n);
                     if (S.ul_valid && cnt > d.ul_cap) S.ul_valid = 0;
                     S.uln = min(cnt, d.ul_cap);
-                    int i = (int)fastmod(S, rs_take(S), (uint64_t)d.M);
+                    int i = d.fix0 + (int)fastmod(S, rs_take(S), (uint64_t)(d.M - d.fix0));
                     uint64_t pk = leader_code(d, S, i);
                     OpParams &o = S.opp;
                     o.op = OP_BALL; o.sgn = -1; o.mi = i; o.pc = pk; o.base = widx_pk(d, pk);
@@ -2856,6 +2858,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     long long N = ipow_h(q, n);
     if (N >= (1LL << 32) - 1) return COV_EINVAL;
     if (prm->wide < 0 || prm->wide > 1) return COV_EINVAL;
+    if (prm->fix0 < 0 || prm->fix0 > 1 || (prm->fix0 && prm->M < 2)) return COV_EINVAL;
     if (R > n) R = n;
     int s = -1;
     for (int k = 0; k < pool->max_slots; k++) if (!pool->slots[k].used) { s = k; break; }
@@ -2879,6 +2882,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.neg_cluster_pairs = pool->neg_cluster_pairs;
     d.list_cost = pool->list_cost;
     d.wide = prm->wide ? 1 : 0;
+    d.fix0 = prm->fix0 ? 1 : 0;
     d.wide_sliced = 1;
     d.padj_warp = padj_auto(q, n, R, M);
     d.zbits = d.padj_warp;
@@ -3070,6 +3074,23 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
             pk[i] = v;
         }
         CK(cudaMemcpyAsync(d.code, pk.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
+    }
+    if (d.fix0) {
+        // --fix0 (covsearch2e.c:1241-1253): w -> w - c_0 digit by digit mod q
+        // is an isometry, so the code is translated to put codeword 0 at 0^n
+        // (the uncovered count does not change) and rebuilt below
+        std::vector<uint64_t> cur((size_t)M);
+        CK(cudaMemcpyAsync(cur.data(), d.code, (size_t)M * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        const uint64_t c0 = cur[0];
+        for (int i = 0; i < M; i++) {
+            uint64_t v = 0;
+            for (int j = 0; j < n; j++)
+                v |= (uint64_t)((cov_nib(cur[i], j) + q - cov_nib(c0, j)) % q) << (4 * j);
+            cur[i] = v;
+        }
+        CK(cudaMemcpyAsync(d.code, cur.data(), (size_t)M * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
     }
     // coverage array, uncovered count, uncovered-word list and private
     // counts of the final M codewords, built tile by tile; then the best code

@@ -14,10 +14,10 @@ DEFAULTS = dict(seed=12345, tabu=0, kick=2, stall=5000, cand=100000)
 
 
 def make_params(q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000,
-                trace=0, trace_cap=0, wide=False):
+                trace=0, trace_cap=0, wide=False, fix0=False):
     return L.CovParams(q=q, n=n, R=R, M=M, seed=seed, tabu=tabu, kick=kick, cand=cand,
                        trace=1 if trace else 0, stall=stall, trace_cap=trace_cap if trace else 0,
-                       wide=1 if wide else 0, reserved=0)
+                       wide=1 if wide else 0, fix0=1 if fix0 else 0)
 
 
 def slot_bytes(q, n, R, M, **kw):
@@ -56,11 +56,11 @@ class Pool:
                 "cov_pool_set_slot_param")
 
     def add(self, q, n, R, M, code=None, random_init=False, seed=12345, tabu=0, kick=2,
-            stall=5000, cand=100000, trace=0, trace_cap=0, wide=False):
+            stall=5000, cand=100000, trace=0, trace_cap=0, wide=False, fix0=False):
         """Create an instance from `code` (m x n digits; m may be <, = or > M).
-        `wide` is covsearch2e's --wide."""
+        `wide` and `fix0` are covsearch2e's --wide and --fix0."""
         p = make_params(q, n, R, M, seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand,
-                        trace=trace, trace_cap=trace_cap, wide=wide)
+                        trace=trace, trace_cap=trace_cap, wide=wide, fix0=fix0)
         if code is None:
             arr = np.zeros((0, n), dtype=np.uint8)
         else:
@@ -207,14 +207,14 @@ class Pool:
 class Search:
     """One covsearch2e instance on the GPU (a pool with a single slot).
 
-    Parameters are covsearch2e's: -q -n -R -M -s --tabu --kick --stall --cand --wide.
+    Parameters are covsearch2e's: -q -n -R -M -s --tabu --kick --stall --cand --wide --fix0.
     """
 
     def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000,
-                 cluster=8, trace=0, trace_cap=0, budget_s=30.0, wide=False):
+                 cluster=8, trace=0, trace_cap=0, budget_s=30.0, wide=False, fix0=False):
         self.q, self.n, self.R, self.M = q, n, R, M
         self.kw = dict(seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand,
-                       trace=trace, trace_cap=trace_cap, wide=wide)
+                       trace=trace, trace_cap=trace_cap, wide=wide, fix0=fix0)
         self.pool = Pool(1, cluster=cluster, budget_s=budget_s)
         self.slot = None
 

@@ -51,7 +51,7 @@ class CovParams(ctypes.Structure):
                 ("M", ctypes.c_int32), ("seed", ctypes.c_uint64), ("tabu", ctypes.c_int32),
                 ("kick", ctypes.c_int32), ("cand", ctypes.c_int32), ("trace", ctypes.c_int32),
                 ("stall", ctypes.c_int64), ("trace_cap", ctypes.c_int64), ("wide", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("fix0", ctypes.c_int32)]
 
 
 class CovStatus(ctypes.Structure):

@@ -79,7 +79,10 @@ typedef struct {
     int64_t trace_cap;    /* records kept when trace = 1                    */
     int32_t wide;         /* --wide  all n(q-1) moves of a candidate codeword
                            *         (covsearch2e.c:1353-1376); 0 = off     */
-    int32_t reserved;     /* 0                                              */
+    int32_t fix0;         /* --fix0  translate the initial code so codeword 0
+                           *         is 0^n and never move it
+                           *         (covsearch2e.c:1241-1253, :1343, :1359,
+                           *         :1560); 0 = off                        */
 } cov_params;
 
 typedef struct {

@@ -18,7 +18,7 @@ def run_cli(args, timeout=300):
                           timeout=timeout, cwd=REPO)
 
 
-@pytest.mark.parametrize("flag", ["--sa", "--fix0", "--ucache", "--upick"])
+@pytest.mark.parametrize("flag", ["--sa", "--ucache", "--upick"])
 def test_trajectory_switches_refused(flag):
     r = run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", flag])
     assert r.returncode == 2 and "trajectory" in r.stderr
@@ -91,6 +91,31 @@ def test_sym_cli_matches_reference_runs(covlib, sym_golden):
             ref = r["ref"]
             assert (int(m.group(1)), int(m.group(2)), int(m.group(4)), int(m.group(5))) == \
                 (ref["orbits"], ref["red_uncovered"], ref["iters"], ref["kicks"]), (r["q"], r["n"], r["R"], r["M"])
+            assert p.returncode == ref["rc"]
+            with open(out) as f:
+                assert f.read() == ref["out"]
+
+
+def test_fix0_arguments_through_the_protocol():
+    """--fix0 reaches the engine with the other flags, and the RESULT line,
+    exit status and --out file equal the reference binary's; the oracle
+    stands in for the GPU engine (tests/portfolio_stub.py)."""
+    import json
+    stub = os.path.join(REPO, "tests", "portfolio_stub.py")
+    with open(os.path.join(REPO, "tests", "golden", "opt_runs.json")) as f:
+        runs = [r for r in json.load(f) if r.get("fix0") and not r["code"]][:2]
+    assert runs
+    for r in runs:
+        with tempfile.TemporaryDirectory() as td:
+            out = os.path.join(td, "out.txt")
+            p = subprocess.run([sys.executable, stub] + [str(a) for a in [
+                "-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
+                "--tabu", r["tabu"], "--kick", r["kick"], "--stall", r["stall"], "--out", out, "--fix0",
+                "--quiet"]], capture_output=True, text=True, timeout=300, cwd=REPO)
+            m = re.search(r"RESULT .*uncovered=(\d+) iters=(\d+) kicks=(\d+)", p.stdout)
+            assert m, p.stdout + p.stderr
+            ref = r["ref"]
+            assert (int(m.group(1)), int(m.group(2)), int(m.group(3))) == (ref["uncovered"], ref["iters"], ref["kicks"])
             assert p.returncode == ref["rc"]
             with open(out) as f:
                 assert f.read() == ref["out"]
