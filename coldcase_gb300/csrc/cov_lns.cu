@@ -41,6 +41,7 @@ namespace cg = cooperative_groups;
 
 #define LNS_MAXR 8
 #define LNS_NT 256
+#define LNS_HIST_MAX 8192   // bins of cov_lns_map_hist (one shared-memory counter each)
 #define MAP_NT 512
 #define MAP_SMEM_MAX (200 * 1024)   // shared memory of one map tile (bytes)
 #define MAP_W_MIN 8                 // narrowest strip: 32 bytes of a layer per row
@@ -237,14 +238,34 @@ __global__ void k_lns_max(const int32_t *A, uint32_t N, int *out)
 }
 
 // histogram of values v >= 1 in nbins bins of [1, vmax]: bin = (v-1)*nbins/vmax
+// histogram of the positive values: value v in bin (min(v,vmax)-1)*nbins/vmax.
+// Counted per block in shared memory (the lanes of a warp that share a bin
+// add once), then one global add per bin and block: the values of a gain map
+// crowd into few bins, where per-element global atomics serialise.
 __global__ void k_lns_hist(const int32_t *A, uint32_t N, int nbins, int vmax, unsigned long long *hist)
 {
-    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x) {
-        const int v = A[x];
-        if (v < 1) continue;
-        int b = (int)((long long)(min(v, vmax) - 1) * nbins / vmax);
-        atomicAdd(&hist[b], 1ull);
+    extern __shared__ uint32_t lh[];
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) lh[b] = 0;
+    __syncthreads();
+    // (v-1)*nbins in 32 bits when it cannot overflow
+    const bool narrow = (unsigned long long)vmax * (unsigned long long)nbins < (1ull << 32);
+    for (uint32_t x0 = blockIdx.x * blockDim.x; x0 < N; x0 += gridDim.x * blockDim.x) {
+        const uint32_t x = x0 + threadIdx.x;
+        int b = -1;
+        if (x < N) {
+            const int v = A[x];
+            if (v >= 1) {
+                const uint32_t t = (uint32_t)(min(v, vmax) - 1);
+                b = narrow ? (int)(t * (uint32_t)nbins / (uint32_t)vmax)
+                           : (int)((unsigned long long)t * (unsigned long long)nbins / (unsigned long long)vmax);
+            }
+        }
+        const unsigned grp = __match_any_sync(0xffffffffu, b);
+        if (b >= 0 && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&lh[b], (uint32_t)__popc(grp));
     }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+        if (lh[b]) atomicAdd(&hist[b], (unsigned long long)lh[b]);
 }
 
 // ordered compaction of {x : A[x] >= thr}: per-block counts, then positions
@@ -893,12 +914,12 @@ int cov_lns_map_max(cov_lns *h, int32_t *out)
 
 int cov_lns_map_hist(cov_lns *h, int32_t nbins, int32_t vmax, int64_t *hist)
 {
-    if (!h || !hist || nbins < 1 || vmax < 1) return COV_EINVAL;
+    if (!h || !hist || nbins < 1 || nbins > LNS_HIST_MAX || vmax < 1) return COV_EINVAL;
     int rc = lns_scratch(h, (size_t)nbins * 8);
     if (rc) return rc;
     unsigned long long *d_h = (unsigned long long *)h->scratch;
     CK(cudaMemset(d_h, 0, (size_t)nbins * 8));
-    k_lns_hist<<<grid_of(h->N), LNS_NT>>>(h->map, h->N, nbins, vmax, d_h);
+    k_lns_hist<<<grid_of(h->N), LNS_NT, (size_t)nbins * 4>>>(h->map, h->N, nbins, vmax, d_h);
     CK(cudaGetLastError());
     CK(cudaMemcpy(hist, d_h, (size_t)nbins * 8, cudaMemcpyDeviceToHost));
     return COV_OK;

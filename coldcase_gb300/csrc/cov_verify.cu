@@ -58,12 +58,16 @@ __device__ __forceinline__ void dt_hist_add(int *sh, int v)
     if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&sh[v], __popc(same));
 }
 
-// One line-min pass over packed bytes: `nfib` fibres of q 32-bit words, word
-// k of fibre f at  base(f) + a*stride  (a < q), base(f) = (f / inner) *
-// q*stride + (f % inner).  Each word holds 4 independent lines (one per byte),
-// so one __vminu4 serves four of them.
-__device__ __forceinline__ void dt_pass4(uint32_t *w, int nfib, int q, int stride, int inner, uint32_t inf4)
+// One line-min pass over packed bytes: `nfib` fibres of Q 32-bit words, word
+// a of fibre f at  base(f) + a*stride  (a < Q), base(f) = (f / inner) *
+// Q*stride + (f % inner).  Each word holds 4 independent lines (one per
+// byte).  The bytes are worked as two pairs of 16-bit lanes (bytes 0,2 and
+// 1,3), where the minimum of three values and min(m + 1, n + 1) are single
+// dynamic-programming instructions (__vimin3_u16x2, __viaddmin_u16x2).
+template <int Q>
+__device__ __forceinline__ void dt_pass4(uint32_t *w, int nfib, int stride, int inner, uint32_t inf4)
 {
+    const uint32_t inf2 = inf4 & 0x00ff00ffu;
     // f / inner by a float reciprocal: f < 2^24, so the estimate is off by
     // at most one and one correction makes it exact
     const float rinv = 1.0f / (float)inner;
@@ -71,35 +75,51 @@ __device__ __forceinline__ void dt_pass4(uint32_t *w, int nfib, int q, int strid
         int o = (int)((float)f * rinv);
         int i = f - o * inner;
         if (i < 0) { o--; i += inner; } else if (i >= inner) { o++; i -= inner; }
-        uint32_t *b = w + o * q * stride + i;
-        uint32_t m = inf4, v[COV_MAXQ];
+        uint32_t *b = w + o * Q * stride + i;
+        uint32_t e[Q], d[Q];                     // bytes 0,2 and bytes 1,3 of each word
 #pragma unroll
-        for (int a = 0; a < COV_MAXQ; a++)
-            if (a < q) { v[a] = b[a * stride]; m = __vminu4(m, v[a]); }
-        const uint32_t c = __vminu4(__vadd4(m, 0x01010101u), inf4);
+        for (int a = 0; a < Q; a++) {
+            const uint32_t x = b[a * stride];
+            e[a] = __byte_perm(x, 0u, 0x4240);
+            d[a] = __byte_perm(x, 0u, 0x4341);
+        }
+        uint32_t me = e[0], md = d[0];
 #pragma unroll
-        for (int a = 0; a < COV_MAXQ; a++)
-            if (a < q) b[a * stride] = __vminu4(v[a], c);
+        for (int a = 1; a + 1 < Q; a += 2) {
+            me = __vimin3_u16x2(me, e[a], e[a + 1]);
+            md = __vimin3_u16x2(md, d[a], d[a + 1]);
+        }
+        if ((Q & 1) == 0) {
+            me = __vminu2(me, e[Q - 1]);
+            md = __vminu2(md, d[Q - 1]);
+        }
+        const uint32_t ce = __viaddmin_u16x2(me, 0x00010001u, inf2);
+        const uint32_t cd = __viaddmin_u16x2(md, 0x00010001u, inf2);
+#pragma unroll
+        for (int a = 0; a < Q; a++)
+            b[a * stride] = __byte_perm(__vminu2(e[a], ce), __vminu2(d[a], cd), 0x6240);
     }
 }
 
-// Pass 1: tiles of T = q^k contiguous words (the low k axes), from the code
-// bitmap.  In shared memory a tile is T/q rows -- the q words of one line of
-// the lowest axis -- each padded to Q4 = 4*ceil(q/4) bytes, so that every
-// axis above the lowest moves whole 32-bit words.  The lowest axis is taken
-// while loading: a word is 0 on the code, 1 if its line holds a codeword,
-// else n+1.  When k == n this is the whole transform and the histogram is
-// taken here.
+// Pass 1: tiles of T = Q^k contiguous words (the low k axes), from the code
+// bitmap.  In shared memory a tile is T/Q rows -- the Q words of one line of
+// the lowest axis -- each padded to 4*ceil(Q/4) bytes, so that every axis
+// above the lowest moves whole 32-bit words.  The lowest axis is taken while
+// loading: a word is 0 on the code, 1 if its line holds a codeword, else
+// n+1.  When k == n this is the whole transform and the histogram is taken
+// here.
+template <int Q>
 __global__ void __launch_bounds__(DT_NT_BIG)
 k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__ D,
          unsigned long long *hist)
 {
     extern __shared__ __align__(16) uint32_t dt_w[];
     __shared__ int sh[COV_MAXN + 2];
-    const int q = g.q;
-    const uint32_t T = g.pw[k];
-    const int rows = (int)(T / (uint32_t)q);
-    const int wpr = (q + 3) >> 2;                 // 32-bit words per row
+    constexpr int WPR = (Q + 3) >> 2;            // 32-bit words per row
+    constexpr uint32_t RB = 4u * WPR;            // padded row bytes
+    uint32_t T = 1;
+    for (int j = 0; j < k; j++) T *= (uint32_t)Q;
+    const int rows = (int)(T / (uint32_t)Q);
     const uint32_t inf = (uint32_t)g.inf, inf4 = inf * 0x01010101u;
     const uint32_t ntile = g.N / T;
     const bool last = (k == g.n) && hist != nullptr;
@@ -109,50 +129,51 @@ k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__
         const uint32_t x0 = tile * T;
         __syncthreads();
         for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const uint32_t xr = x0 + (uint32_t)r * (uint32_t)q;
-            // q bits of the row from at most two bitmap words
+            const uint32_t xr = x0 + (uint32_t)r * (uint32_t)Q;
+            // Q bits of the row from at most two bitmap words
             const uint32_t lo = __ldg(&bm[xr >> 5]);
-            const uint32_t hi = ((xr & 31) + (uint32_t)q > 32) ? __ldg(&bm[(xr >> 5) + 1]) : 0u;
-            const uint64_t bits = ((((uint64_t)hi << 32) | lo) >> (xr & 31)) & ((1ull << q) - 1);
+            const uint32_t hi = ((xr & 31) + (uint32_t)Q > 32) ? __ldg(&bm[(xr >> 5) + 1]) : 0u;
+            const uint32_t bits = (uint32_t)(((((uint64_t)hi << 32) | lo) >> (xr & 31)) & ((1ull << Q) - 1));
             const uint32_t fill = bits ? 1u : inf;
-            for (int w = 0; w < wpr; w++) {
+#pragma unroll
+            for (int w = 0; w < WPR; w++) {
                 uint32_t v = 0;
+#pragma unroll
                 for (int b = 0; b < 4; b++) {
                     const int a = 4 * w + b;
-                    const uint32_t byte = a >= q ? inf : (((bits >> a) & 1) ? 0u : fill);
+                    const uint32_t byte = a >= Q ? inf : (((bits >> a) & 1u) ? 0u : fill);
                     v |= byte << (8 * b);
                 }
-                dt_w[r * wpr + w] = v;
+                dt_w[r * WPR + w] = v;
             }
         }
         __syncthreads();
-        for (int j = 1; j < k; j++) {          // rows of axis j: stride q^(j-1) rows
-            const int inner = (int)g.pw[j - 1] * wpr;
-            dt_pass4(dt_w, rows / q * wpr, q, inner, inner, inf4);
+        int inner = WPR;                       // rows of axis j: stride Q^(j-1) rows
+        for (int j = 1; j < k; j++, inner *= Q) {
+            dt_pass4<Q>(dt_w, rows / Q * WPR, inner, inner, inf4);
             __syncthreads();
         }
         // out: the tile is T contiguous bytes of D; the 4-byte-aligned
-        // interior goes out as whole words (byte b of the tile is row b / q,
-        // column b % q of the padded rows), the unaligned ends as bytes
+        // interior goes out as whole words (byte b of the tile is row b / Q,
+        // column b % Q of the padded rows), the unaligned ends as bytes
         const uint32_t head = min((4u - (uint32_t)(reinterpret_cast<uintptr_t>(D + x0) & 3u)) & 3u, T);
         const uint32_t nw = (T - head) >> 2;
-        const int rb = wpr * 4;                   // padded row bytes
         for (uint32_t e = threadIdx.x; e < head + ((T - head) & 3u); e += blockDim.x) {
             const uint32_t b = e < head ? e : head + 4 * nw + (e - head);
-            const uint32_t r = b / (uint32_t)q;
-            const uint8_t v = dt_b[r * rb + (b - r * (uint32_t)q)];
+            const uint32_t r = b / (uint32_t)Q;
+            const uint8_t v = dt_b[r * RB + (b - r * (uint32_t)Q)];
             D[x0 + b] = v;
             if (last) dt_hist_add(sh, v);
         }
         for (uint32_t wi = threadIdx.x; wi < nw; wi += blockDim.x) {
             const uint32_t b0 = head + 4 * wi;
-            uint32_t r = b0 / (uint32_t)q, a = b0 - r * (uint32_t)q, v = 0;
+            uint32_t r = b0 / (uint32_t)Q, a = b0 - r * (uint32_t)Q, v = 0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const uint32_t byte = dt_b[r * rb + a];
-                v |= byte << (8 * k);
+            for (int t = 0; t < 4; t++) {
+                const uint32_t byte = dt_b[r * RB + a];
+                v |= byte << (8 * t);
                 if (last) dt_hist_add(sh, (int)byte);
-                if (++a == (uint32_t)q) { a = 0; r++; }
+                if (++a == (uint32_t)Q) { a = 0; r++; }
             }
             *reinterpret_cast<uint32_t *>(D + x0 + b0) = v;
         }
@@ -162,11 +183,23 @@ k_dt_low(DtGeom g, int k, const uint32_t *__restrict__ bm, uint8_t *__restrict__
         atomicAdd(&hist[threadIdx.x], (unsigned long long)sh[threadIdx.x]);
 }
 
-// Pass 2+: the axes of group [j0, j0+gsz) (in-word strides q^j0 .. ), for a
+// the aligned 32-bit word that holds byte p
+__device__ __forceinline__ uint32_t *dt_word_of(uint8_t *p)
+{
+    return reinterpret_cast<uint32_t *>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)3);
+}
+
+// Pass 2+: the axes of group [j0, j0+gsz) (in-word strides Q^j0 .. ), for a
 // strip of W = 32 << lw consecutive positions below the group: rows of W
 // bytes, W/4 words, so each pass moves whole words.  W is as wide as the
-// shared memory allows for the group's q^gsz rows, so that a group of few
+// shared memory allows for the group's Q^gsz rows, so that a group of few
 // rows (the last axes of a long word) still moves long contiguous runs.
+// A row starts at any byte (the strides are powers of Q), so it is moved
+// as 32-bit words: each loaded word is two aligned words funnel-shifted by
+// the row's misalignment (the second only when it holds bytes of the row),
+// and each row goes out as aligned words plus at most three bytes at either
+// end.  Every word touched holds a byte of the row, so no access leaves it.
+template <int Q>
 __global__ void __launch_bounds__(DT_NT)
 k_dt_high(DtGeom g, int j0, int gsz, int lw, int last_, uint8_t *__restrict__ D, unsigned long long *hist)
 {
@@ -174,52 +207,90 @@ k_dt_high(DtGeom g, int j0, int gsz, int lw, int last_, uint8_t *__restrict__ D,
     extern __shared__ __align__(16) uint32_t dt_w[];
     __shared__ int sh[COV_MAXN + 2];
     const int lwb = lw + 5;                      // log2 of the strip width in bytes
+    const int lww = lwb - 2;                     // log2 of the words per row
     const uint32_t W = 1u << lwb;
-    const int WW = (int)(W >> 2);                // words per row
+    const uint32_t WW = W >> 2;
     uint8_t *dt_b = reinterpret_cast<uint8_t *>(dt_w);
     const uint32_t inf4 = (uint32_t)g.inf * 0x01010101u;
-    const uint32_t s = g.pw[j0];                 // stride of the lowest axis in the group
-    const uint32_t rows = g.pw[gsz];
+    uint32_t s = 1;                              // stride of the lowest axis in the group
+    for (int j = 0; j < j0; j++) s *= (uint32_t)Q;
+    uint32_t rows = 1;
+    for (int j = 0; j < gsz; j++) rows *= (uint32_t)Q;
     const uint32_t span = rows * s;              // words spanned by one value of the outer digits
     const uint32_t outer = g.N / span;
     const uint32_t nstrip = (s + W - 1) >> lwb;
     const unsigned long long ntiles = (unsigned long long)outer * nstrip;
     if (threadIdx.x < COV_MAXN + 2) sh[threadIdx.x] = 0;
+    const uint32_t totw = rows << lww;
     for (unsigned long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint32_t o = (uint32_t)(tile / nstrip);
         const uint32_t c0 = (uint32_t)(tile - (unsigned long long)o * nstrip) << lwb;
-        const uint32_t w = min(W, s - c0);
-        const uint32_t base = o * span + c0;
+        const uint32_t w = min(W, s - c0);       // bytes of each row in this strip
+        uint8_t *const Db = D + (size_t)o * span + c0;
         __syncthreads();
-        // element (row r, column c) at base + r*s + c, kept at byte r*W + c;
-        // eight loads of a thread in flight before their stores
-        const uint32_t tot = rows << lwb;
-        for (uint32_t e0 = threadIdx.x; e0 < tot; e0 += 8 * blockDim.x) {
-            uint8_t v[8];
+        // word k of row r: bytes 4k..4k+3 of the row at Db + r*s (n+1
+        // past w); eight words of a thread in flight before their stores
+        for (uint32_t e0 = threadIdx.x; e0 < totw; e0 += 8 * blockDim.x) {
+            uint32_t v[8];
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const uint32_t e = e0 + (uint32_t)u * blockDim.x;
-                const uint32_t r = e >> lwb, c = e & (W - 1);
-                v[u] = (e < tot && c < w) ? D[base + r * s + c] : (uint8_t)g.inf;
+                const uint32_t r = e >> lww, c = (e & (WW - 1)) << 2;
+                v[u] = inf4;
+                if (e < totw && c < w) {
+                    uint8_t *p = Db + (size_t)r * s + c;
+                    const uint32_t m = (uint32_t)(reinterpret_cast<uintptr_t>(p) & 3u);
+                    const uint32_t need = min(4u, w - c);
+                    const uint32_t *pa = dt_word_of(p);
+                    const uint32_t lo = pa[0];
+                    const uint32_t hi = m + need > 4u ? pa[1] : 0u;
+                    uint32_t x = __funnelshift_r(lo, hi, 8u * m);
+                    if (need < 4u) {
+                        const uint32_t keep = (1u << (8u * need)) - 1u;
+                        x = (x & keep) | (inf4 & ~keep);
+                    }
+                    v[u] = x;
+                }
             }
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const uint32_t e = e0 + (uint32_t)u * blockDim.x;
-                if (e < tot) dt_b[e] = v[u];
+                if (e < totw) dt_w[e] = v[u];
             }
         }
         __syncthreads();
-        for (int j = 0; j < gsz; j++) {          // row stride q^j
-            const int inner = (int)g.pw[j] * WW;
-            dt_pass4(dt_w, (int)(rows / (uint32_t)g.q) * WW, g.q, inner, inner, inf4);
+        int inner = (int)WW;                     // row stride Q^j
+        for (int j = 0; j < gsz; j++, inner *= Q) {
+            dt_pass4<Q>(dt_w, (int)(rows / (uint32_t)Q) * (int)WW, inner, inner, inf4);
             __syncthreads();
         }
-        for (uint32_t e = threadIdx.x; e < tot; e += blockDim.x) {
-            const uint32_t r = e >> lwb, c = e & (W - 1);
-            if (c < w) {
-                uint8_t v = dt_b[e];
-                D[base + r * s + c] = v;
-                if (last) dt_hist_add(sh, v);
+        // out: row r's aligned words from its first 4-byte boundary on, then
+        // the ends (at most 3 bytes each) by the thread of the row's last word
+        for (uint32_t e = threadIdx.x; e < totw; e += blockDim.x) {
+            const uint32_t r = e >> lww, k = e & (WW - 1);
+            uint8_t *p0 = Db + (size_t)r * s;
+            const uint32_t head = min((4u - (uint32_t)(reinterpret_cast<uintptr_t>(p0) & 3u)) & 3u, w);
+            const uint32_t nwr = (w - head) >> 2;
+            if (k < nwr) {
+                const uint32_t lo = dt_w[(r << lww) + k];
+                const uint32_t hi = head ? dt_w[(r << lww) + k + 1] : 0u;
+                const uint32_t x = __funnelshift_r(lo, hi, 8u * head);
+                *reinterpret_cast<uint32_t *>(p0 + head + 4 * k) = x;
+                if (last) {
+#pragma unroll
+                    for (int b = 0; b < 4; b++) dt_hist_add(sh, (int)((x >> (8 * b)) & 0xffu));
+                }
+            }
+            if (k == WW - 1) {
+                const uint8_t *row = dt_b + ((size_t)r << lwb);
+                for (uint32_t b = 0; b < head; b++) {
+                    p0[b] = row[b];
+                    if (last) atomicAdd(&sh[row[b]], 1);
+                }
+                for (uint32_t b = head + 4 * nwr; b < w; b++) {
+                    p0[b] = row[b];
+                    if (last) atomicAdd(&sh[row[b]], 1);
+                }
             }
         }
     }
@@ -227,6 +298,46 @@ k_dt_high(DtGeom g, int j0, int gsz, int lw, int last_, uint8_t *__restrict__ D,
     if (last && threadIdx.x < g.n + 2 && sh[threadIdx.x])
         atomicAdd(&hist[threadIdx.x], (unsigned long long)sh[threadIdx.x]);
 }
+
+// the transform kernels of every q, for a runtime q
+template <template <int> class F, class... A>
+int dt_for_q(int q, A... a)
+{
+    switch (q) {
+    case 2: return F<2>::run(a...);   case 3: return F<3>::run(a...);   case 4: return F<4>::run(a...);
+    case 5: return F<5>::run(a...);   case 6: return F<6>::run(a...);   case 7: return F<7>::run(a...);
+    case 8: return F<8>::run(a...);   case 9: return F<9>::run(a...);   case 10: return F<10>::run(a...);
+    case 11: return F<11>::run(a...); case 12: return F<12>::run(a...); case 13: return F<13>::run(a...);
+    case 14: return F<14>::run(a...); case 15: return F<15>::run(a...); case 16: return F<16>::run(a...);
+    default: return COV_EINVAL;
+    }
+}
+
+template <int Q> struct DtAttrs {
+    static int run()
+    {
+        if (cudaFuncSetAttribute(k_dt_low<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_TILE_BIG) != cudaSuccess ||
+            cudaFuncSetAttribute(k_dt_high<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_STRIP_MAX) != cudaSuccess)
+            return -(100 + (int)cudaGetLastError());
+        return 0;
+    }
+};
+template <int Q> struct DtLow {
+    static int run(int grid, int nt, size_t smem, cudaStream_t st, DtGeom g, int k, const uint32_t *bm,
+                   uint8_t *D, unsigned long long *hist)
+    {
+        k_dt_low<Q><<<grid, nt, smem, st>>>(g, k, bm, D, hist);
+        return 0;
+    }
+};
+template <int Q> struct DtHigh {
+    static int run(int grid, size_t smem, cudaStream_t st, DtGeom g, int j0, int gsz, int lw, int last,
+                   uint8_t *D, unsigned long long *hist)
+    {
+        k_dt_high<Q><<<grid, DT_NT, smem, st>>>(g, j0, gsz, lw, last, D, hist);
+        return 0;
+    }
+};
 
 __global__ void k_count_above(const uint8_t *__restrict__ D, uint32_t N, int R, unsigned long long *out)
 {
@@ -466,8 +577,10 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
 {
     int dev = 0;
     if (!g_dt_attr.done(dev)) {
-        CK(cudaFuncSetAttribute(k_dt_low, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_TILE_BIG));
-        CK(cudaFuncSetAttribute(k_dt_high, cudaFuncAttributeMaxDynamicSharedMemorySize, DT_STRIP_MAX));
+        for (int q = 2; q <= COV_MAXQ; q++) {
+            const int rc = dt_for_q<DtAttrs>(q);
+            if (rc) return rc;
+        }
         g_dt_attr.set(dev);
     }
     CK(cudaMemsetAsync(d_bm, 0, (size_t)((g.N + 31) / 32) * 4, st));
@@ -500,7 +613,8 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
     const uint32_t ntile = g.N / g.pw[k];
     {
         int grid = (int)std::min<uint32_t>(ntile, (uint32_t)sms * (big ? 1 : 4));
-        k_dt_low<<<grid, big ? DT_NT_BIG : DT_NT, (size_t)low_bytes(k), st>>>(g, k, d_bm, d_D, d_hist);
+        dt_for_q<DtLow>(g.q, grid, big ? DT_NT_BIG : DT_NT, (size_t)low_bytes(k), st, g, k,
+                        (const uint32_t *)d_bm, d_D, d_hist);
         CK(cudaGetLastError());
     }
     // high groups
@@ -520,7 +634,7 @@ int dt_run(const DtGeom &g, const uint8_t *d_code, int M, uint8_t *d_D, unsigned
         const uint32_t W = (uint32_t)DT_STRIP_W << lw;
         const unsigned long long tiles = (unsigned long long)(g.N / (g.pw[gsz] * s)) * ((s + W - 1) / W);
         int grid = (int)std::min<unsigned long long>(tiles, (unsigned long long)sms * 4);
-        k_dt_high<<<grid, DT_NT, (size_t)g.pw[gsz] * W, st>>>(g, j0, gsz, lw, last, d_D, d_hist);
+        dt_for_q<DtHigh>(g.q, grid, (size_t)g.pw[gsz] * W, st, g, j0, gsz, lw, last, d_D, d_hist);
         CK(cudaGetLastError());
         j0 += gsz;
     }
@@ -559,8 +673,7 @@ int cov_mindist_dev(int32_t q, int32_t n, const uint8_t *d_code, int32_t M, uint
 //  * Limit: q^n <= COV_DT_STATIC_MAX_WORDS (2^26 words, an 8 MiB bitmap that
 //    every GPU which loads the library keeps until the process exits).
 //  * The first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current) and caches it; make
-//    that first call before any stream capture.
+//    (cudaGetSymbolAddress, with that device current) and caches it.
 //  * Every call uses the same array and clears it before use: two calls
 //    whose work overlaps on the GPU (different streams, no ordering) race.
 #define COV_DT_STATIC_MAX_WORDS (1u << 26)

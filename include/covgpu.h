@@ -281,7 +281,8 @@ int cov_lns_recount(cov_lns *h, const uint32_t *idx, int32_t m);
 /* map[x] = #{y : d(x,y) <= R, cnt[y] == target}: target 0 = gain, 1 = loss */
 int cov_lns_map(cov_lns *h, int32_t target);
 int cov_lns_map_max(cov_lns *h, int32_t *out);
-/* counts of map values v >= 1 in bins (v-1)*nbins/vmax, v capped at vmax */
+/* counts of map values v >= 1 in bins (v-1)*nbins/vmax, v capped at vmax;
+ * 1 <= nbins <= 8192 */
 int cov_lns_map_hist(cov_lns *h, int32_t nbins, int32_t vmax, int64_t *hist);
 /* positions with map >= thr in increasing index order (at most cap), and
  * how many there are */
@@ -330,9 +331,9 @@ int cov_finish(int32_t q, int32_t n, int32_t R, int32_t M, const uint8_t *code, 
  * allocate (their device memory belongs to another allocator, or they run
  * where an allocation is not allowed).  No counterpart in the reference.
  * Its one scratch buffer is a file-scope device array: q^n must be at most
- * 2^26 (else COV_ERANGE); the first call on a device looks the array up and
- * should come before any stream capture; calls that overlap on the GPU
- * share the array and race. */
+ * 2^26 (else COV_ERANGE); the first call on a device also looks up the
+ * array's device address on the host; calls that overlap on the GPU share
+ * the array and race. */
 int cov_mindist_dev_static(int32_t q, int32_t n, const uint8_t *d_code,
                            int32_t M, uint8_t *d_dist, void *stream);
 

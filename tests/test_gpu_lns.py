@@ -52,10 +52,11 @@ def test_primitives_exact(covlib, q, n, R, m):
         idx, val, found = e.map_extract(thr, 1 << 20)
         want = np.flatnonzero(gain >= thr)
         assert found == len(want) and (idx == want).all() and (val == gain[want]).all()
-        hist = e.map_hist(8, int(gain.max()) or 1)
-        v = gain[gain >= 1]
-        assert (hist == np.bincount((np.minimum(v, max(1, gain.max())) - 1) * 8 // max(1, gain.max()),
-                                    minlength=8)).all()
+        v = gain[gain >= 1].astype(np.int64)
+        # 32-bit binning, and the 64-bit one where (vmax-1) * nbins passes 2^32
+        for nb, vmax in ((8, int(gain.max()) or 1), (1024, 3), (8192, 600000)):
+            hist = e.map_hist(nb, vmax)
+            assert (hist == np.bincount((np.minimum(v, vmax) - 1) * nb // vmax, minlength=nb)).all(), (nb, vmax)
         probe = rng.integers(0, N, 9)
         assert (e.ball_count(probe, 0) == gain[probe]).all()
         e.loss_map()

@@ -60,3 +60,27 @@ def test_empty_code(covlib):
     dist, hist, rad = verify.mindist(np.zeros((0, 5), np.uint8), 3, 5)
     assert (dist == 6).all() and rad == 6 and hist[6] == 3 ** 5
     assert verify.verify(np.zeros((0, 5), np.uint8), 5, 3, 2, want_witness=False)[0] == 3 ** 5
+
+
+@pytest.mark.parametrize("q,n,M", [(5, 9, 300), (3, 13, 200), (7, 8, 400), (6, 8, 90), (2, 16, 500)])
+def test_transform_into_unaligned_output(covlib, q, n, M):
+    """cov_mindist_dev writing its words at byte offsets 0..3 of a device
+    buffer (rows of every pass start at any byte; the kernels move them as
+    aligned words plus edge bytes): every word equals the oracle's, and the
+    bytes around the output stay untouched."""
+    import torch
+    from coldcase_gb300.workloads import uniform_code
+    code = uniform_code(q, n, M, 5)
+    want = torch.from_numpy(po.mindist(code, q, n, threads=8))
+    dev = torch.device("cuda", 0)
+    d_code = torch.from_numpy(code).to(dev)
+    N = q ** n
+    buf = torch.empty(N + 8, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for off in range(4):
+        buf.fill_(0xA5)
+        assert covlib.cov_mindist_dev(q, n, d_code.data_ptr(), M, buf.data_ptr() + off, stream) == 0
+        torch.cuda.synchronize()
+        h = buf.cpu()
+        assert torch.equal(h[off:off + N], want), off
+        assert (h[:off] == 0xA5).all() and (h[off + N:] == 0xA5).all(), off
