@@ -866,26 +866,45 @@ def gpu_bench(args, rank, world, dist):
                                     read=1e3 * t_read / args.e2e_steps))
     pool.close()
 
-    # ---------------- plain: one instance, one wide cluster, same GPU
+    # ---------------- plain: one instance on the GPU: its cluster, with the
+    # commits of its moves shared by helper CTAs on the other SMs (grid help),
+    # and its cluster alone
     plain = None
     if not args.no_plain and rank == 0:
-        eng = Search(Q, N_, R_, M_, seed=seeds[0], tabu=TENURE, cluster=args.plain_cluster, budget_s=120.0)
-        eng.load(codes[0])
-        ps = torch.cuda.Stream(device=dev)
-        eng.pool.set_stream(ps.cuda_stream)
-        for _ in range(args.warmup):
-            eng.pool.run(args.plain_moves)
-        i0 = eng.status()["it"]
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(ps)
-        for _ in range(args.steps):
-            eng.pool.run_async(args.plain_moves)
-        b.record(ps)
-        ps.synchronize()
-        pm = eng.status()["it"] - i0
-        plain = dict(value=pm / (a.elapsed_time(b) / 1e3), unit="moves/s", cluster=args.plain_cluster,
-                     moves=pm)
-        eng.close()
+        runs = {}
+        for help_ in ((args.plain_help, 0) if args.plain_help else (0,)):
+            eng = Search(Q, N_, R_, M_, seed=seeds[0], tabu=TENURE, cluster=args.plain_cluster, budget_s=120.0)
+            if help_:
+                eng.pool.set_param("grid_help", help_)
+            eng.load(codes[0])
+            ps = torch.cuda.Stream(device=dev)
+            eng.pool.set_stream(ps.cuda_stream)
+            for _ in range(args.warmup):
+                eng.pool.run(args.plain_moves)
+            i0 = eng.status()["it"]
+            p0 = eng.pool.prof(eng.slot)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(ps)
+            for _ in range(args.steps):
+                eng.pool.run_async(args.plain_moves)
+            b.record(ps)
+            ps.synchronize()
+            st = eng.status()
+            if st["status"] != 0:
+                raise RuntimeError("plain engine status %d" % st["status"])
+            pm = st["it"] - i0
+            p1 = eng.pool.prof(eng.slot)
+            # the phase counters are SM cycles: at the clock sampled under the batched leg
+            mhz = (clocks.get("sm_mhz") or 2070.0) if isinstance(clocks, dict) else 2070.0
+            us = {k: round((p1[k] - p0[k]) / (mhz * pm), 2) for k in eng.pool.PROF_NAMES if p1[k] > p0[k]}
+            runs[help_] = dict(value=pm / (a.elapsed_time(b) / 1e3), unit="moves/s", cluster=args.plain_cluster,
+                               grid_help=help_, moves=pm, us_per_move=us)
+            eng.close()
+        plain = dict(runs[args.plain_help])
+        if args.plain_help:
+            plain["cluster_only"] = runs[0]
+            plain["note"] = ("one instance: the leader's serial steps on its cluster, each move's commit shared "
+                             "with helper CTAs on the SMs the cluster leaves free")
 
     # ---------------- the other plain configurations (one instance each)
     plain_cfgs = None
@@ -1062,6 +1081,8 @@ def main():
     ap.add_argument("--cluster", type=int, default=2, help="CTAs per restart (batched)")
     ap.add_argument("--plain-cluster", type=int, default=16)
     ap.add_argument("--plain-moves", type=int, default=1000)
+    ap.add_argument("--plain-help", type=int, default=64,
+                    help="helper clusters that share the plain instance's commits (0: its cluster alone)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-moves", type=int, default=100,
                     help="moves per reference-engine process per step (CPU baselines and the reference arm)")

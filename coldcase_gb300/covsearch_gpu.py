@@ -30,13 +30,13 @@ from .lib import CovError
 USAGE = ("usage: covsearch -q Q -n N -R R -M M [-t sec] [-s seed] [--in f] [--out f]\n"
          "                 [--cand K] [--tabu T] [--kick K] [--noise PERMILLE] [--iters I]\n"
          "                 [--stall S] [--sa --t0 T0 --cool C --tmin TMIN]\n"
-         "                 [--random-init] [--wide] [--fix0]\n"
+         "                 [--random-init] [--wide] [--fix0] [--grid-help K]\n"
          "                 [--threads T] [--quiet]\n")
 
 PRESETS = {"base", "p1", "p2", "p2b", "p3", "p4", "p5", "best", "p5b"}
 VALUE_FLAGS = {"-q", "-n", "-R", "-M", "-t", "-s", "--in", "--out", "--cand", "--tabu", "--kick",
                "--noise", "--iters", "--stall", "--threads", "--t0", "--cool", "--tmin", "--st",
-               "--eval", "--walk", "--target", "--cpu", "--preset", "--cluster", "--chunk"}
+               "--eval", "--walk", "--target", "--cpu", "--preset", "--cluster", "--chunk", "--grid-help"}
 SPEED_SWITCHES = {"--hoist", "--early", "--pf", "--huge"}
 TRAJECTORY_SWITCHES = {"--sa", "--ucache", "--upick"}
 
@@ -44,7 +44,7 @@ TRAJECTORY_SWITCHES = {"--sa", "--ucache", "--upick"}
 def parse(argv):
     a = dict(q=0, n=0, R=-1, M=0, t=60.0, s=12345, inp=None, out=None, cand=100000, tabu=0,
              kick=2, noise=0, iters=-1, stall=5000, random_init=False, quiet=False, target=-1,
-             cluster=None, chunk=0, wide=False, fix0=False)
+             cluster=None, chunk=0, wide=False, fix0=False, grid_help=0)
     i = 0
     while i < len(argv):
         f = argv[i]
@@ -68,6 +68,7 @@ def parse(argv):
             elif f == "--target": a["target"] = int(v)
             elif f == "--cluster": a["cluster"] = int(v)
             elif f == "--chunk": a["chunk"] = int(v)
+            elif f == "--grid-help": a["grid_help"] = int(v)
             elif f == "--preset" and v not in PRESETS:
                 sys.stderr.write("unknown preset %s\n" % v)
                 return None, 2
@@ -135,6 +136,9 @@ def main(argv=None):
     try:
         eng = Search(q, n, R, M, seed=a["s"], tabu=a["tabu"], kick=a["kick"], stall=a["stall"],
                      cand=a["cand"], cluster=cluster, wide=a["wide"], fix0=a["fix0"])
+        if a["grid_help"]:
+            # this process's search takes the whole GPU: helper clusters share its commits
+            eng.pool.set_param("grid_help", a["grid_help"])
         unc0 = eng.load(code, random_init=a["random_init"])
     except CovError as e:
         sys.stderr.write("covsearch_gpu: %s\n" % e)

@@ -156,7 +156,8 @@ struct CovSlotState {
     // 0 pick, 1 candidates + sample, 2 entering side, 3 select, 4 move op
     // (commit + sphere), 5 finish, 6 list compaction, 7 other ops
     long long it_limit;          // iteration count at which the slot stops (-1: none)
-    unsigned long long prof[24];   // 8..19: sub-phases (diagnostics); 20: sum of candidate
+    unsigned long long prof[24];   // 8..19: sub-phases (diagnostics: 11 RNG refill in the move op,
+                                   // 12 wait for helper CTAs, 15 move op up to that wait); 20: sum of candidate
                                    // codewords, 21: sum of list lengths, 22: planned moves
 };
 

@@ -48,6 +48,8 @@ namespace cg = cooperative_groups;
 #define RS        1024         // RNG stream ring (draws generated ahead)
 #define RS_CKI    128          // a generator checkpoint every RS_CKI draws
 #define RS_NCK    16           // checkpoints kept (RS_NCK * RS_CKI > RS + RS_CKI)
+static_assert(RS % RS_CKI == 0 && (RS & (RS - 1)) == 0 && (RS_CKI & (RS_CKI - 1)) == 0,
+              "RNG ring: powers of two, whole checkpoint blocks");
 #define INV_N     1024         // moduli with a reciprocal in shared memory
 #define CODE_SM   2048         // codewords mirrored in every CTA's shared memory
 #define NEG_CLUSTER_PAIRS 4096  // list x candidate pairs above which the whole cluster helps
@@ -75,14 +77,37 @@ struct OpParams {
     int wide;                  // OP_NEG counts every (candidate, position, value) into g_negw
 };
 
+// Sums of one op over the CTAs that share it: the change of the uncovered
+// count and of the moved codeword's private counts T / H.
+struct MoveAcc {
+    unsigned long long dunc;
+    int accT;
+    int accH[COV_MAXN];
+};
+
+// One search instance's moves shared with helper CTAs outside its cluster
+// (one instance on the whole GPU): the search cluster publishes each move
+// here, the helpers take their share of its commit, add their sums to `acc`
+// and count themselves in `done`.  Zeroed before every launch.
+struct GridHelp {
+    unsigned int seq;          // moves published in this launch
+    unsigned int done;         // helper CTAs finished with the current move
+    int stop;                  // the search cluster has left: helpers leave
+    int code_gen;              // codeword changes other than moves (kicks) so far
+    OpParams op;
+    MoveAcc acc;
+};
+
 struct Smem {
     CovSlot slot;              // this CTA's copy of the slot descriptor
     OpParams opp;              // written by the leader
     OpParams opl;              // each CTA's local copy
-    // leader accumulators (targets of DSMEM atomics)
-    unsigned long long dunc;
-    int accT;
-    int accH[COV_MAXN];
+    MoveAcc acc;               // leader accumulators (targets of DSMEM atomics)
+    unsigned int gh_seq;       // moves published to the helpers (leader)
+    int gh_got;                // helper: 1 a move to share, 0 leave
+    int code_cached;           // code_sm mirrors the code
+    int code_gen;              // leader: codeword changes other than moves; helper: the last one seen
+    int gh_reload;             // helper: reload code_sm before the move
     // per-CTA partials
     int partT;
     int partH[COV_MAXN];
@@ -205,6 +230,18 @@ __device__ __forceinline__ long long cov_clock()
     return t;
 }
 
+// gpu-scope acquire load / release store of a 32-bit flag
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
 // The launch deadline is kept in SM cycles (read through cov_clock): a
 // %globaltimer read can stall the reading warp for tens of microseconds,
 // which is too slow for a check made every iteration.
@@ -297,13 +334,20 @@ __device__ __forceinline__ void rs_fill(Smem &S, unsigned long long limit)
     unsigned long long g = S.rs_gen;
     if (g >= limit) return;
     CovRng st = S.rs_state;
-    for (; g < limit; g++) {
-        if ((g % RS_CKI) == 0) {
+    while (g < limit) {
+        if ((g & (RS_CKI - 1)) == 0) {
             const int k = (int)((g / RS_CKI) % RS_NCK);
             S.rs_ck[k] = st;
             S.rs_ckpos[k] = g;
         }
-        S.rs_buf[g % RS] = cov_rng_next(st);
+        // the draws up to the next checkpoint: RS is a multiple of RS_CKI,
+        // so their ring slots are consecutive
+        const unsigned long long nxt = min(limit, (g | (unsigned long long)(RS_CKI - 1)) + 1ull);
+        uint64_t *buf = S.rs_buf + ((uint32_t)g & (RS - 1));
+        const uint32_t cnt = (uint32_t)(nxt - g);
+#pragma unroll 4
+        for (uint32_t k = 0; k < cnt; k++) buf[k] = cov_rng_next(st);
+        g = nxt;
     }
     S.rs_state = st;
     S.rs_gen = g;
@@ -433,8 +477,8 @@ __device__ __forceinline__ void private_adjust(const CovSlot &d, int k, uint64_t
 {
     if (k < 0 || k >= d.M) { set_error(d, COV_EDRIFT); return; }
     extern __shared__ __align__(16) unsigned char cov_smem[];
-    const uint64_t ck = d.M <= CODE_SM ? reinterpret_cast<const Smem *>(cov_smem)->code_sm[k]
-                                       : cov_ldcg(&d.code[k]);
+    const Smem *Sm = reinterpret_cast<const Smem *>(cov_smem);
+    const uint64_t ck = d.M <= CODE_SM && Sm->code_cached ? Sm->code_sm[k] : cov_ldcg(&d.code[k]);
     uint64_t D = cov_spread(pkw ^ ck);
     if (__popcll(D) != d.R) return;
     int32_t *Pk = nullptr;
@@ -476,8 +520,8 @@ __device__ __forceinline__ void warp_private_adjust_slow(const CovSlot &d, const
         if (k < 0 || k >= d.M) {
             set_error(d, COV_EDRIFT);
         } else {
-            const uint64_t ck = d.M <= CODE_SM ? reinterpret_cast<const Smem *>(cov_smem)->code_sm[k]
-                                               : cov_ldcg(&d.code[k]);
+            const Smem *Sm = reinterpret_cast<const Smem *>(cov_smem);
+            const uint64_t ck = d.M <= CODE_SM && Sm->code_cached ? Sm->code_sm[k] : cov_ldcg(&d.code[k]);
             D = cov_spread(pkw ^ ck);
             on = __popcll(D) == d.R;
         }
@@ -616,7 +660,7 @@ __device__ __forceinline__ uint32_t sphere_items(const CovSlot &d, int r, int ns
 
 // the CTA's share of a change in the uncovered count: reduced in the CTA,
 // then one atomic into the leader's shared memory
-__device__ __forceinline__ void cta_add_dunc(long long dunc, Smem *LS)
+__device__ __forceinline__ void cta_add_dunc(long long dunc, MoveAcc *acc)
 {
     __shared__ long long cta_dunc;
     if (threadIdx.x == 0) cta_dunc = 0;
@@ -625,7 +669,7 @@ __device__ __forceinline__ void cta_add_dunc(long long dunc, Smem *LS)
     dunc = warp_sum(dunc);
     if ((threadIdx.x & 31) == 0 && dunc != 0) atomicAdd((unsigned long long *)&cta_dunc, (unsigned long long)dunc);
     cov_bar();
-    if (threadIdx.x == 0 && cta_dunc != 0) atomicAdd(&LS->dunc, (unsigned long long)cta_dunc);
+    if (threadIdx.x == 0 && cta_dunc != 0) atomicAdd(&acc->dunc, (unsigned long long)cta_dunc);
 }
 
 // add v to the shared counter of every position of a subset, once per group
@@ -781,9 +825,15 @@ __device__ __forceinline__ void commit_pairs_warp(const CovSlot &d, const OpPara
     }
 }
 
+// part / parts: this CTA's share of the move among all CTAs that take one
+// (the search cluster first, then any helper CTAs); acc receives the sums
+// (the leader's shared memory, or the helpers' global accumulator).  With
+// lead set the leader CTA (part 0) takes no share: its warp 0 generates the
+// next draws of the RNG stream with the SM to itself, which with helper CTAs
+// is the longest task of a move.
 template <bool WARP>
-__device__ __forceinline__ void op_move_t(const CovSlot &d, const OpParams &P, Smem &S, Smem *LS, int rank,
-                                          int csize)
+__device__ __forceinline__ void op_move_t(const CovSlot &d, const OpParams &P, Smem &S, MoveAcc *acc, int part,
+                                          int parts, bool lead = false)
 {
     const int R = d.R, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) S.partT = 0;
@@ -805,14 +855,22 @@ __device__ __forceinline__ void op_move_t(const CovSlot &d, const OpParams &P, S
     int T = 0;
     // the leader's warp 0 generates RNG draws for the next iterations while
     // every other warp of the cluster shares the move
-    const int gw = rank * NWARP + (int)(threadIdx.x >> 5) - 1;
+    const int warp = (int)(threadIdx.x >> 5);
+    // with lead the share of the CTAs is interleaved (warp-major), so that a
+    // move with fewer items than warps spreads its gathers over every SM
+    const int gw = !lead ? part * NWARP + warp - 1 : part == 0 ? (warp == 0 ? -1 : -2) : warp * (parts - 1) + part - 1;
     const uint32_t wid = (uint32_t)max(gw, 0);
-    const uint32_t wstride = (uint32_t)(csize * NWARP - 1) * 32;
+    const uint32_t wstride = (uint32_t)(lead ? (parts - 1) * NWARP : parts * NWARP - 1) * 32;
+    const int p0 = lead ? 1 : 0;                 // the part whose thread 32 takes the single-word steps
     if (gw < 0) {
-        if (threadIdx.x == 0) rs_fill(S, S.rs_use + RS);
+        if (gw == -1 && threadIdx.x == 0) {
+            const long long t0 = cov_clock();
+            rs_fill(S, S.rs_use + RS);
+            S.prof[11] += cov_clock() - t0;
+        }
         __syncwarp();
     } else if (R == 0) {
-        if (rank == 0 && threadIdx.x == 32) {
+        if (part == p0 && threadIdx.x == 32) {
             const uint32_t oa = cov_ldcg(&d.cw[P.base]);
             const uint32_t ob = cov_ldcg(&d.cw[P.base + P.dv]);
             T -= (oa & 0xffffu) == 1;
@@ -827,7 +885,7 @@ __device__ __forceinline__ void op_move_t(const CovSlot &d, const OpParams &P, S
         const int qm1 = d.q - 1;
         // X / Y pairs: (R-1)-subsets avoiding p
         if (R == 1) {
-            if (rank == 0 && threadIdx.x == 32) {
+            if (part == p0 && threadIdx.x == 32) {
                 const int dy = (int)((cov_ldcg(&d.cw[P.base]) & 0xffffu) == 1) -
                                (int)((cov_ldcg(&d.cw[P.base + P.dv]) & 0xffffu) == 1);
                 T += dy;
@@ -866,12 +924,12 @@ __device__ __forceinline__ void op_move_t(const CovSlot &d, const OpParams &P, S
             }
         }
     }
-    cta_add_dunc(dunc, LS);
+    cta_add_dunc(dunc, acc);
     T = warp_sum(T);
     if (lane == 0 && T) atomicAdd(&S.partT, T);
     cov_bar();
-    if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
-    if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
+    if (threadIdx.x == 0 && S.partT) atomicAdd(&acc->accT, S.partT);
+    if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&acc->accH[threadIdx.x], S.partH[threadIdx.x]);
     // private-count deltas of this CTA to P
     if (WARP) for (int e = threadIdx.x; e < tab.hs * tab.w; e += NT) {
         const int v = tab.cnt[e];
@@ -928,8 +986,8 @@ __device__ void op_recompute(const CovSlot &d, uint32_t base, uint64_t pc, Smem 
     }
     if (lane == 0 && T) atomicAdd(&S.partT, T);
     cov_bar();
-    if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->accT, S.partT);
-    if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->accH[threadIdx.x], S.partH[threadIdx.x]);
+    if (threadIdx.x == 0 && S.partT) atomicAdd(&LS->acc.accT, S.partT);
+    if (threadIdx.x < d.n && S.partH[threadIdx.x]) atomicAdd(&LS->acc.accH[threadIdx.x], S.partH[threadIdx.x]);
 }
 
 // +1 / -1 over the whole radius-R ball of codeword i: covsearch2e.c:353-380
@@ -960,7 +1018,7 @@ __device__ void op_ball(const CovSlot &d, const OpParams &P, Smem *LS, int rank,
             else dunc += word_inc(d, P.mi, w, pk);
         }
     }
-    cta_add_dunc(dunc, LS);
+    cta_add_dunc(dunc, &LS->acc);
 }
 
 // Entering-side counts by walking, used while the uncovered list is not
@@ -1502,9 +1560,9 @@ __device__ void fy_parallel(Smem &S, int take, int ncand)
 
 __device__ void zero_acc(Smem &S)
 {
-    if (threadIdx.x == 0) { S.dunc = 0; S.accT = 0; }
+    if (threadIdx.x == 0) { S.acc.dunc = 0; S.acc.accT = 0; }
     __syncwarp();
-    if (threadIdx.x < COV_MAXN) S.accH[threadIdx.x] = 0;
+    if (threadIdx.x < COV_MAXN) S.acc.accH[threadIdx.x] = 0;
 }
 
 // Plan one iteration up to the point where the entering-side counts are
@@ -2001,14 +2059,14 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
     const int n = d.n, q = d.q;
     const long long t0 = cov_clock();
     if (tid == 0) {
-        long long dunc = (long long)S.dunc;
+        long long dunc = (long long)S.acc.dunc;
         S.unc += dunc;
         if (dunc != S.chosen_delta) S.status = COV_EDRIFT;
         const OpParams &o = S.opp;
         leader_set_code(d, S, o.mi, o.pcn);
         int32_t *Pk = d.P + (size_t)o.mi * (n + 1);
-        cov_stcg(&Pk[0], cov_ldcg(&Pk[0]) + S.accT);
-        for (int j = 0; j < n; j++) cov_stcg(&Pk[1 + j], cov_ldcg(&Pk[1 + j]) + S.accH[j]);
+        cov_stcg(&Pk[0], cov_ldcg(&Pk[0]) + S.acc.accT);
+        for (int j = 0; j < n; j++) cov_stcg(&Pk[1 + j], cov_ldcg(&Pk[1 + j]) + S.acc.accH[j]);
         const int oldv = S.ibc[3];
         uint64_t r4 = rs_take(S) % 4ull;
         cov_stcg(&d.tabu[((size_t)o.mi * n + o.mp) * q + oldv], (int32_t)(S.it + d.tenure + (long long)r4));
@@ -2078,7 +2136,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                     OpParams &o = S.opp;
                     o.op = OP_BALL; o.sgn = -1; o.mi = i; o.pc = pk; o.base = widx_pk(d, pk);
                     o.ul_valid = S.ul_valid;
-                    S.dunc = 0;
+                    S.acc.dunc = 0;
                     S.phase = PH_KICK_PICK;
                 }
             }
@@ -2088,7 +2146,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
         }
         if (ph == PH_KICK_PICK) {
             if (tid == 0) {
-                S.unc += (long long)S.dunc;
+                S.unc += (long long)S.acc.dunc;
                 // the -1 ball appended newly uncovered words to the list
                 const int cnt = cov_ldcg(&d.st->ul_n);
                 if (S.ul_valid && cnt > d.ul_cap) S.ul_valid = 0;
@@ -2115,9 +2173,10 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 }
                 OpParams &o = S.opp;
                 leader_set_code(d, S, o.mi, pk);
+                S.code_gen++;
                 o.op = OP_BALL; o.sgn = +1; o.pc = pk; o.base = widx_pk(d, pk);
                 o.ul_valid = S.ul_valid;
-                S.dunc = 0;
+                S.acc.dunc = 0;
                 S.phase = PH_KICK_RECOMP;
             }
             __syncwarp();
@@ -2126,7 +2185,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
         }
         if (ph == PH_KICK_RECOMP) {
             if (tid == 0) {
-                S.unc += (long long)S.dunc;
+                S.unc += (long long)S.acc.dunc;
                 OpParams &o = S.opp;
                 o.op = OP_RECOMPUTE;
                 o.basen = o.base; o.pcn = o.pc;
@@ -2141,8 +2200,8 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
             if (tid == 0) {
                 const OpParams &o = S.opp;
                 int32_t *Pk = d.P + (size_t)o.mi * (d.n + 1);
-                cov_stcg(&Pk[0], S.accT);
-                for (int j = 0; j < d.n; j++) cov_stcg(&Pk[1 + j], S.accH[j]);
+                cov_stcg(&Pk[0], S.acc.accT);
+                for (int j = 0; j < d.n; j++) cov_stcg(&Pk[1 + j], S.acc.accH[j]);
                 S.kick_t++;
                 S.phase = PH_KICK_START;
             }
@@ -2176,10 +2235,11 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
                 uint64_t pk = pk_of_idx(d, (uint32_t)w);
                 int i = S.greedy_i;
                 leader_set_code(d, S, i, pk);
+                S.code_gen++;
                 OpParams &o = S.opp;
                 o.op = OP_BALL; o.sgn = +1; o.mi = i; o.pc = pk; o.base = (uint32_t)w;
                 o.ul_valid = 0;
-                S.dunc = 0;
+                S.acc.dunc = 0;
                 S.phase = PH_GREEDY_NEXT;
             }
             __syncwarp();
@@ -2188,7 +2248,7 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
         }
         if (ph == PH_GREEDY_NEXT) {
             if (tid == 0) {
-                S.unc += (long long)S.dunc;
+                S.unc += (long long)S.acc.dunc;
                 S.greedy_i++;
                 S.phase = PH_GREEDY;
             }
@@ -2209,10 +2269,17 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
 // One instantiation per private-count upkeep form (per-lane or warp-
 // aggregated commit), so that each is register-allocated on its own; a slot
 // runs in the one its adjust mode names.
+//
+// help_ctas > 0 (one slot, gh set): the clusters after the first are helper
+// CTAs of the first cluster's slot.  Each move's commit is then shared by
+// every CTA of the grid: the search cluster publishes the move in gh, the
+// helpers poll for it, take their share, add their sums to gh->acc and count
+// themselves done; the leader waits for them (every wait is bounded by the
+// launch deadline) before it reads the sums.
 template <bool WARP>
 __global__ void __launch_bounds__(NT, 1)
 cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluster_slot, int mode,
-               unsigned long long budget_ns, long long op_guard)
+               unsigned long long budget_ns, long long op_guard, GridHelp *gh, int help_ctas)
 {
     extern __shared__ __align__(16) unsigned char cov_smem[];
     Smem &S = *reinterpret_cast<Smem *>(cov_smem);
@@ -2220,10 +2287,57 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
     const int rank = (int)cl.block_rank();
     const int csize = (int)cl.num_blocks();
     const int cid = blockIdx.x / csize;
-    if (threadIdx.x == 0) S.slot = slots[cluster_slot[cid]];
+    const bool helper = help_ctas > 0 && cid > 0;
+    if (threadIdx.x == 0) S.slot = slots[cluster_slot[helper ? 0 : cid]];
     __syncwarp();
     cov_bar();
     const CovSlot &d = S.slot;
+    if (threadIdx.x == 0) { S.code_cached = d.M <= CODE_SM; S.code_gen = 0; }
+    if (helper) {
+        // the code mirror: loaded here, then each shared move applied and
+        // the whole code reloaded after other changes (kicks)
+        if (d.M <= CODE_SM)
+            for (int i = threadIdx.x; i < d.M; i += NT) S.code_sm[i] = cov_ldcg(&d.code[i]);
+        cov_bar();
+        const unsigned long long dl = (unsigned long long)cov_clock() +
+                                      (budget_ns + 1000000000ull) * COV_CYCLES_PER_NS;
+        unsigned seen = 0;
+        for (;;) {
+            if (threadIdx.x == 0) {
+                int got = 0;
+                // stop first: a helper that starts after the search cluster
+                // has left must not replay the last move
+                for (;;) {
+                    if (ld_acquire_u32((const unsigned *)&gh->stop)) break;
+                    const unsigned sq = ld_acquire_u32(&gh->seq);
+                    if (sq != seen) { seen = sq; got = 1; break; }
+                    if ((unsigned long long)cov_clock() > dl) { set_error(d, COV_ETIMEOUT); break; }
+                    __nanosleep(64);
+                }
+                if (got) {
+                    const unsigned *src = reinterpret_cast<const unsigned *>(&gh->op);
+                    unsigned *dst = reinterpret_cast<unsigned *>(&S.opl);
+                    for (int k = 0; k < (int)(sizeof(OpParams) / 4); k++) dst[k] = __ldcg(src + k);
+                    const int cg = __ldcg(&gh->code_gen);
+                    S.gh_reload = cg != S.code_gen;
+                    S.code_gen = cg;
+                }
+                S.gh_got = got;
+            }
+            cov_bar();
+            if (!S.gh_got) break;
+            if (S.gh_reload && d.M <= CODE_SM) {
+                for (int i = threadIdx.x; i < d.M; i += NT) S.code_sm[i] = cov_ldcg(&d.code[i]);
+                cov_bar();
+            }
+            op_move_t<WARP>(d, S.opl, S, &gh->acc, (int)blockIdx.x, (int)gridDim.x, true);
+            __threadfence();
+            cov_bar();
+            if (threadIdx.x == 0 && d.M <= CODE_SM) S.code_sm[S.opl.mi] = S.opl.pcn;
+            if (threadIdx.x == 0) atomicAdd(&gh->done, 1u);
+        }
+        return;
+    }
     const bool leader = rank == 0;
     Smem *LS = cl.map_shared_rank(&S, 0);
 
@@ -2245,6 +2359,8 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         S.t_deadline = (unsigned long long)cov_clock() + budget_ns * COV_CYCLES_PER_NS;
         S.guard = 0;
         S.opp.op = -1;
+        S.gh_seq = 0;
+        S.code_gen = 0;
         for (int k = 0; k < 24; k++) S.prof[k] = st->prof[k];
         S.ul_pairs = st->stat_ul_pairs;
     }
@@ -2270,8 +2386,18 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         const int op = P.op;
         if (op == OP_STOP) break;
         const long long top = cov_clock();
+        const bool shared_move = op == OP_MOVE && help_ctas > 0;
+        if (shared_move && leader && threadIdx.x == 0) {
+            // publish the move to the helpers (they are all done with the last one)
+            gh->done = 0;
+            gh->code_gen = S.code_gen;
+            const unsigned *src = reinterpret_cast<const unsigned *>(&P);
+            unsigned *dst = reinterpret_cast<unsigned *>(&gh->op);
+            for (int k = 0; k < (int)(sizeof(OpParams) / 4); k++) dst[k] = src[k];
+            st_release_u32(&gh->seq, ++S.gh_seq);
+        }
         if (op == OP_MOVE) {
-            op_move_t<WARP>(d, P, S, LS, rank, csize);
+            op_move_t<WARP>(d, P, S, &LS->acc, rank, csize + help_ctas, help_ctas > 0);
             if (d.M <= CODE_SM && threadIdx.x == 0) S.code_sm[P.mi] = P.pcn;
         } else if (op == OP_NEGWALK) {
             op_negwalk<WARP>(d, P, S, LS, rank, csize, cl);
@@ -2290,6 +2416,35 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
             op_rebuild_ul(d, rank, csize, cl);
         }
         cov_cbar(cl);
+        if (shared_move && leader) {
+            // the helpers' share: wait for all of them, then add their sums
+            if (threadIdx.x == 0) {
+                bool ok = true;
+                const long long tw = cov_clock();
+                S.prof[15] += tw - top;
+                while (ld_acquire_u32(&gh->done) < (unsigned)help_ctas) {
+                    if ((unsigned long long)cov_clock() > S.t_deadline + 1000000000ull * COV_CYCLES_PER_NS) {
+                        ok = false;
+                        break;
+                    }
+                }
+                S.prof[12] += cov_clock() - tw;
+                if (ok) {
+                    S.acc.dunc += __ldcg(&gh->acc.dunc);
+                    S.acc.accT += __ldcg(&gh->acc.accT);
+                    for (int j = 0; j < d.n; j++) S.acc.accH[j] += __ldcg(&gh->acc.accH[j]);
+                    gh->acc.dunc = 0;
+                    gh->acc.accT = 0;
+                    for (int j = 0; j < d.n; j++) gh->acc.accH[j] = 0;
+                } else {
+                    // a helper never answered: its share of the move may be
+                    // missing, so the state is no longer consistent
+                    S.status = COV_EDRIFT;
+                    S.phase = PH_STOPPED;
+                }
+            }
+            cov_bar();
+        }
         if (leader && threadIdx.x == 0) {
             const long long dt = cov_clock() - top;
             if (op == OP_MOVE) S.prof[4] += dt;
@@ -2299,6 +2454,7 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
     }
     // no CTA may leave while another can still read the leader's shared memory
     cov_cbar(cl);
+    if (help_ctas > 0 && leader && threadIdx.x == 0) st_release_u32((unsigned *)&gh->stop, 1u);
     if (leader && threadIdx.x == 0) {
         CovSlotState *st = d.st;
         rs_final(S, st->rng);
@@ -2588,6 +2744,11 @@ struct cov_pool {
     std::vector<Group> groups;
     std::vector<cudaStream_t> aux;
     std::vector<cudaEvent_t> ev;      // ev[0] fork, ev[1 + g] join of group g
+    // a pool with one slot: its moves' commits shared with helper CTAs on
+    // the SMs its cluster leaves free (0 off, else the most helper clusters)
+    int grid_help = 0;
+    GridHelp *d_gh = nullptr;
+    int help_clusters[17][2] = {};    // co-resident clusters - 1, per cluster size and form (+1: known)
     cudaStream_t cur_stream() const { return use_ext ? ext : stream; }
 };
 
@@ -2606,13 +2767,46 @@ static int ensure_attrs()
     return 0;
 }
 
+// helper clusters for a one-slot search at cluster size csize: as many as
+// can be resident beside the search cluster, at most pool->grid_help
+static int help_clusters(cov_pool *pool, int csize, int warp, int *out)
+{
+    *out = 0;
+    int &c = pool->help_clusters[csize][warp];
+    if (!c) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)csize);
+        cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = sizeof(Smem);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)csize;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        CK(cudaOccupancyMaxActiveClusters(&nc, warp ? cov_run_kernel<true> : cov_run_kernel<false>, &cfg));
+        c = 1 + std::max(0, nc - 1);
+    }
+    *out = std::min(c - 1, pool->grid_help);
+    return 0;
+}
+
 // one cluster per listed slot; d_list holds `count` slot indices on the device
 static int launch_kernel(cov_pool *pool, const int *d_list, int count, int csize, int warp, int mode,
                          long long moves, cudaStream_t stream)
 {
     if (count <= 0) return 0;
+    int help = 0;
+    if (pool->grid_help > 0 && count == 1 && pool->n_all == 1 && mode == MODE_SEARCH) {
+        int rc = help_clusters(pool, csize, warp, &help);
+        if (rc) return rc;
+    }
+    const int help_ctas = help * csize;
+    if (help_ctas) CK(cudaMemsetAsync(pool->d_gh, 0, sizeof(GridHelp), stream));
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(count * csize));
+    cfg.gridDim = dim3((unsigned)(count * csize + help_ctas));
     cfg.blockDim = dim3(NT);
     cfg.dynamicSmemBytes = sizeof(Smem);
     cfg.stream = stream;
@@ -2635,7 +2829,7 @@ static int launch_kernel(cov_pool *pool, const int *d_list, int count, int csize
     long long guard = mode == MODE_GREEDY ? 4 * mmax + 4096 : moves * (6 + 3LL * kmax) + 4096;
     CK(cudaLaunchKernelEx(&cfg, warp ? cov_run_kernel<true> : cov_run_kernel<false>,
                           (const CovSlot *)pool->d_slots, d_list, mode, budget_ns,
-                          guard));
+                          guard, pool->d_gh, help_ctas));
     CK(cudaGetLastError());
     return 0;
 }
@@ -2805,6 +2999,7 @@ int cov_pool_destroy(cov_pool *pool)
         if (pool->slots[s].used) cudaFree(pool->slots[s].arena);
     if (pool->gexec) cudaGraphExecDestroy(pool->gexec);
     cudaFree(pool->d_slots); cudaFree(pool->d_map); cudaFree(pool->d_all); cudaFree(pool->d_states);
+    cudaFree(pool->d_gh);
     for (cudaStream_t a : pool->aux) cudaStreamDestroy(a);
     for (cudaEvent_t e : pool->ev) cudaEventDestroy(e);
     cudaStreamDestroy(pool->stream);
@@ -3222,6 +3417,18 @@ int cov_pool_graph_run(cov_pool *pool, int64_t moves, int64_t target, int32_t st
 int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value)
 {
     if (!pool || !name) return COV_EINVAL;
+    if (!strcmp(name, "grid_help")) {
+        // a pool with one slot: share each move's commit with up to `value`
+        // helper clusters (0: off)
+        if (value < 0 || value > 1024) return COV_EINVAL;
+        CK(cudaStreamSynchronize(pool->cur_stream()));
+        if (value > 0 && !pool->d_gh) {
+            if (cudaMalloc(&pool->d_gh, sizeof(GridHelp)) != cudaSuccess) { cudaGetLastError(); return COV_ENOMEM; }
+        }
+        pool->grid_help = (int)value;
+        if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        return COV_OK;
+    }
     if (!strcmp(name, "neg_cluster_pairs")) {
         if (value < 0) return COV_EINVAL;
         pool->neg_cluster_pairs = value;

@@ -104,8 +104,11 @@ int cov_pool_set_budget(cov_pool *pool, double seconds);   /* per-launch wall li
 /* Tuning knob by name: "neg_cluster_pairs" (list x candidate pairs from
  * which the whole cluster shares the uncovered-list pass), "list_cost"
  * (weight of one uncovered-list entry against one walked word when the
- * entering side chooses between them, covsearch2e.c:1466-1467).  Neither
- * changes a trajectory. */
+ * entering side chooses between them, covsearch2e.c:1466-1467),
+ * "grid_help" (a pool with one slot: up to `value` helper clusters, on the
+ * SMs its cluster leaves free, share the commit of each move; 0 = off; the
+ * launch then holds the whole GPU and must not share it with other work).
+ * None changes a trajectory. */
 int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value);
 /* Per-slot setting by name: "cluster" (CTAs per instance, 1..16; slots of
  * each cluster size run as one launch, the launches of a step side by side),

@@ -162,3 +162,47 @@ def test_wide_variants_match_oracle(covlib, golden):
                             gpu=None if g1 is None else g1.tolist(), orc=None if o1 is None else o1.tolist()))
         pool.close()
     assert not bad, bad[:3]
+
+
+@pytest.mark.parametrize("cluster", [16, 8, 2])
+def test_grid_help_matches_oracle(covlib, golden, cluster):
+    """One instance whose move commits are shared with helper CTAs on the
+    rest of the GPU ("grid_help"): q7 n9 R4 M1500 (tenure 20) for 300 moves,
+    move by move against the oracle, then golden runs (R = 0 and 1
+    included) against the reference's fingerprints and the oracle's state."""
+    from oracle.pyoracle import Oracle
+    from coldcase_gb300.workloads import uniform_code
+    q, n, R, M = 7, 9, 4, 1500
+    code = uniform_code(q, n, M, 3)
+    o = Oracle(q, n, R, M, seed=3, tabu=20, threads=8)
+    o.init(code)
+    otr = o.run(300, trace=True)
+    pool = Pool(1, cluster=cluster)
+    pool.set_param("grid_help", 64)
+    s = pool.add(q, n, R, M, code=code, seed=3, tabu=20, trace=1, trace_cap=300)
+    for _ in range(3):
+        pool.run(100)
+    gtr = pool.trace(s)
+    k, g1, o1 = first_diff(gtr, otr)
+    assert pool.status(s)["status"] == 0
+    assert len(gtr) == len(otr) and k == len(otr), (k, g1, o1)
+    assert (pool.cnt(s) == o.cnt()).all() and (pool.best(s) == o.best()).all()
+    pool.close()
+    o.close()
+    runs, _ = golden
+    picked = [r for r in runs if r["R"] <= 1][:3] + [r for r in runs if r["R"] >= 2 and r["code"]][:3]
+    for r in picked:
+        pool = Pool(1, cluster=cluster)
+        pool.set_param("grid_help", 64)
+        code = code_from_text(r["code"], r["n"]) if r["code"] else None
+        s = pool.add(r["q"], r["n"], r["R"], r["M"], code=code, random_init=r["random_init"], seed=r["seed"],
+                     tabu=r["tabu"], kick=r["kick"], stall=r["stall"], trace=1, trace_cap=max(1, r["iters"]))
+        pool.run(r["iters"])
+        st = pool.status(s)
+        o, otr = oracle_run(r)
+        assert st["status"] == 0, (r, st)
+        assert (st["best"], st["it"], st["kicks"]) == (r["ref"]["uncovered"], r["ref"]["iters"], r["ref"]["kicks"])
+        assert pool.trace(s).tobytes() == otr.tobytes()
+        assert (pool.cnt(s) == o.cnt()).all() and (pool.tabu(s) == o.tabu()).all()
+        o.close()
+        pool.close()
