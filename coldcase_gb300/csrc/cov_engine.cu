@@ -1420,16 +1420,25 @@ __device__ long long leader_pick(const CovSlot &d, Smem &S)
         __syncwarp();
         return -1;
     }
-    // chunked linear scan from start
-    for (uint32_t off = 0; off < d.N; off += NT * 4) {
+    // chunked linear scan from start: PK consecutive counters per thread,
+    // all loaded before any is tested
+    constexpr int PK = 8;
+    for (uint32_t off = 0; off < d.N; off += NT * PK) {
         unsigned best = 0xffffffffu;
-        for (int k = 0; k < 4; k++) {
-            uint32_t o2 = off + (uint32_t)tid * 4 + k;
-            if (o2 >= d.N) break;
-            unsigned long long x = (unsigned long long)start + o2;
-            if (x >= d.N) x -= d.N;
-            if ((cov_ldcg(&d.cw[x]) & 0xffffu) == 0) { best = o2; break; }
+        uint32_t c[PK];
+#pragma unroll
+        for (int k = 0; k < PK; k++) {
+            const uint32_t o2 = off + (uint32_t)tid * PK + k;
+            c[k] = 1;
+            if (o2 < d.N) {
+                unsigned long long x = (unsigned long long)start + o2;
+                if (x >= d.N) x -= d.N;
+                c[k] = cov_ldcg(&d.cw[x]) & 0xffffu;
+            }
         }
+#pragma unroll
+        for (int k = PK - 1; k >= 0; k--)
+            if (c[k] == 0) best = off + (uint32_t)tid * PK + (uint32_t)k;
         best = block_min_u32(S, best);
         if (best != 0xffffffffu) {
             unsigned long long x = (unsigned long long)start + best;
