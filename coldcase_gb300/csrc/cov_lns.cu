@@ -98,10 +98,41 @@ struct MapGeom {
 // ----------------------------------------------------------- the maps -----
 // One axis over `nfib` lines of q elements at element stride st, held in
 // shared memory as R1 layers of E elements each.  Each thread owns whole
-// lines, so the update needs no synchronisation inside a pass.
-template <int R1>
+// lines, so the update needs no synchronisation inside a pass.  With the
+// alphabet size Q known at compile time a line's Q x R1 counts are read
+// once into registers (R1 loads and R1 - 1 stores per element, no division
+// by st); Q = 0 is the form for any q.
+template <int R1, int Q>
 __device__ __forceinline__ void map_axis(int32_t *Ls, uint32_t E, int q, uint32_t nfib, uint32_t st)
 {
+    if constexpr (Q > 0) {
+        // f / st by a float reciprocal: f < 2^24, so the estimate is off by
+        // at most one and one correction makes it exact
+        const float rinv = 1.0f / (float)st;
+        for (uint32_t f = threadIdx.x; f < nfib; f += blockDim.x) {
+            int o = (int)((float)f * rinv);
+            int i = (int)f - o * (int)st;
+            if (i < 0) { o--; i += (int)st; } else if (i >= (int)st) { o++; i -= (int)st; }
+            const uint32_t e0 = (uint32_t)o * st * (uint32_t)Q + (uint32_t)i;
+            int32_t v[Q][R1];
+#pragma unroll
+            for (int a = 0; a < Q; a++)
+#pragma unroll
+                for (int d = 0; d < R1; d++) v[a][d] = Ls[d * E + e0 + (uint32_t)a * st];
+            int32_t S[R1 > 1 ? R1 - 1 : 1];
+#pragma unroll
+            for (int d = 0; d < R1 - 1; d++) {
+                S[d] = 0;
+#pragma unroll
+                for (int a = 0; a < Q; a++) S[d] += v[a][d];
+            }
+#pragma unroll
+            for (int a = 0; a < Q; a++)
+#pragma unroll
+                for (int d = 1; d < R1; d++) Ls[d * E + e0 + (uint32_t)a * st] = v[a][d] + S[d - 1] - v[a][d - 1];
+        }
+        return;
+    }
     for (uint32_t f = threadIdx.x; f < nfib; f += blockDim.x) {
         const uint32_t o = f / st, i = f - o * st;
         const uint32_t e0 = o * st * (uint32_t)q + i;
@@ -146,12 +177,13 @@ __device__ __forceinline__ void map_out(int32_t *Ls, uint32_t E, uint32_t e, uin
 // [cnt == target] (cnt given) or as the layer-0 array (the code's word
 // counts); the higher layers start at 0.  With fin (k == n) the map is
 // written, else the layers.
-template <int R1>
+template <int R1, int Q>
 __global__ void __launch_bounds__(MAP_NT) k_map_low(MapGeom g, int k, const uint16_t *__restrict__ cnt, int target,
                                                     LayerPtrs L, int fin, int32_t *out, uint16_t *cnt16)
 {
     extern __shared__ __align__(16) int32_t Ls[];
-    const uint32_t T = g.pk[k];
+    uint32_t T = 1;
+    for (int j = 0; j < k; j++) T *= (uint32_t)g.q;
     const uint32_t ntile = g.N / T;
     for (uint32_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const uint32_t x0 = tile * T;
@@ -163,8 +195,9 @@ __global__ void __launch_bounds__(MAP_NT) k_map_low(MapGeom g, int k, const uint
             for (int d = 1; d < R1; d++) Ls[d * T + e] = 0;
         }
         __syncthreads();
-        for (int j = 0; j < k; j++) {
-            map_axis<R1>(Ls, T, g.q, T / (uint32_t)g.q, g.pk[j]);
+        uint32_t st = 1;
+        for (int j = 0; j < k; j++, st *= (uint32_t)g.q) {
+            map_axis<R1, Q>(Ls, T, g.q, T / (uint32_t)g.q, st);
             __syncthreads();
         }
         for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) map_out<R1>(Ls, T, e, x0 + e, fin, L, out, cnt16);
@@ -173,13 +206,16 @@ __global__ void __launch_bounds__(MAP_NT) k_map_low(MapGeom g, int k, const uint
 
 // Axes j0..j0+gsz-1 on strips: q^gsz rows (row r at stride s = q^j0) of
 // W = 2^lw consecutive words, element (r, c) at base + r*s + c.
-template <int R1>
+template <int R1, int Q>
 __global__ void __launch_bounds__(MAP_NT) k_map_high(MapGeom g, int j0, int gsz, int lw, LayerPtrs L, int fin,
                                                      int32_t *out, uint16_t *cnt16)
 {
     extern __shared__ __align__(16) int32_t Ls[];
     const uint32_t W = 1u << lw;
-    const uint32_t s = g.pk[j0], rows = g.pk[gsz], E = rows << lw;
+    uint32_t s = 1, rows = 1;
+    for (int j = 0; j < j0; j++) s *= (uint32_t)g.q;
+    for (int j = 0; j < gsz; j++) rows *= (uint32_t)g.q;
+    const uint32_t E = rows << lw;
     const uint32_t span = rows * s, outer = g.N / span;
     const uint32_t nstrip = (s + W - 1) >> lw;
     const unsigned long long ntiles = (unsigned long long)outer * nstrip;
@@ -196,8 +232,9 @@ __global__ void __launch_bounds__(MAP_NT) k_map_high(MapGeom g, int j0, int gsz,
             for (int d = 0; d < R1; d++) Ls[d * E + e] = c < w ? L.a[d][x] : 0;
         }
         __syncthreads();
-        for (int jj = 0; jj < gsz; jj++) {
-            map_axis<R1>(Ls, E, g.q, E / (uint32_t)g.q, g.pk[jj] << lw);
+        uint32_t st = W;
+        for (int jj = 0; jj < gsz; jj++, st *= (uint32_t)g.q) {
+            map_axis<R1, Q>(Ls, E, g.q, E / (uint32_t)g.q, st);
             __syncthreads();
         }
         for (uint32_t e = threadIdx.x; e < E; e += blockDim.x) {
@@ -599,12 +636,25 @@ int grid_of(uint32_t N)
 
 CovDeviceFlags g_map_attr;      // shared-memory opt-in of the map kernels, per device
 
+// alphabet sizes with their own map kernels (others run the Q = 0 form)
+#define MAP_Q_LIST(X) X(5) X(6) X(7) X(8)
+
+template <int R1, int Q>
+int map_attrs_rq()
+{
+    CK(cudaFuncSetAttribute(k_map_low<R1, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, MAP_SMEM_MAX));
+    CK(cudaFuncSetAttribute(k_map_high<R1, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, MAP_SMEM_MAX));
+    return 0;
+}
+
 template <int R1>
 int map_attrs_one()
 {
-    CK(cudaFuncSetAttribute(k_map_low<R1>, cudaFuncAttributeMaxDynamicSharedMemorySize, MAP_SMEM_MAX));
-    CK(cudaFuncSetAttribute(k_map_high<R1>, cudaFuncAttributeMaxDynamicSharedMemorySize, MAP_SMEM_MAX));
-    return 0;
+    int rc = map_attrs_rq<R1, 0>();
+#define MAP_ATTR_Q(QQ) if (!rc) rc = map_attrs_rq<R1, QQ>();
+    MAP_Q_LIST(MAP_ATTR_Q)
+#undef MAP_ATTR_Q
+    return rc;
 }
 
 int map_attrs()
@@ -628,7 +678,12 @@ template <int R1>
 int map_launch_low(int grid, size_t smem, const MapGeom &g, int k, const uint16_t *cnt, int target, LayerPtrs L,
                    int fin, int32_t *out, uint16_t *cnt16)
 {
-    k_map_low<R1><<<grid, MAP_NT, smem>>>(g, k, cnt, target, L, fin, out, cnt16);
+    switch (g.q) {
+#define MAP_LOW_Q(QQ) case QQ: k_map_low<R1, QQ><<<grid, MAP_NT, smem>>>(g, k, cnt, target, L, fin, out, cnt16); break;
+    MAP_Q_LIST(MAP_LOW_Q)
+#undef MAP_LOW_Q
+    default: k_map_low<R1, 0><<<grid, MAP_NT, smem>>>(g, k, cnt, target, L, fin, out, cnt16); break;
+    }
     CK(cudaGetLastError());
     return 0;
 }
@@ -637,7 +692,12 @@ template <int R1>
 int map_launch_high(int grid, size_t smem, const MapGeom &g, int j0, int gsz, int lw, LayerPtrs L, int fin,
                     int32_t *out, uint16_t *cnt16)
 {
-    k_map_high<R1><<<grid, MAP_NT, smem>>>(g, j0, gsz, lw, L, fin, out, cnt16);
+    switch (g.q) {
+#define MAP_HIGH_Q(QQ) case QQ: k_map_high<R1, QQ><<<grid, MAP_NT, smem>>>(g, j0, gsz, lw, L, fin, out, cnt16); break;
+    MAP_Q_LIST(MAP_HIGH_Q)
+#undef MAP_HIGH_Q
+    default: k_map_high<R1, 0><<<grid, MAP_NT, smem>>>(g, j0, gsz, lw, L, fin, out, cnt16); break;
+    }
     CK(cudaGetLastError());
     return 0;
 }
