@@ -2523,6 +2523,7 @@ __global__ void k_mark_balls(CovSlot d, int first, int count, int sgn)
 // counts the reference's shared-sphere walk (covsearch2e.c:592-654)
 // produces for k.  ul_bit must be clear beforehand.
 
+template <int Q>
 __global__ void __launch_bounds__(BT_NT) k_build_state(CovSlot d, unsigned long long *zeros)
 {
     extern __shared__ __align__(16) unsigned char bt_raw[];
@@ -2541,8 +2542,8 @@ __global__ void __launch_bounds__(BT_NT) k_build_state(CovSlot d, unsigned long 
     }
     for (uint32_t x = threadIdx.x; x < T; x += BT_NT) tile[x] = 0;
     BtScratch sc{lpc, lid, lbase, gcnt, gpos, gfill};
-    bt_mark_tile(tile, d.q, d.n, R, d.M, d.code, d.pw, nh, nl, d.bt_items, d.bt_last, d.bt_v, hp, sc,
-                 [](uint32_t id) { return cov_cw_unit((int)id); });
+    bt_mark_tile<Q>(tile, d.q, d.n, R, d.M, d.code, d.pw, nh, nl, d.bt_items, d.bt_last, d.bt_v, hp, sc,
+                    [](uint32_t id) { return cov_cw_unit((int)id); });
 
     uint32_t *gout = d.cw + (size_t)blockIdx.x * T;
     unsigned long long z = 0;
@@ -2771,7 +2772,11 @@ static int ensure_attrs()
     CK(cudaFuncSetAttribute(cov_run_kernel<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     CK(cudaFuncSetAttribute(cov_run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem)));
     CK(cudaFuncSetAttribute(cov_run_kernel<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    CK(cudaFuncSetAttribute(k_build_state, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem_bytes(BT_MAX)));
+    CK(cudaFuncSetAttribute(k_build_state<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem_bytes(BT_MAX)));
+#define BS_ATTR_Q(QQ) \
+    CK(cudaFuncSetAttribute(k_build_state<QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem_bytes(BT_MAX)));
+    BT_Q_LIST(BS_ATTR_Q)
+#undef BS_ATTR_Q
     g_attr_done.set(dev);
     return 0;
 }
@@ -3302,7 +3307,13 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
     CK(cudaMemsetAsync(d.P, 0, (size_t)M * (n + 1) * 4, st));
     CK(cudaMemsetAsync(d.ul_bit, 0, (size_t)((N + 31) / 32) * 4, st));
     CK(cudaMemsetAsync(d.zb, 0, (size_t)((N + 31) / 32) * 4, st));
-    k_build_state<<<(unsigned)ipow_h(q, d.bt_nh), BT_NT, bt_smem_bytes(d.bt_tw), st>>>(d, d_z);
+    switch (q) {
+#define BS_LAUNCH_Q(QQ) \
+    case QQ: k_build_state<QQ><<<(unsigned)ipow_h(q, d.bt_nh), BT_NT, bt_smem_bytes(d.bt_tw), st>>>(d, d_z); break;
+    BT_Q_LIST(BS_LAUNCH_Q)
+#undef BS_LAUNCH_Q
+    default: k_build_state<0><<<(unsigned)ipow_h(q, d.bt_nh), BT_NT, bt_smem_bytes(d.bt_tw), st>>>(d, d_z); break;
+    }
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(d.best, d.code, (size_t)M * 8, cudaMemcpyDeviceToDevice, st));
     unsigned long long zl[2] = {0, 0};

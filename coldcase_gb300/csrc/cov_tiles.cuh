@@ -88,17 +88,25 @@ struct BtScratch {
     int *gcnt, *gpos, *gfill;  // [COV_MAXN + 2] per radius: count, start, fill
 };
 
+// alphabet sizes with their own tile-marking kernels (others run Q = 0)
+#define BT_Q_LIST(X) X(5) X(6) X(7) X(8)
+
 // Mark into `tile` (zeroed by the caller) the balls of codewords 0..M-1
 // (packed, code[]) intersecting the tile with high digits hp; inc(id) is the
 // value added per covered word; items/last/vcum are bt_items_h's groups.
-// Every thread of the CTA (BT_NT) calls it.
-template <class Inc>
+// Q > 0: the alphabet size at compile time (the loop over a group's last
+// position unrolled); Q = 0: any q.  Every thread of the CTA (BT_NT) calls it.
+template <int Q, class Inc>
 __device__ void bt_mark_tile(uint32_t *tile, int q, int n, int R, int M, const uint64_t *__restrict__ code,
-                             const uint32_t *pw, int nh, int nl, const uint64_t *__restrict__ items,
+                             const uint32_t *pw_in, int nh, int nl, const uint64_t *__restrict__ items,
                              const uint8_t *__restrict__ last, const uint32_t *vcum, uint64_t hp,
                              const BtScratch &sc, Inc inc)
 {
     constexpr int PER = BT_LCH / BT_NT;
+    // the word strides in shared memory: indexed by position in the inner loop
+    __shared__ uint32_t pw[COV_MAXN];
+    if (threadIdx.x < COV_MAXN) pw[threadIdx.x] = threadIdx.x < (unsigned)n ? pw_in[threadIdx.x] : 0u;
+    __syncthreads();
     const int rmax = min(R, nl);
     const uint64_t hmask = (1ull << (4 * nh)) - 1;   // nh <= 15
     for (int m0 = 0; m0 < M; m0 += BT_LCH) {
@@ -168,8 +176,14 @@ __device__ void bt_mark_tile(uint32_t *tile, int q, int n, int R, int M, const u
                     const int step = (int)pw[lj];
                     const int cj = cov_nib(pc, lj);
                     int o2 = off - cj * step;
-                    for (int v = 0; v < q; v++, o2 += step)
-                        if (v != cj) atomicAdd(&tile[o2], add);
+                    if constexpr (Q > 0) {
+#pragma unroll
+                        for (int v = 0; v < Q; v++, o2 += step)
+                            if (v != cj) atomicAdd(&tile[o2], add);
+                    } else {
+                        for (int v = 0; v < q; v++, o2 += step)
+                            if (v != cj) atomicAdd(&tile[o2], add);
+                    }
                 }
             }
         }

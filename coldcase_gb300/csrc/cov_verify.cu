@@ -369,6 +369,7 @@ struct CountGeom {
 // cnt[x] = #{i : d(x, c_i) <= R} saturated at 65535 (the cnt[] of
 // covsearch2e.c:958-967, the OUT=2 map of cov/gemm2/dct.cu:360-411), one CTA
 // per tile (cov_tiles.cuh); the tile's uncovered words are counted too.
+template <int Q>
 __global__ void __launch_bounds__(BT_NT) k_count_tiles(CountGeom g, const uint64_t *__restrict__ code,
                                                        const uint64_t *__restrict__ items, uint16_t *cnt,
                                                        unsigned long long *zeros)
@@ -386,7 +387,7 @@ __global__ void __launch_bounds__(BT_NT) k_count_tiles(CountGeom g, const uint64
     }
     for (uint32_t x = threadIdx.x; x < g.tw; x += BT_NT) tile[x] = 0;
     BtScratch sc{lpc, lid, lbase, gcnt, gpos, gfill};
-    bt_mark_tile(tile, g.q, g.n, g.R, g.M, code, g.pw, g.nh, g.nl, items,
+    bt_mark_tile<Q>(tile, g.q, g.n, g.R, g.M, code, g.pw, g.nh, g.nl, items,
                  reinterpret_cast<const uint8_t *>(items + g.nitems), g.vcum, hp, sc,
                  [](uint32_t) { return 1u; });
     unsigned long long z = 0;
@@ -561,12 +562,28 @@ int geom(int q, int n, DtGeom &g)
 CovDeviceFlags g_dt_attr;   // shared-memory opt-in of the transform kernels, per device
 CovDeviceFlags g_ct_attr;   // the same for the tile count
 
+// the tile count of the alphabet size q (a kernel of its own for q = 5..8)
+void ct_launch(int q, unsigned grid, size_t smem, cudaStream_t st, const CountGeom &g, const uint64_t *code,
+               const uint64_t *items, uint16_t *cnt)
+{
+    switch (q) {
+#define CT_LAUNCH_Q(QQ) case QQ: k_count_tiles<QQ><<<grid, BT_NT, smem, st>>>(g, code, items, cnt, nullptr); break;
+    BT_Q_LIST(CT_LAUNCH_Q)
+#undef CT_LAUNCH_Q
+    default: k_count_tiles<0><<<grid, BT_NT, smem, st>>>(g, code, items, cnt, nullptr); break;
+    }
+}
+
 int ct_attrs()
 {
     int dev = 0;
     if (g_ct_attr.done(dev)) return 0;
-    CK(cudaFuncSetAttribute(k_count_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CK(cudaFuncSetAttribute(k_count_tiles<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)bt_smem_bytes(BT_MAX)));
+#define CT_ATTR_Q(QQ) \
+    CK(cudaFuncSetAttribute(k_count_tiles<QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_smem_bytes(BT_MAX)));
+    BT_Q_LIST(CT_ATTR_Q)
+#undef CT_ATTR_Q
     g_ct_attr.set(dev);
     return 0;
 }
@@ -808,7 +825,7 @@ int cov_count_dev(int32_t q, int32_t n, int32_t R, const uint8_t *d_code, int32_
         k_pack_code<<<std::min(1024, (M + 255) / 256), 256, 0, st>>>(d_code, M, n, d_pk);
         CK(cudaGetLastError());
     }
-    k_count_tiles<<<(unsigned)ipw(q, g.nh), BT_NT, bt_smem_bytes(g.tw), st>>>(g, d_pk, d_items, d_cnt, nullptr);
+    ct_launch(q, (unsigned)ipw(q, g.nh), bt_smem_bytes(g.tw), st, g, d_pk, d_items, d_cnt);
     CK(cudaGetLastError());
     // items is pageable host memory: wait before it goes out of scope
     CK(cudaStreamSynchronize(st));
@@ -903,7 +920,7 @@ int cov_finish(int32_t q, int32_t n, int32_t R, int32_t M, const uint8_t *code, 
     if (e == cudaSuccess && m0 > 0) e = cudaMemcpy(d_code, pk.data(), (size_t)m0 * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(d_z, 0, 8);
     if (e != cudaSuccess) return done(-(100 + (int)e));
-    k_count_tiles<<<(unsigned)ipw(q, g.nh), BT_NT, bt_smem_bytes(g.tw)>>>(g, d_code, d_ti, d_cnt, nullptr);
+    ct_launch(q, (unsigned)ipw(q, g.nh), bt_smem_bytes(g.tw), 0, g, d_code, d_ti, d_cnt);
     e = cudaGetLastError();
     if (e == cudaSuccess && m0 < M) {
         k_topup<<<1, 512>>>(fg, d_cnt, d_code, m0, d_bi, d_bl);
