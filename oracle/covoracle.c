@@ -7,8 +7,9 @@
  *
  * The algorithm is that of cov/engine/covsearch2e.c run as
  * `--preset p5b` (opt_hoist=1, opt_st=2, opt_eval=2; covsearch2e.c:1090),
- * with or without --wide (orc_set_wide) and --fix0 (orc_set_fix0), without
- * --sa, --noise, --ucache or --upick.  Each function
+ * with or without --wide (orc_set_wide), --fix0 (orc_set_fix0), --sa
+ * (orc_set_sa) and --noise (orc_set_noise), without --ucache or --upick.
+ * Each function
  * names the reference lines it restates.  Everything that decides the search
  * trajectory -- RNG consumption order, candidate order, tie-breaking, tabu
  * arithmetic -- is reproduced exactly; what only affects speed (offset
@@ -20,6 +21,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
+#include <math.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -83,6 +85,9 @@ struct cov_oracle {
     int tenure, kick, cand, threads;
     int wide;                       /* --wide: all n(q-1) moves per codeword */
     int fix0;                       /* --fix0: codeword 0 translated to 0^n and frozen */
+    int sa;                         /* --sa: focused simulated annealing (covsearch2e.c:1408-1441) */
+    double sa_t0, sa_cool, sa_tmin, sa_T;   /* --t0 --cool --tmin and the temperature */
+    int noise;                      /* --noise: per-mille of unevaluated moves (:1443-1448) */
     size_t cand_cap;                /* entries of ci/cp/cv/cd */
     long long stall;
     long long it, since_improve, nkicks;
@@ -639,20 +644,68 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
             }
             if (o->dv_ep[i] != ep) { o->dv_ep[i] = ep; o->cwl[ncw++] = i; }
         }
-        /* evaluation: covsearch2e.c:1455-1476 */
         int use_ul = o->ul_valid && ((long long)o->ul_n * n < (long long)(R + 1) * o->totpat);
-#pragma omp parallel for schedule(dynamic, 1) if (ncw > 1 && par_cand && o->threads > 1)
-        for (int z = 0; z < ncw; z++) {
+        if (o->sa) {
+            /* focused simulated annealing (covsearch2e.c:1408-1441): one
+             * random sampled move, its exact delta, Metropolis acceptance */
+            const int s2 = (int)orng_mod(&o->rng, (uint64_t)take);
+            const int i = o->ci[s2], p = o->cp[s2], v = o->cv[s2];
+            eval_codeword(o, i, u, o->offs + (size_t)i * n * q, o->dvec + (size_t)i * n * q, use_ul);
+            const long long d = o->dvec[((size_t)i * n + p) * q + v];
+            int accept;
+            if (d <= 0) accept = 1;
+            else {
+                const double pr = exp(-(double)d / o->sa_T);
+                accept = (double)(orng_next(&o->rng) >> 11) * 0x1.0p-53 < pr;
+            }
+            cov_move_rec rec;
+            memset(&rec, 0, sizeof rec);
+            rec.it = o->it; rec.u = uw; rec.delta = d; rec.ncand = ncand; rec.ncw = 1;
+            /* kicked: bit 1 the proposal was rejected, bit 0 the stall reheat */
+            rec.i = i; rec.p = p; rec.v = v; rec.kicked = accept ? 0 : 2;
+            if (accept) {
+                move_commit(o, i, p, v);
+                if (o->unc < o->best_unc) {
+                    o->best_unc = o->unc;
+                    memcpy(o->best, o->code, (size_t)M * n);
+                    o->since_improve = 0;
+                }
+            }
+            rec.unc = o->unc;
+            o->sa_T *= o->sa_cool;
+            if (o->sa_T < o->sa_tmin) o->sa_T = o->sa_t0;      /* reheat */
+            if (++o->since_improve > o->stall) {
+                o->sa_T = o->sa_t0;
+                o->since_improve = 0;
+                o->nkicks++;
+                rec.kicked |= 1;
+            }
+            rec.unc_end = o->unc;
+            rec.best = o->best_unc;
+            if (trace) trace[done - 1] = rec;
+            if (o->best_unc == 0) break;
+            continue;
+        }
+        int noisy = 0, ns = 0;
+        if (o->noise && (int)orng_mod(&o->rng, 1000) < o->noise) {
+            /* covsearch2e.c:1443-1448: a random sampled move, not evaluated */
+            noisy = 1;
+            ns = (int)orng_mod(&o->rng, (uint64_t)take);
+        }
+        /* evaluation: covsearch2e.c:1455-1476 */
+#pragma omp parallel for schedule(dynamic, 1) if (!noisy && ncw > 1 && par_cand && o->threads > 1)
+        for (int z = 0; z < (noisy ? 0 : ncw); z++) {
             int i = o->cwl[z];
             eval_codeword(o, i, u, o->offs + (size_t)i * n * q, o->dvec + (size_t)i * n * q, use_ul);
         }
-        for (int s = 0; s < take; s++)
+        for (int s = 0; s < (noisy ? 0 : take); s++)
             o->cd[s] = o->dvec[((size_t)o->ci[s] * n + o->cp[s]) * q + o->cv[s]];
 
         /* selection: covsearch2e.c:1503-1518 */
         long long bestd = 1LL << 60;
         int nties = 0, bi = -1, bp = -1, bv = -1, bs = -1;
-        for (int s = 0; s < take; s++) {
+        if (noisy) { bi = o->ci[ns]; bp = o->cp[ns]; bv = o->cv[ns]; bs = ns; }
+        for (int s = 0; s < (noisy ? 0 : take); s++) {
             int i = o->ci[s], p = o->cp[s], v = o->cv[s];
             long long d = o->cd[s];
             int is_tabu = o->tabu[((size_t)i * n + p) * q + v] > o->it;
@@ -667,9 +720,10 @@ long long orc_run(cov_oracle *o, long long max_moves, long long target, cov_move
             int s = (int)orng_mod(&o->rng, (uint64_t)take);
             bi = o->ci[s]; bp = o->cp[s]; bv = o->cv[s]; bs = s;
         }
-        long long chosen_d = o->cd[bs];
+        long long chosen_d = noisy ? 0 : o->cd[bs];
         int oldv = o->code[(size_t)bi * n + bp];
-        move_commit(o, bi, bp, bv);
+        const long long dunc = move_commit(o, bi, bp, bv);
+        if (noisy) chosen_d = dunc;
         o->tabu[((size_t)bi * n + bp) * q + oldv] = (int)(o->it + o->tenure + (long long)orng_mod(&o->rng, 4));
 
         cov_move_rec rec;
@@ -734,6 +788,22 @@ int orc_set_wide(cov_oracle *o, int wide)
         o->cand_cap = cap;
     }
     o->wide = wide ? 1 : 0;
+    return 0;
+}
+
+/* --sa --t0 --cool --tmin (covsearch2e.c:1034-1035, :1061-1064) */
+int orc_set_sa(cov_oracle *o, int sa, double t0, double cool, double tmin)
+{
+    o->sa = sa ? 1 : 0;
+    o->sa_t0 = t0; o->sa_cool = cool; o->sa_tmin = tmin; o->sa_T = t0;
+    return 0;
+}
+
+/* --noise PERMILLE (covsearch2e.c:1032, :1056) */
+int orc_set_noise(cov_oracle *o, int permille)
+{
+    if (permille < 0) return -1;
+    o->noise = permille;
     return 0;
 }
 

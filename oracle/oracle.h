@@ -71,6 +71,11 @@ int orc_set_wide(cov_oracle *o, int wide);
 /* --fix0 (covsearch2e.c:1241-1253): before orc_init; codeword 0 is moved to
  * 0^n by translating the whole code and never moves again.  -1 if M < 2. */
 int orc_set_fix0(cov_oracle *o, int fix0);
+/* --sa --t0 --cool --tmin: focused simulated annealing instead of the tabu
+ * selection (covsearch2e.c:1408-1441); --noise PERMILLE: that share of the
+ * moves is a random sampled move, not evaluated (:1443-1448) */
+int orc_set_sa(cov_oracle *o, int sa, double t0, double cool, double tmin);
+int orc_set_noise(cov_oracle *o, int permille);
 /* the uncovered-word list: valid flag and length, stale entries included */
 void orc_ul_state(const cov_oracle *o, int *valid, int *n);
 

@@ -57,6 +57,10 @@ def load():
     lib.orc_eval_codeword.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
     lib.orc_set_fix0.restype = ctypes.c_int
     lib.orc_set_fix0.argtypes = [P, ctypes.c_int]
+    lib.orc_set_sa.restype = ctypes.c_int
+    lib.orc_set_sa.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    lib.orc_set_noise.restype = ctypes.c_int
+    lib.orc_set_noise.argtypes = [P, ctypes.c_int]
     lib.orc_set_wide.restype = ctypes.c_int
     lib.orc_set_wide.argtypes = [P, ctypes.c_int]
     lib.orc_ul_state.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
@@ -102,7 +106,9 @@ class Oracle:
     """One restated covsearch2e p5b search (covsearch2e.c:1023-1621)."""
 
     def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000, threads=1,
-                 wide=False, fix0=False):
+                 wide=False, fix0=False, sa=None, noise=0):
+        """sa: None, or (t0, cool, tmin) for --sa --t0 --cool --tmin;
+        noise: --noise PERMILLE."""
         self.lib = load()
         self.q, self.n, self.R, self.M = q, n, R, M
         self.h = self.lib.orc_create(q, n, R, M, seed, tabu, kick, stall, cand, threads)
@@ -114,6 +120,11 @@ class Oracle:
         if fix0 and self.lib.orc_set_fix0(self.h, 1) != 0:
             self.close()
             raise ValueError("oracle: --fix0 needs M >= 2")
+        if sa is not None:
+            self.lib.orc_set_sa(self.h, 1, float(sa[0]), float(sa[1]), float(sa[2]))
+        if noise and self.lib.orc_set_noise(self.h, int(noise)) != 0:
+            self.close()
+            raise ValueError("oracle: bad --noise")
 
     def init(self, code=None, random_init=False):
         a = np.zeros((0, self.n), dtype=np.uint8) if code is None else \

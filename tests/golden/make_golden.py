@@ -16,6 +16,10 @@ Runs in the build container only (it needs the reference checkout):
                           with duplicates, malformed lines, too few and too
                           many words: COUNT line, exit status and --out file,
                           with and without --fast.
+  * method_runs.json   -- the reference engine's other move methods: --sa
+                          (simulated annealing, three cooling schedules)
+                          and --noise (two per-mille rates, with tabu,
+                          kicks, --wide and --fix0): fingerprint and --out.
   * opt_runs.json      -- the reference engine on the configurations of the
                           optimisation gate cov/opt/selftest.sh (p5b, with
                           and without --wide, and --fix0): fingerprint and
@@ -34,7 +38,7 @@ Runs in the build container only (it needs the reference checkout):
                           answer cases of cov/test_verify.py (whole space,
                           single word, perfect Hamming codes, direct sums).
 
-Usage: python3 tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT]
+Usage: python3 tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT] [--only methods]
 (default: $COLDCASE_REF, else /root/reference)
 """
 import argparse
@@ -269,6 +273,40 @@ def opt_runs(binary):
     return runs
 
 
+def method_runs(binary):
+    """The reference engine's other move methods: --sa (focused simulated
+    annealing, covsearch2e.c:1408-1441) at its default schedule and at fast
+    cooling schedules that reheat, with short stalls; --noise PERMILLE
+    (:1443-1448) with and without tabu, kicks, --wide and --fix0."""
+    runs = []
+    cfgs = [(6, 4, 2, 15, 3000), (7, 3, 1, 25, 3000), (2, 8, 2, 12, 3000), (6, 6, 3, 41, 2000),
+            (3, 4, 1, 9, 3000), (5, 4, 1, 125, 1500), (6, 5, 2, 60, 1500), (4, 6, 1, 420, 800)]
+    sa_sched = [(0.6, 0.999999, 0.02), (2.0, 0.995, 0.05), (1.0, 0.98, 0.3)]
+    for k, (q, n, R, M, it) in enumerate(cfgs):
+        for j, sch in enumerate(sa_sched):
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=11 + j, iters=it, tabu=0, stall=5000 if j == 0 else 300,
+                             kick=2, random_init=False, code=None, wide=False, fix0=(k == 3 and j == 1),
+                             sa=list(sch), noise=0))
+    for k, (q, n, R, M, it) in enumerate(cfgs):
+        for j, nz in enumerate((50, 300)):
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=21 + j, iters=it, tabu=0 if j == 0 else 6,
+                             stall=5000 if j == 0 else 60, kick=2, random_init=False, code=None,
+                             wide=(k % 3 == 1), fix0=(k == 0 and j == 1), sa=None, noise=nz))
+    for r in runs:
+        args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
+                "--threads", 1, "--tabu", r["tabu"], "--stall", r["stall"], "--kick", r["kick"]]
+        if r["wide"]:
+            args.append("--wide")
+        if r["fix0"]:
+            args.append("--fix0")
+        if r["sa"] is not None:
+            args += ["--sa", "--t0", repr(r["sa"][0]), "--cool", repr(r["sa"][1]), "--tmin", repr(r["sa"][2])]
+        if r["noise"]:
+            args += ["--noise", r["noise"]]
+        r["ref"] = run_ref(binary, args, r["code"])
+    return runs
+
+
 def sym_text(rep, q):
     """symsearch's --out file: orbit by orbit, its q words (j, e + j)."""
     return "".join(DIG[j] + "".join(DIG[(int(x) + j) % q] for x in e) + "\n" for e in rep for j in range(q))
@@ -315,9 +353,16 @@ def sym_runs(binary):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("COLDCASE_REF", "/root/reference"))
+    ap.add_argument("--only", choices=["methods"], help="write only this fixture")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=%s" % a.ref], check=True)
     binary = os.path.join(REPO, "oracle", "_ref", "covsearch2e")
+    mr = method_runs(binary)
+    with open(os.path.join(HERE, "method_runs.json"), "w") as f:
+        json.dump(mr, f)
+    if a.only == "methods":
+        print("method runs: %d" % len(mr))
+        return
     runs = engine_runs(binary)
     with open(os.path.join(HERE, "engine_runs.json"), "w") as f:
         json.dump(runs, f)

@@ -123,3 +123,27 @@ def test_opt_gate_runs_match_reference():
         if got != want or out != ref["out"] or po.verify_pure(words, r["q"], r["n"], r["R"]) != ref["uncovered"]:
             bad.append((r["q"], r["n"], r["R"], r["M"], r["seed"], r["wide"], got, want))
     assert not bad, bad
+
+
+def test_method_runs_match_reference():
+    """--sa (focused simulated annealing at three cooling schedules) and
+    --noise (two rates, with tabu, kicks, --wide and --fix0): the oracle's
+    fingerprint and --out file equal the reference engine's
+    (tests/golden/method_runs.json, made by tests/golden/make_golden.py)."""
+    import json
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    with open(os.path.join(here, "method_runs.json")) as f:
+        runs = json.load(f)
+    assert sum(1 for r in runs if r["sa"]) >= 20 and sum(1 for r in runs if r["noise"]) >= 10
+    bad = []
+    for r in runs:
+        o, _ = oracle_run(r)
+        ref = r["ref"]
+        got = (o.best_uncovered(), o.iters(), o.kicks())
+        want = (ref["uncovered"], ref["iters"], ref["kicks"])
+        out = codefile.format_code(codefile.distinct_code(o.best(), r["q"], r["n"], r["M"]), r["q"])
+        if got != want or out != ref["out"]:
+            bad.append((r["q"], r["n"], r["R"], r["M"], r["seed"], r["sa"], r["noise"], got, want, out == ref["out"]))
+        o.close()
+    assert not bad, bad
