@@ -9,13 +9,15 @@ exit status (0 iff the best code covers, 1 otherwise, 2 on bad arguments).
 
 The search is the p5b trajectory, with or without --wide (every
 single-coordinate move of each candidate codeword while the uncovered list
-is short, covsearch2e.c:1353-1376) and --fix0 (the initial code translated
+is short, covsearch2e.c:1353-1376), --fix0 (the initial code translated
 so that codeword 0 is 0^n, which then never moves, :1241-1253, :1343,
-:1560).  Presets base/p1..p5/p5b/best and the speed-only switches (--st
---eval --walk --hoist --early --pf --huge --threads) leave the trajectory
-unchanged in the reference (cov/opt/METHODS.md:395-409) and are accepted;
-the other switches that change the trajectory (--sa --noise --ucache
---upick) are rejected with exit status 2.
+:1560), --noise PERMILLE (that share of the moves taken from the sample
+unevaluated, :1443-1448) and --sa --t0 --cool --tmin (focused simulated
+annealing in place of the tabu selection, :1408-1441).  Presets
+base/p1..p5/p5b/best and the speed-only switches (--st --eval --walk --hoist
+--early --pf --huge --threads) leave the trajectory unchanged in the
+reference (cov/opt/METHODS.md:395-409) and are accepted; --ucache and
+--upick, which change the trajectory, are rejected with exit status 2.
 """
 import os
 import sys
@@ -38,13 +40,14 @@ VALUE_FLAGS = {"-q", "-n", "-R", "-M", "-t", "-s", "--in", "--out", "--cand", "-
                "--noise", "--iters", "--stall", "--threads", "--t0", "--cool", "--tmin", "--st",
                "--eval", "--walk", "--target", "--cpu", "--preset", "--cluster", "--chunk", "--grid-help"}
 SPEED_SWITCHES = {"--hoist", "--early", "--pf", "--huge"}
-TRAJECTORY_SWITCHES = {"--sa", "--ucache", "--upick"}
+TRAJECTORY_SWITCHES = {"--ucache", "--upick"}
 
 
 def parse(argv):
     a = dict(q=0, n=0, R=-1, M=0, t=60.0, s=12345, inp=None, out=None, cand=100000, tabu=0,
              kick=2, noise=0, iters=-1, stall=5000, random_init=False, quiet=False, target=-1,
-             cluster=None, chunk=0, wide=False, fix0=False, grid_help=0)
+             cluster=None, chunk=0, wide=False, fix0=False, grid_help=0, sa=False, t0=0.6, cool=0.999999,
+             tmin=0.02)
     i = 0
     while i < len(argv):
         f = argv[i]
@@ -63,6 +66,9 @@ def parse(argv):
             elif f == "--tabu": a["tabu"] = int(v)
             elif f == "--kick": a["kick"] = int(v)
             elif f == "--noise": a["noise"] = int(v)
+            elif f == "--t0": a["t0"] = float(v)
+            elif f == "--cool": a["cool"] = float(v)
+            elif f == "--tmin": a["tmin"] = float(v)
             elif f == "--iters": a["iters"] = int(v)
             elif f == "--stall": a["stall"] = int(v)
             elif f == "--target": a["target"] = int(v)
@@ -79,6 +85,8 @@ def parse(argv):
             a["wide"] = True
         elif f == "--fix0":
             a["fix0"] = True
+        elif f == "--sa":
+            a["sa"] = True
         elif f == "--quiet":
             a["quiet"] = True
         elif f in SPEED_SWITCHES:
@@ -90,9 +98,6 @@ def parse(argv):
             sys.stderr.write("unknown/incomplete option %s\n" % f)
             return None, 2
         i += 1
-    if a["noise"]:
-        sys.stderr.write("--noise changes the search trajectory and is not provided by the GPU engine\n")
-        return None, 2
     if a["q"] < 2 or a["n"] < 1 or a["R"] < 0 or a["M"] < 1:
         sys.stderr.write(USAGE)
         return None, 2
@@ -135,7 +140,8 @@ def main(argv=None):
     cluster = a["cluster"] or (8 if N >= 1 << 20 else 2)
     try:
         eng = Search(q, n, R, M, seed=a["s"], tabu=a["tabu"], kick=a["kick"], stall=a["stall"],
-                     cand=a["cand"], cluster=cluster, wide=a["wide"], fix0=a["fix0"])
+                     cand=a["cand"], cluster=cluster, wide=a["wide"], fix0=a["fix0"], noise=a["noise"],
+                     sa=(a["t0"], a["cool"], a["tmin"]) if a["sa"] else None)
         if a["grid_help"]:
             # this process's search takes the whole GPU: helper clusters share its commits
             eng.pool.set_param("grid_help", a["grid_help"])

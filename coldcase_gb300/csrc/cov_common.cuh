@@ -98,6 +98,9 @@ struct CovSlot {
                                  // while the list is valid and U_n n < (R+1) S'
     int wide_sliced;             // its list pass finds hits by bit-sliced counts (<= 64 candidates)
     int fix0;                    // --fix0: codeword 0 translated to 0^n and never moved (0 or 1)
+    int sa;                      // --sa: focused simulated annealing instead of the tabu selection
+    int noise;                   // --noise: per-mille of moves taken without evaluation
+    double sa_t0, sa_cool, sa_tmin;  // --t0 --cool --tmin
     // device arrays
     uint32_t *cw;                // [N]  cnt (bits 0-15) | sum of covering ids mod 2^16 (16-31)
     uint64_t *code;              // [M]  packed codewords
@@ -156,6 +159,7 @@ struct CovSlotState {
     // 0 pick, 1 candidates + sample, 2 entering side, 3 select, 4 move op
     // (commit + sphere), 5 finish, 6 list compaction, 7 other ops
     long long it_limit;          // iteration count at which the slot stops (-1: none)
+    double sa_T;                 // --sa: the temperature
     unsigned long long prof[24];   // 8..19: sub-phases (diagnostics: 11 RNG refill in the move op,
                                    // 12 wait for helper CTAs, 15 move op up to that wait); 20: sum of candidate
                                    // codewords, 21: sum of list lengths, 22: planned moves

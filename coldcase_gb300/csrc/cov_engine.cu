@@ -59,7 +59,7 @@ static_assert(RS % RS_CKI == 0 && (RS & (RS - 1)) == 0 && (RS_CKI & (RS_CKI - 1)
 enum { OP_STOP = 0, OP_MOVE, OP_NEGWALK, OP_BALL, OP_RECOMPUTE, OP_ZERO_TABU, OP_REBUILD_UL, OP_NEG };
 enum {
     PH_PLAN = 0, PH_SELECT, PH_FINISH_MOVE, PH_KICK_START, PH_KICK_PICK, PH_KICK_RECOMP,
-    PH_KICK_END, PH_KICK_DONE, PH_REBUILD_DONE, PH_GREEDY, PH_GREEDY_NEXT, PH_STOPPED
+    PH_KICK_END, PH_KICK_DONE, PH_REBUILD_DONE, PH_GREEDY, PH_GREEDY_NEXT, PH_STOPPED, PH_SA_END
 };
 enum { MODE_SEARCH = 0, MODE_GREEDY = 1 };
 
@@ -105,6 +105,10 @@ struct Smem {
     MoveAcc acc;               // leader accumulators (targets of DSMEM atomics)
     unsigned int gh_seq;       // moves published to the helpers (leader)
     int gh_got;                // helper: 1 a move to share, 0 leave
+    double sa_T;               // --sa temperature
+    int sa_p, sa_v;            // --sa: the proposed move of codeword L[0]
+    int sa_accept;             // --sa: the proposal was accepted
+    int noisy;                 // --noise: this move was taken without evaluation
     int code_cached;           // code_sm mirrors the code
     int code_gen;              // leader: codeword changes other than moves; helper: the last one seen
     int gh_reload;             // helper: reload code_sm before the move
@@ -1574,6 +1578,11 @@ __device__ void zero_acc(Smem &S)
     if (threadIdx.x < COV_MAXN) S.acc.accH[threadIdx.x] = 0;
 }
 
+__device__ void issue_move(const CovSlot &d, Smem &S, int k, uint64_t pk, int p, int v, long long dd);
+__device__ bool method_pick(const CovSlot &d, Smem &S, uint32_t *Lp);
+__device__ void write_trace(const CovSlot &d, Smem &S);
+__device__ void copy_best(const CovSlot &d);
+
 // Plan one iteration up to the point where the entering-side counts are
 // needed.  Returns with S.opp set.
 __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
@@ -1674,7 +1683,7 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         }
         nL += tot;
     }
-    const int Lsm = nL <= L_SM;
+    int Lsm = nL <= L_SM;
     uint32_t *Lp = Lsm ? S.L : d.g_list;
     // --wide (covsearch2e.c:1353-1376): while the list is valid and
     // U_n n < (R+1) S', the candidates are all n(q-1) moves of each
@@ -1741,6 +1750,21 @@ __device__ void leader_plan(const CovSlot &d, Smem &S, int csize)
         t0 = t1;
     }
     __syncwarp();
+    // --noise / --sa (covsearch2e.c:1408-1448): a move drawn from the sample
+    // before any evaluation.  A noisy move is committed as it is; an
+    // annealing proposal is evaluated alone (its codeword is the whole list)
+    if (d.sa || d.noise) {
+        cov_bar();
+        if (tid == 0) S.ibc[0] = method_pick(d, S, Lp) ? 1 : 0;
+        __syncwarp();
+        cov_bar();
+        if (S.noisy) return;                   // OP_MOVE issued
+        if (S.ibc[0]) {                         // --sa: the proposal's codeword alone
+            nL = 1;
+            Lsm = 1;
+            Lp = S.L;
+        }
+    }
     // entering side
     const int nsm = nL <= L_SM;
     int32_t *negp = nsm ? S.neg : d.g_neg;
@@ -1883,6 +1907,132 @@ __device__ __forceinline__ int cand_neg(const CovSlot &d, bool wide, const int32
     return wide ? cov_ldcg(&d.g_negw[(l * d.n + p) * d.q + v]) : negp[l * d.n + p];
 }
 
+// OP_MOVE of codeword k (packed pk) at position p to value v, evaluated
+// delta dd
+__device__ void issue_move(const CovSlot &d, Smem &S, int k, uint64_t pk, int p, int v, long long dd)
+{
+    S.chosen_delta = dd;
+    OpParams &o = S.opp;
+    o.op = OP_MOVE;
+    o.mi = k; o.mp = p; o.mv = v; o.sgn = 0;
+    o.ul_valid = S.ul_valid;
+    o.pc = pk;
+    o.base = widx_pk(d, pk);
+    const int oldv = cov_nib(pk, p);
+    o.dv = (uint32_t)((long long)(v - oldv) * (long long)d.pw[p]);
+    o.pcn = cov_setnib(pk, p, v);
+    o.basen = o.base + o.dv;
+    S.ibc[3] = oldv;
+    S.rec.i = k; S.rec.p = p; S.rec.v = v; S.rec.delta = dd;
+}
+
+// --noise and --sa, after the candidate sample (one thread).  --noise
+// (covsearch2e.c:1443-1448): with probability noise/1000 a sampled move is
+// committed unevaluated; the move is issued and S.noisy set.  --sa
+// (:1408-1414): one sampled move is proposed; its codeword becomes the whole
+// candidate list (L[0]) so that the entering side counts only its moves, and
+// true is returned.  The draws are the reference's, in its order.
+__device__ bool method_pick(const CovSlot &d, Smem &S, uint32_t *Lp)
+{
+    S.noisy = 0;
+    int s = -1;
+    if (d.sa) s = (int)fastmod(S, rs_take(S), (uint64_t)S.take);
+    else if ((int)fastmod(S, rs_take(S), 1000ull) < d.noise) {
+        S.noisy = 1;
+        s = (int)fastmod(S, rs_take(S), (uint64_t)S.take);
+    }
+    if (s < 0) return false;
+    apply_swaps(d, S);                          // the sample's order
+    const int psm = S.ncand <= PERM_CAP;
+    const uint32_t c = (psm ? S.perm : d.g_perm)[s];
+    const int l = (int)(c / (uint32_t)S.cpw), r = (int)(c - (uint32_t)l * S.cpw);
+    const int k = (int)Lp[l];
+    const uint64_t pk = cov_ldcg(&d.code[k]);
+    int p, v;
+    cand_pv(d, S.wide_now, r, pk, S.pu, p, v);
+    if (S.noisy) {
+        // the entering side is skipped, and with it the accumulators' reset
+        S.acc.dunc = 0;
+        S.acc.accT = 0;
+        for (int j = 0; j < COV_MAXN; j++) S.acc.accH[j] = 0;
+        issue_move(d, S, k, pk, p, v, 0);
+        S.phase = PH_FINISH_MOVE;
+        return false;
+    }
+    S.L[0] = (uint32_t)k;
+    S.Lpk[0] = pk;
+    S.nL = 1;
+    S.sa_p = p;
+    S.sa_v = v;
+    S.rec.ncw = 1;
+    return true;
+}
+
+// --sa (covsearch2e.c:1415-1420): the proposal's exact delta and the
+// Metropolis test; an accepted move is issued (one thread)
+__device__ void sa_decide(const CovSlot &d, Smem &S)
+{
+    const int k = (int)S.L[0], p = S.sa_p, v = S.sa_v;
+    const uint64_t pk = S.Lpk[0];
+    const int32_t *Pk = d.P + (size_t)k * (d.n + 1);
+    const long long dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - cand_neg(d, S.wide_now, S.neg, 0, p, v);
+    int accept = dd <= 0;
+    if (!accept) {
+        const double pr = exp(-(double)dd / S.sa_T);
+        accept = (double)(rs_take(S) >> 11) * 0x1.0p-53 < pr;
+    }
+    S.sa_accept = accept;
+    S.rec.i = k; S.rec.p = p; S.rec.v = v; S.rec.delta = dd;
+    if (accept) issue_move(d, S, k, pk, p, v, dd);
+    else S.opp.op = -1;
+    S.phase = PH_SA_END;
+}
+
+// --sa, after the proposal (covsearch2e.c:1421-1441): the accepted move's
+// bookkeeping (no tabu), the cooling schedule and the stall reheat
+__device__ void leader_sa_end(const CovSlot &d, Smem &S)
+{
+    const int tid = threadIdx.x;
+    const int n = d.n;
+    if (tid == 0) {
+        S.improved = 0;
+        S.rec.kicked = S.sa_accept ? 0 : 2;    // bit 1: rejected
+        if (S.sa_accept) {
+            const long long dunc = (long long)S.acc.dunc;
+            S.unc += dunc;
+            if (dunc != S.chosen_delta) S.status = COV_EDRIFT;
+            const OpParams &o = S.opp;
+            leader_set_code(d, S, o.mi, o.pcn);
+            int32_t *Pk = d.P + (size_t)o.mi * (n + 1);
+            cov_stcg(&Pk[0], cov_ldcg(&Pk[0]) + S.acc.accT);
+            for (int j = 0; j < n; j++) cov_stcg(&Pk[1 + j], cov_ldcg(&Pk[1 + j]) + S.acc.accH[j]);
+            S.improved = S.unc < S.best_unc;
+            if (S.improved) { S.best_unc = S.unc; S.since_improve = 0; }
+        }
+        S.rec.unc = S.unc;
+        S.sa_T *= d.sa_cool;
+        if (S.sa_T < d.sa_tmin) S.sa_T = d.sa_t0;            // reheat
+        if (++S.since_improve > d.stall) {
+            S.sa_T = d.sa_t0;
+            S.since_improve = 0;
+            S.nkicks++;
+            S.rec.kicked |= 1;                                // bit 0: the stall reheat
+        }
+    }
+    __syncwarp();
+    cov_bar();
+    if (S.improved) copy_best(d);
+    cov_bar();
+    if (tid == 0) {
+        S.rec.unc_end = S.unc;
+        S.rec.best = S.best_unc;
+        write_trace(d, S);
+        S.phase = PH_PLAN;
+    }
+    __syncwarp();
+    cov_bar();
+}
+
 // Deltas of the sampled candidates and the tabu/aspiration/reservoir
 // selection of covsearch2e.c:1503-1518; emits OP_MOVE.
 __device__ void leader_select(const CovSlot &d, Smem &S)
@@ -1901,6 +2051,11 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
     if (tid == 0) apply_swaps(d, S);
     __syncwarp();
     cov_bar();
+    if (d.sa) {
+        if (tid == 0) { sa_decide(d, S); S.prof[3] += cov_clock() - t0; }
+        __syncwarp();
+        return;
+    }
     // deltas and tabu flags in parallel (shared-memory case); the rare
     // oversized case recomputes them inside the serial scan below
     if (psm) {
@@ -2030,19 +2185,7 @@ __device__ void leader_select(const CovSlot &d, Smem &S)
         cand_pv(d, wide, rr, pk, pu, p, v);
         const int32_t *Pk = d.P + (size_t)k * (n + 1);
         long long dd = (cov_ldcg(&Pk[0]) - cov_ldcg(&Pk[1 + p])) - cand_neg(d, wide, negp, l, p, v);
-        S.chosen_delta = dd;
-        OpParams &o = S.opp;
-        o.op = OP_MOVE;
-        o.mi = k; o.mp = p; o.mv = v; o.sgn = 0;
-        o.ul_valid = S.ul_valid;
-        o.pc = pk;
-        o.base = widx_pk(d, pk);
-        int oldv = cov_nib(pk, p);
-        o.dv = (uint32_t)((long long)(v - oldv) * (long long)d.pw[p]);
-        o.pcn = cov_setnib(pk, p, v);
-        o.basen = o.base + o.dv;
-        S.ibc[3] = oldv;
-        S.rec.i = k; S.rec.p = p; S.rec.v = v; S.rec.delta = dd;
+        issue_move(d, S, k, pk, p, v, dd);
         S.phase = PH_FINISH_MOVE;
         S.prof[3] += cov_clock() - t0;
     }
@@ -2070,7 +2213,8 @@ __device__ void leader_finish_move(const CovSlot &d, Smem &S)
     if (tid == 0) {
         long long dunc = (long long)S.acc.dunc;
         S.unc += dunc;
-        if (dunc != S.chosen_delta) S.status = COV_EDRIFT;
+        if (S.noisy) S.rec.delta = dunc;        // --noise: the move was not evaluated
+        else if (dunc != S.chosen_delta) S.status = COV_EDRIFT;
         const OpParams &o = S.opp;
         leader_set_code(d, S, o.mi, o.pcn);
         int32_t *Pk = d.P + (size_t)o.mi * (n + 1);
@@ -2116,11 +2260,28 @@ __device__ void leader_step(const CovSlot &d, Smem &S, int csize)
             if (S.mode == MODE_GREEDY) { if (tid == 0) S.phase = PH_GREEDY; continue; }
             leader_plan(d, S, csize);
             cov_bar();
-            if (S.phase == PH_SELECT && S.opp.op == -1) { leader_select(d, S); cov_bar(); return; }
+            if (S.phase == PH_SELECT && S.opp.op == -1) {
+                leader_select(d, S);
+                cov_bar();
+                if (S.phase == PH_SA_END && S.opp.op == -1) continue;   // rejected proposal
+            }
             return;
         }
-        if (ph == PH_SELECT) { leader_select(d, S); cov_bar(); return; }
+        if (ph == PH_SELECT) {
+            leader_select(d, S);
+            cov_bar();
+            if (S.phase == PH_SA_END && S.opp.op == -1) continue;       // rejected proposal
+            return;
+        }
         if (ph == PH_FINISH_MOVE) { leader_finish_move(d, S); continue; }
+        if (ph == PH_SA_END) {
+            // a finished --sa iteration: a rejected proposal issues no op, so
+            // one step can run many iterations; each uses one move of the
+            // launch's budget, which bounds the loop
+            leader_sa_end(d, S);
+            guard = 0;
+            continue;
+        }
         if (ph == PH_REBUILD_DONE) {
             if (tid == 0) {
                 int cnt = cov_ldcg(&d.st->ul_n);
@@ -2370,6 +2531,9 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         S.opp.op = -1;
         S.gh_seq = 0;
         S.code_gen = 0;
+        S.noisy = 0;
+        S.sa_accept = 0;
+        S.sa_T = st->sa_T;
         for (int k = 0; k < 24; k++) S.prof[k] = st->prof[k];
         S.ul_pairs = st->stat_ul_pairs;
     }
@@ -2471,6 +2635,7 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
         st->since_improve = S.since_improve; st->nkicks = S.nkicks;
         st->moves_left = S.moves_left; st->trace_n = S.trace_n;
         st->ul_valid = S.ul_valid;
+        st->sa_T = S.sa_T;
         for (int k = 0; k < 24; k++) st->prof[k] = S.prof[k];
         st->stat_ul_pairs = S.ul_pairs;
         int s0 = atomicAdd(&st->status, 0);
@@ -3068,6 +3233,7 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     if (N >= (1LL << 32) - 1) return COV_EINVAL;
     if (prm->wide < 0 || prm->wide > 1) return COV_EINVAL;
     if (prm->fix0 < 0 || prm->fix0 > 1 || (prm->fix0 && prm->M < 2)) return COV_EINVAL;
+    if (prm->sa < 0 || prm->sa > 1) return COV_EINVAL;
     if (R > n) R = n;
     int s = -1;
     for (int k = 0; k < pool->max_slots; k++) if (!pool->slots[k].used) { s = k; break; }
@@ -3092,6 +3258,11 @@ static int slot_alloc(cov_pool *pool, const cov_params *prm, int cap, int *s_out
     d.list_cost = pool->list_cost;
     d.wide = prm->wide ? 1 : 0;
     d.fix0 = prm->fix0 ? 1 : 0;
+    d.sa = prm->sa ? 1 : 0;
+    d.noise = prm->noise;
+    d.sa_t0 = prm->t0;
+    d.sa_cool = prm->cool;
+    d.sa_tmin = prm->tmin;
     d.wide_sliced = 1;
     d.padj_warp = padj_auto(q, n, R, M);
     d.zbits = d.padj_warp;
@@ -3326,6 +3497,7 @@ static int slot_init(cov_pool *pool, int s, uint64_t seed, const uint8_t *code, 
     hs.best_unc = hs.unc;
     hs.target = -1;
     hs.it_limit = -1;
+    hs.sa_T = d.sa_t0;                   // --sa starts at --t0 (covsearch2e.c:1035)
     // the list is in use from the first move when the uncovered words are at
     // most half its capacity -- when the reference's first iteration would
     // rebuild it (covsearch2e.c:1326-1329)

@@ -13,11 +13,17 @@ from . import lib as L
 DEFAULTS = dict(seed=12345, tabu=0, kick=2, stall=5000, cand=100000)
 
 
+SA_DEFAULTS = (0.6, 0.999999, 0.02)     # --t0 --cool --tmin (covsearch2e.c:1035)
+
+
 def make_params(q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000,
-                trace=0, trace_cap=0, wide=False, fix0=False):
+                trace=0, trace_cap=0, wide=False, fix0=False, sa=None, noise=0):
+    """sa: None, or (t0, cool, tmin) for --sa; noise: --noise PERMILLE."""
+    t0, cool, tmin = SA_DEFAULTS if sa is None else sa
     return L.CovParams(q=q, n=n, R=R, M=M, seed=seed, tabu=tabu, kick=kick, cand=cand,
                        trace=1 if trace else 0, stall=stall, trace_cap=trace_cap if trace else 0,
-                       wide=1 if wide else 0, fix0=1 if fix0 else 0)
+                       wide=1 if wide else 0, fix0=1 if fix0 else 0, sa=0 if sa is None else 1,
+                       noise=int(noise), t0=float(t0), cool=float(cool), tmin=float(tmin))
 
 
 def slot_bytes(q, n, R, M, **kw):
@@ -56,11 +62,12 @@ class Pool:
                 "cov_pool_set_slot_param")
 
     def add(self, q, n, R, M, code=None, random_init=False, seed=12345, tabu=0, kick=2,
-            stall=5000, cand=100000, trace=0, trace_cap=0, wide=False, fix0=False):
+            stall=5000, cand=100000, trace=0, trace_cap=0, wide=False, fix0=False, sa=None, noise=0):
         """Create an instance from `code` (m x n digits; m may be <, = or > M).
-        `wide` and `fix0` are covsearch2e's --wide and --fix0."""
+        `wide`, `fix0` and `noise` are covsearch2e's --wide, --fix0 and
+        --noise; `sa` = (t0, cool, tmin) is --sa --t0 --cool --tmin."""
         p = make_params(q, n, R, M, seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand,
-                        trace=trace, trace_cap=trace_cap, wide=wide, fix0=fix0)
+                        trace=trace, trace_cap=trace_cap, wide=wide, fix0=fix0, sa=sa, noise=noise)
         if code is None:
             arr = np.zeros((0, n), dtype=np.uint8)
         else:
@@ -207,14 +214,15 @@ class Pool:
 class Search:
     """One covsearch2e instance on the GPU (a pool with a single slot).
 
-    Parameters are covsearch2e's: -q -n -R -M -s --tabu --kick --stall --cand --wide --fix0.
+    Parameters are covsearch2e's: -q -n -R -M -s --tabu --kick --stall --cand --wide --fix0,
+    --noise, and --sa --t0 --cool --tmin as sa=(t0, cool, tmin).
     """
 
     def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000,
-                 cluster=8, trace=0, trace_cap=0, budget_s=30.0, wide=False, fix0=False):
+                 cluster=8, trace=0, trace_cap=0, budget_s=30.0, wide=False, fix0=False, sa=None, noise=0):
         self.q, self.n, self.R, self.M = q, n, R, M
         self.kw = dict(seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand,
-                       trace=trace, trace_cap=trace_cap, wide=wide, fix0=fix0)
+                       trace=trace, trace_cap=trace_cap, wide=wide, fix0=fix0, sa=sa, noise=noise)
         self.pool = Pool(1, cluster=cluster, budget_s=budget_s)
         self.slot = None
 

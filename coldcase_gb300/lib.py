@@ -51,7 +51,8 @@ class CovParams(ctypes.Structure):
                 ("M", ctypes.c_int32), ("seed", ctypes.c_uint64), ("tabu", ctypes.c_int32),
                 ("kick", ctypes.c_int32), ("cand", ctypes.c_int32), ("trace", ctypes.c_int32),
                 ("stall", ctypes.c_int64), ("trace_cap", ctypes.c_int64), ("wide", ctypes.c_int32),
-                ("fix0", ctypes.c_int32)]
+                ("fix0", ctypes.c_int32), ("sa", ctypes.c_int32), ("noise", ctypes.c_int32),
+                ("t0", ctypes.c_double), ("cool", ctypes.c_double), ("tmin", ctypes.c_double)]
 
 
 class CovStatus(ctypes.Structure):

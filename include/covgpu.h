@@ -48,7 +48,9 @@ typedef struct {
     int32_t ncand;      /* candidate moves collected (:1359-1380)           */
     int32_t ncw;        /* distinct candidate codewords (:1458-1465)        */
     int32_t i, p, v;    /* committed move: codeword, position, new value    */
-    int32_t kicked;     /* 1 when the iteration ended in a kick             */
+    int32_t kicked;     /* 1 when the iteration ended in a kick; with --sa
+                           bit 0 is the stall reheat and bit 1 a rejected
+                           proposal (i, p, v, delta are the proposal's)   */
 } cov_move_rec;
 
 
@@ -83,6 +85,12 @@ typedef struct {
                            *         is 0^n and never move it
                            *         (covsearch2e.c:1241-1253, :1343, :1359,
                            *         :1560); 0 = off                        */
+    int32_t sa;           /* --sa    focused simulated annealing instead of
+                           *         the tabu selection (:1408-1441); 0 = off */
+    int32_t noise;        /* --noise per-mille of moves taken unevaluated
+                           *         (:1443-1448); 0 = off                  */
+    double t0, cool, tmin; /* --t0 --cool --tmin of --sa
+                           *         (reference defaults 0.6, 0.999999, 0.02) */
 } cov_params;
 
 typedef struct {

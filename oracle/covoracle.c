@@ -802,8 +802,7 @@ int orc_set_sa(cov_oracle *o, int sa, double t0, double cool, double tmin)
 /* --noise PERMILLE (covsearch2e.c:1032, :1056) */
 int orc_set_noise(cov_oracle *o, int permille)
 {
-    if (permille < 0) return -1;
-    o->noise = permille;
+    o->noise = permille;        /* any value: a nonzero one draws the coin */
     return 0;
 }
 

@@ -22,8 +22,9 @@ class OracleSearch:
     """The part of engine.Search the command line uses, on the oracle."""
 
     def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000, cluster=1, wide=False,
-                 fix0=False):
-        self.o = Oracle(q, n, R, M, seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand, wide=wide, fix0=fix0)
+                 fix0=False, sa=None, noise=0):
+        self.o = Oracle(q, n, R, M, seed=seed, tabu=tabu, kick=kick, stall=stall, cand=cand, wide=wide, fix0=fix0,
+                        sa=sa, noise=noise)
 
     def load(self, code=None, random_init=False):
         self.o.init(code, random_init=random_init)

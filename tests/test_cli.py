@@ -18,7 +18,7 @@ def run_cli(args, timeout=300):
                           timeout=timeout, cwd=REPO)
 
 
-@pytest.mark.parametrize("flag", ["--sa", "--ucache", "--upick"])
+@pytest.mark.parametrize("flag", ["--ucache", "--upick"])
 def test_trajectory_switches_refused(flag):
     r = run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", flag])
     assert r.returncode == 2 and "trajectory" in r.stderr
@@ -29,7 +29,6 @@ def test_bad_arguments_exit_2():
     assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", "--bogus"]).returncode == 2
     assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", "--preset", "p9"]).returncode == 2
     assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "70000"]).returncode == 2
-    assert run_cli(["-q", "4", "-n", "6", "-R", "1", "-M", "420", "--noise", "5"]).returncode == 2
 
 
 @pytest.mark.gpu
