@@ -118,3 +118,44 @@ def test_fix0_arguments_through_the_protocol():
             assert p.returncode == ref["rc"]
             with open(out) as f:
                 assert f.read() == ref["out"]
+
+
+def test_method_flags_through_the_protocol():
+    """--sa --t0 --cool --tmin and --noise reach the engine with the other
+    flags; RESULT line, exit status and --out file equal the reference
+    binary's (the oracle stands in for the GPU engine,
+    tests/portfolio_stub.py)."""
+    import json
+    stub = os.path.join(REPO, "tests", "portfolio_stub.py")
+    with open(os.path.join(REPO, "tests", "golden", "method_runs.json")) as f:
+        runs = json.load(f)
+    picked = [r for r in runs if r["sa"] and r["ref"]["iters"] > 100][:2] + \
+        [r for r in runs if r["noise"] and r["ref"]["iters"] > 100][:2]
+    for r in picked:
+        with tempfile.TemporaryDirectory() as td:
+            out = os.path.join(td, "out.txt")
+            args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
+                    "--tabu", r["tabu"], "--kick", r["kick"], "--stall", r["stall"], "--out", out, "--quiet"]
+            args += ["--wide"] if r["wide"] else []
+            args += ["--fix0"] if r["fix0"] else []
+            if r["sa"]:
+                args += ["--sa", "--t0", repr(r["sa"][0]), "--cool", repr(r["sa"][1]), "--tmin", repr(r["sa"][2])]
+            if r["noise"]:
+                args += ["--noise", r["noise"]]
+            p = subprocess.run([sys.executable, stub] + [str(a) for a in args], capture_output=True, text=True,
+                               timeout=300, cwd=REPO)
+            m = re.search(r"RESULT .*uncovered=(\d+) iters=(\d+) kicks=(\d+)", p.stdout)
+            assert m, p.stdout + p.stderr
+            ref = r["ref"]
+            assert (int(m.group(1)), int(m.group(2)), int(m.group(3))) == (ref["uncovered"], ref["iters"], ref["kicks"])
+            assert p.returncode == ref["rc"]
+            with open(out) as f:
+                assert f.read() == ref["out"]
+
+
+def test_gpu_only_flags_parse():
+    from coldcase_gb300 import covsearch_gpu as cg
+    a, rc = cg.parse(["-q", "7", "-n", "9", "-R", "4", "-M", "1500", "--grid-help", "64", "--sa", "--t0", "1.5",
+                      "--cool", "0.99", "--tmin", "0.1", "--noise", "20", "--cluster", "16"])
+    assert rc == 0 and a["grid_help"] == 64 and a["sa"] and (a["t0"], a["cool"], a["tmin"]) == (1.5, 0.99, 0.1)
+    assert a["noise"] == 20 and a["cluster"] == 16
