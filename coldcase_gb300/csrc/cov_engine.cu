@@ -94,6 +94,9 @@ struct GridHelp {
     unsigned int done;         // helper CTAs finished with the current move
     int stop;                  // the search cluster has left: helpers leave
     int code_gen;              // codeword changes other than moves (kicks) so far
+    int absent;                // test setting: the helpers leave at once, so
+                               // the leader's wait for them runs out
+    int pad2;
     OpParams op;
     MoveAcc acc;
 };
@@ -2463,6 +2466,7 @@ cov_run_kernel(const CovSlot *__restrict__ slots, const int *__restrict__ cluste
     cov_bar();
     const CovSlot &d = S.slot;
     if (threadIdx.x == 0) { S.code_cached = d.M <= CODE_SM; S.code_gen = 0; }
+    if (helper && __ldcg(&gh->absent)) return;
     if (helper) {
         // the code mirror: loaded here, then each shared move applied and
         // the whole code reloaded after other changes (kicks)
@@ -2922,6 +2926,7 @@ struct cov_pool {
     // a pool with one slot: its moves' commits shared with helper CTAs on
     // the SMs its cluster leaves free (0 off, else the most helper clusters)
     int grid_help = 0;
+    int grid_help_absent = 0;        // test setting (GridHelp::absent)
     GridHelp *d_gh = nullptr;
     int help_clusters[17][2] = {};    // co-resident clusters - 1, per cluster size and form (+1: known)
     cudaStream_t cur_stream() const { return use_ext ? ext : stream; }
@@ -2983,7 +2988,12 @@ static int launch_kernel(cov_pool *pool, const int *d_list, int count, int csize
         if (rc) return rc;
     }
     const int help_ctas = help * csize;
-    if (help_ctas) CK(cudaMemsetAsync(pool->d_gh, 0, sizeof(GridHelp), stream));
+    if (help_ctas) {
+        CK(cudaMemsetAsync(pool->d_gh, 0, sizeof(GridHelp), stream));
+        if (pool->grid_help_absent)
+            CK(cudaMemcpyAsync(&pool->d_gh->absent, &pool->grid_help_absent, sizeof(int), cudaMemcpyHostToDevice,
+                               stream));
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(count * csize + help_ctas));
     cfg.blockDim = dim3(NT);
@@ -3618,6 +3628,15 @@ int cov_pool_set_param(cov_pool *pool, const char *name, int64_t value)
             if (cudaMalloc(&pool->d_gh, sizeof(GridHelp)) != cudaSuccess) { cudaGetLastError(); return COV_ENOMEM; }
         }
         pool->grid_help = (int)value;
+        if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
+        return COV_OK;
+    }
+    if (!strcmp(name, "grid_help_absent")) {
+        // test setting: the helper clusters leave at once, so that the
+        // leader's bounded wait for them runs out (status COV_EDRIFT)
+        if (value < 0 || value > 1) return COV_EINVAL;
+        CK(cudaStreamSynchronize(pool->cur_stream()));
+        pool->grid_help_absent = (int)value;
         if (pool->gexec) { cudaGraphExecDestroy(pool->gexec); pool->gexec = nullptr; }
         return COV_OK;
     }

@@ -64,3 +64,28 @@ def test_host_side_refusals(covlib):
         pool.add(4, 6, 1, 50)               # pool full
     assert e.value.rc == -7
     pool.close()
+
+
+def test_grid_help_wait_runs_out(covlib):
+    """The leader's wait for its helper clusters is bounded: with the helpers
+    told to leave at once (a test setting), the wait runs out one second past
+    the launch budget, the slot reports COV_EDRIFT on the host (its state may
+    lack a share of a move), and the context stays usable."""
+    import time
+    q, n, R, M = 6, 7, 3, 74
+    pool = Pool(1, cluster=2, budget_s=0.05)
+    pool.set_param("grid_help", 64)
+    pool.set_param("grid_help_absent", 1)
+    s = pool.add(q, n, R, M, code=uniform_code(q, n, M, 9), seed=9)
+    t0 = time.monotonic()
+    pool.run(100)
+    st = pool.status(s)
+    assert st["status"] == -5 and st["it"] <= 1                 # COV_EDRIFT, after the first move
+    assert time.monotonic() - t0 < 30
+    pool.close()
+    other = Pool(1, cluster=2)
+    other.set_param("grid_help", 64)
+    o = other.add(q, n, R, M, code=uniform_code(q, n, M, 9), seed=9)
+    other.run(100)
+    assert other.status(o)["status"] == 0 and other.status(o)["it"] == 100
+    other.close()
