@@ -8,7 +8,8 @@
  * The algorithm is that of cov/engine/covsearch2e.c run as
  * `--preset p5b` (opt_hoist=1, opt_st=2, opt_eval=2; covsearch2e.c:1090),
  * with or without --wide (orc_set_wide), --fix0 (orc_set_fix0), --sa
- * (orc_set_sa) and --noise (orc_set_noise), without --ucache or --upick.
+ * (orc_set_sa), --noise (orc_set_noise) and --upick / --ucache
+ * (orc_set_pick).
  * Each function
  * names the reference lines it restates.  Everything that decides the search
  * trajectory -- RNG consumption order, candidate order, tie-breaking, tabu
@@ -88,6 +89,10 @@ struct cov_oracle {
     int sa;                         /* --sa: focused simulated annealing (covsearch2e.c:1408-1441) */
     double sa_t0, sa_cool, sa_tmin, sa_T;   /* --t0 --cool --tmin and the temperature */
     int noise;                      /* --noise: per-mille of unevaluated moves (:1443-1448) */
+    int upick;                      /* --upick: the oldest listed uncovered word (:978-985) */
+    int ucache;                     /* --ucache: a cache of uncovered words (:986-995, :1007-1012) */
+    long long ucbuf[4096];          /* the cache (UCCAP, covsearch2e.c:87-90) */
+    int ucn;
     size_t cand_cap;                /* entries of ci/cp/cv/cd */
     long long stall;
     long long it, since_improve, nkicks;
@@ -390,7 +395,12 @@ static long long move_commit(cov_oracle *o, int i, int p, int v)
         const uint8_t *ps = sp + (size_t)k * o->rs;
         SPHERE_SUBSET(o, ps, base, offs, {
             int ca = --o->cnt[w];
-            if (ca == 0) { dunc++; ul_add(o, w); }
+            if (ca == 0) {
+                dunc++;
+                /* --ucache: commits donate newly uncovered words (covsearch2e.c:460, :477) */
+                if (o->ucache && o->ucn < 4096) o->ucbuf[o->ucn++] = w;
+                ul_add(o, w);
+            }
             st_put(o, w, ca);
             int cb = ++o->cnt[w + dv];
             if (cb == 1) dunc--;
@@ -406,17 +416,39 @@ static long long move_commit(cov_oracle *o, int i, int p, int v)
 /* covsearch2e.c:973-1016 with opt_upick = opt_ucache = 0 */
 static long long pick_uncovered(cov_oracle *o)
 {
+    if (o->upick && o->ul_valid) {
+        /* --upick: the list is append-ordered, so its first uncovered entry
+         * has been uncovered longest (covsearch2e.c:978-985) */
+        for (int e = 0; e < o->ul_n; e++)
+            if (o->cnt[o->ul_idx[e]] == 0) return o->ul_idx[e];
+    }
+    if (o->ucache) {
+        /* --ucache: a random cache slot, covered entries discarded (:986-995) */
+        while (o->ucn > 0) {
+            int j = (int)(orng_next(&o->rng) % (uint64_t)o->ucn);
+            long long w = o->ucbuf[j];
+            o->ucbuf[j] = o->ucbuf[--o->ucn];
+            if (o->cnt[w] == 0) return w;
+        }
+    }
     for (int t = 0; t < 64; t++) {
         long long w = (long long)(orng_next(&o->rng) % (uint64_t)o->N);
         if (o->cnt[w] == 0) return w;
     }
     long long start = (long long)(orng_next(&o->rng) % (uint64_t)o->N);
+    long long found = -1;
     for (long long d = 0; d < o->N; d++) {
         long long w = start + d;
         if (w >= o->N) w -= o->N;
-        if (o->cnt[w] == 0) return w;
+        if (o->cnt[w] == 0) {
+            if (!o->ucache) return w;
+            /* --ucache: the scan goes on to fill the cache (:1007-1012) */
+            if (found < 0) found = w;
+            else if (o->ucn < 4096) o->ucbuf[o->ucn++] = w;
+            else break;
+        }
     }
-    return -1;
+    return found;
 }
 
 /* ------------------------------------------------------ lifecycle ------ */
@@ -803,6 +835,15 @@ int orc_set_sa(cov_oracle *o, int sa, double t0, double cool, double tmin)
 int orc_set_noise(cov_oracle *o, int permille)
 {
     o->noise = permille;        /* any value: a nonzero one draws the coin */
+    return 0;
+}
+
+/* --upick / --ucache (covsearch2e.c:1075-1076, :1145); set before orc_init */
+int orc_set_pick(cov_oracle *o, int upick, int ucache)
+{
+    o->upick = upick ? 1 : 0;
+    o->ucache = ucache ? 1 : 0;
+    o->ucn = 0;
     return 0;
 }
 

@@ -76,6 +76,9 @@ int orc_set_fix0(cov_oracle *o, int fix0);
  * moves is a random sampled move, not evaluated (:1443-1448) */
 int orc_set_sa(cov_oracle *o, int sa, double t0, double cool, double tmin);
 int orc_set_noise(cov_oracle *o, int permille);
+/* --upick (the oldest listed uncovered word) and --ucache (a cache of
+ * uncovered words filled by the scan and by commits), covsearch2e.c:978-1012 */
+int orc_set_pick(cov_oracle *o, int upick, int ucache);
 /* the uncovered-word list: valid flag and length, stale entries included */
 void orc_ul_state(const cov_oracle *o, int *valid, int *n);
 

@@ -61,6 +61,8 @@ def load():
     lib.orc_set_sa.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
     lib.orc_set_noise.restype = ctypes.c_int
     lib.orc_set_noise.argtypes = [P, ctypes.c_int]
+    lib.orc_set_pick.restype = ctypes.c_int
+    lib.orc_set_pick.argtypes = [P, ctypes.c_int, ctypes.c_int]
     lib.orc_set_wide.restype = ctypes.c_int
     lib.orc_set_wide.argtypes = [P, ctypes.c_int]
     lib.orc_ul_state.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
@@ -106,9 +108,9 @@ class Oracle:
     """One restated covsearch2e p5b search (covsearch2e.c:1023-1621)."""
 
     def __init__(self, q, n, R, M, seed=12345, tabu=0, kick=2, stall=5000, cand=100000, threads=1,
-                 wide=False, fix0=False, sa=None, noise=0):
+                 wide=False, fix0=False, sa=None, noise=0, upick=False, ucache=False):
         """sa: None, or (t0, cool, tmin) for --sa --t0 --cool --tmin;
-        noise: --noise PERMILLE."""
+        noise: --noise PERMILLE; upick / ucache: --upick / --ucache."""
         self.lib = load()
         self.q, self.n, self.R, self.M = q, n, R, M
         self.h = self.lib.orc_create(q, n, R, M, seed, tabu, kick, stall, cand, threads)
@@ -125,6 +127,8 @@ class Oracle:
         if noise and self.lib.orc_set_noise(self.h, int(noise)) != 0:
             self.close()
             raise ValueError("oracle: bad --noise")
+        if upick or ucache:
+            self.lib.orc_set_pick(self.h, 1 if upick else 0, 1 if ucache else 0)
 
     def init(self, code=None, random_init=False):
         a = np.zeros((0, self.n), dtype=np.uint8) if code is None else \

@@ -20,6 +20,9 @@ Runs in the build container only (it needs the reference checkout):
                           (simulated annealing, three cooling schedules)
                           and --noise (two per-mille rates, with tabu,
                           kicks, --wide and --fix0): fingerprint and --out.
+  * pick_runs.json     -- the reference engine's experimental pick rules
+                          --upick and --ucache (alone and together): the
+                          oracle's pinning for them (the GPU refuses them).
   * opt_runs.json      -- the reference engine on the configurations of the
                           optimisation gate cov/opt/selftest.sh (p5b, with
                           and without --wide, and --fix0): fingerprint and
@@ -38,7 +41,7 @@ Runs in the build container only (it needs the reference checkout):
                           answer cases of cov/test_verify.py (whole space,
                           single word, perfect Hamming codes, direct sums).
 
-Usage: python3 tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT] [--only methods]
+Usage: python3 tests/golden/make_golden.py [--ref REFERENCE_CHECKOUT] [--only methods|picks]
 (default: $COLDCASE_REF, else /root/reference)
 """
 import argparse
@@ -307,6 +310,30 @@ def method_runs(binary):
     return runs
 
 
+def pick_runs(binary):
+    """The reference engine's experimental pick rules, --upick (the oldest
+    listed uncovered word, covsearch2e.c:978-985) and --ucache (a cache of
+    uncovered words filled by the scan and by commits, :986-1012), alone and
+    together, with tabu and kicks."""
+    runs = []
+    cfgs = [(6, 4, 2, 15, 3000), (7, 3, 1, 25, 3000), (2, 8, 2, 12, 3000), (6, 6, 3, 41, 2000),
+            (3, 4, 1, 9, 3000), (6, 5, 2, 60, 1500), (4, 6, 1, 420, 800), (5, 6, 2, 120, 1500)]
+    for k, (q, n, R, M, it) in enumerate(cfgs):
+        for j, (up, uc) in enumerate(((1, 0), (0, 1), (1, 1))):
+            runs.append(dict(q=q, n=n, R=R, M=M, seed=31 + j, iters=it, tabu=0 if j != 1 else 6,
+                             stall=5000 if j == 0 else 80, kick=2, random_init=False, code=None, wide=False,
+                             fix0=False, upick=bool(up), ucache=bool(uc)))
+    for r in runs:
+        args = ["-q", r["q"], "-n", r["n"], "-R", r["R"], "-M", r["M"], "-s", r["seed"], "--iters", r["iters"],
+                "--threads", 1, "--tabu", r["tabu"], "--stall", r["stall"], "--kick", r["kick"]]
+        if r["upick"]:
+            args.append("--upick")
+        if r["ucache"]:
+            args.append("--ucache")
+        r["ref"] = run_ref(binary, args, r["code"])
+    return runs
+
+
 def sym_text(rep, q):
     """symsearch's --out file: orbit by orbit, its q words (j, e + j)."""
     return "".join(DIG[j] + "".join(DIG[(int(x) + j) % q] for x in e) + "\n" for e in rep for j in range(q))
@@ -353,10 +380,17 @@ def sym_runs(binary):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("COLDCASE_REF", "/root/reference"))
-    ap.add_argument("--only", choices=["methods"], help="write only this fixture")
+    ap.add_argument("--only", choices=["methods", "picks"], help="write only this fixture")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=%s" % a.ref], check=True)
     binary = os.path.join(REPO, "oracle", "_ref", "covsearch2e")
+    if a.only in (None, "picks"):
+        pr = pick_runs(binary)
+        with open(os.path.join(HERE, "pick_runs.json"), "w") as f:
+            json.dump(pr, f)
+        if a.only == "picks":
+            print("pick runs: %d" % len(pr))
+            return
     mr = method_runs(binary)
     with open(os.path.join(HERE, "method_runs.json"), "w") as f:
         json.dump(mr, f)

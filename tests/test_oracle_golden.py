@@ -147,3 +147,26 @@ def test_method_runs_match_reference():
             bad.append((r["q"], r["n"], r["R"], r["M"], r["seed"], r["sa"], r["noise"], got, want, out == ref["out"]))
         o.close()
     assert not bad, bad
+
+
+def test_pick_runs_match_reference():
+    """The experimental pick rules --upick and --ucache (alone and together,
+    with tabu and kicks): the oracle's fingerprint and --out file equal the
+    reference engine's (tests/golden/pick_runs.json).  The GPU engine
+    refuses these flags; the oracle restates them."""
+    import json
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    with open(os.path.join(here, "pick_runs.json")) as f:
+        runs = json.load(f)
+    bad = []
+    for r in runs:
+        o, _ = oracle_run(r)
+        ref = r["ref"]
+        got = (o.best_uncovered(), o.iters(), o.kicks())
+        want = (ref["uncovered"], ref["iters"], ref["kicks"])
+        out = codefile.format_code(codefile.distinct_code(o.best(), r["q"], r["n"], r["M"]), r["q"])
+        if got != want or out != ref["out"]:
+            bad.append((r["q"], r["n"], r["R"], r["M"], r["seed"], r["upick"], r["ucache"], got, want))
+        o.close()
+    assert not bad, bad

@@ -18,7 +18,8 @@ def oracle_run(run, threads=1):
     from oracle.pyoracle import Oracle
     o = Oracle(run["q"], run["n"], run["R"], run["M"], seed=run["seed"], tabu=run["tabu"],
                kick=run["kick"], stall=run["stall"], threads=threads, wide=run.get("wide", False),
-               fix0=run.get("fix0", False), sa=run.get("sa"), noise=run.get("noise", 0))
+               fix0=run.get("fix0", False), sa=run.get("sa"), noise=run.get("noise", 0),
+               upick=run.get("upick", False), ucache=run.get("ucache", False))
     code = code_from_text(run["code"], run["n"]) if run["code"] else None
     o.init(code, random_init=run["random_init"])
     tr = o.run(run["iters"], trace=True)
